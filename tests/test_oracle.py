@@ -1,0 +1,274 @@
+"""Pins the CPU oracle (oracle/oracle.c) against golden vectors produced by the
+reference's own code (tests/golden/make_golden.py) and against the known-answer
+constants that the reference's tests hold.  CPU only."""
+import hashlib
+
+import numpy as np
+import pytest
+
+import oracle as O
+
+
+def _sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def _check(out, summary):
+    assert out.size == summary["n"]
+    if "values" in summary:
+        assert out.reshape(-1).tolist() == summary["values"]
+    assert _sha(out) == summary["sha256"]
+
+
+# ---------------------------------------------------------------- KATs
+def test_known_answers_from_reference_tests(golden):
+    L = O.lib()
+    # test_two_adic.cpp:95  primitive 2^27-th root
+    assert L.orc_bb_two_adic_generator(27) == 440564289
+    # test_extension_field.cpp:76  dth_root
+    assert L.orc_bb4_dth_root() == 1728404513
+    k = golden["kat"]
+    assert k["bb_two_adic_27"] == 440564289
+    assert [L.orc_bb_two_adic_generator(i) for i in range(28)] == k["bb_two_adic"]
+    assert [L.orc_gl_two_adic_generator(i) for i in range(33)] == k["gl_two_adic"]
+    # two-adic generator orders
+    for bits in range(1, 28):
+        g = L.orc_bb_two_adic_generator(bits)
+        assert L.orc_bb_pow(g, 1 << bits) == 1
+        assert L.orc_bb_pow(g, 1 << (bits - 1)) != 1
+
+
+def test_mt19937_standard_values():
+    # The C++ standard's conformance values: the 10000th draw of a
+    # default-seeded (5489) mt19937 / mt19937_64.
+    assert int(O.mt19937(5489, 10000)[-1]) == 4123659995
+    assert int(O.mt19937_64(5489, 10000)[-1]) == 9981545732273789042
+
+
+def test_poseidon2_constants_match_reference(golden):
+    c = golden["consts"]
+    ini, ter, inr = O.example_constants_bb16()
+    assert ini.reshape(-1).tolist() == c["bb16_initial"]
+    assert ter.reshape(-1).tolist() == c["bb16_terminal"]
+    assert inr.tolist() == c["bb16_internal"]
+    ini, ter, inr = O.example_constants_gl8()
+    assert [int(x) for x in ini.reshape(-1)] == c["gl8_initial"]
+    assert [int(x) for x in ter.reshape(-1)] == c["gl8_terminal"]
+    assert [int(x) for x in inr] == c["gl8_internal"]
+
+
+def test_field_edge_values():
+    L = O.lib()
+    p = O.BB_P
+    for a in (0, 1, 2, p - 1, p - 2, 1 << 30, (1 << 31) - 1 - (1 << 27)):
+        for b in (0, 1, p - 1, 12345678):
+            assert L.orc_bb_add(a, b) == (a + b) % p
+            assert L.orc_bb_sub(a, b) == (a - b) % p
+            assert L.orc_bb_mul(a, b) == (a * b) % p
+        if a:
+            assert L.orc_bb_mul(a, L.orc_bb_inv(a)) == 1
+    q = O.GL_P
+    for a in (0, 1, q - 1, 1 << 63, (1 << 64) - 1 - q + 5, 0xFFFFFFFF):
+        for b in (0, 1, q - 1, 1 << 32):
+            assert L.orc_gl_add(a, b) == (a + b) % q
+            assert L.orc_gl_mul(a, b) == (a * b) % q
+            assert L.orc_gl_sub(a, b) == (a - b) % q
+
+
+def test_bb4_inverse_and_mul():
+    rng = np.random.default_rng(5)
+    for _ in range(20):
+        a = rng.integers(0, O.BB_P, 4, dtype=np.uint32)
+        if not a.any():
+            continue
+        assert O.bb4_mul(a, O.bb4_inv(a)).tolist() == [1, 0, 0, 0]
+
+
+# ---------------------------------------------------------------- DFT / LDE
+def test_dft_variants_vs_reference(golden):
+    for case in golden["dft"]:
+        m = O.bb_random_matrix(1 << case["log_h"], case["w"], case["seed"])
+        out = O.bb_dft(case["kind"], m, case["shift"])
+        _check(out, case["out"])
+
+
+def test_dft_known_answers():
+    # test_dft.cpp:410-451: DFT of e_k gives omega^{jk}; f(x)=1+2x at omega^j.
+    L = O.lib()
+    n, k = 8, 2
+    e = np.zeros((n, 1), np.uint32)
+    e[k, 0] = 1
+    out = O.bb_dft("dft", e)
+    om = L.orc_bb_two_adic_generator(3)
+    assert out[:, 0].tolist() == [L.orc_bb_pow(om, j * k) for j in range(n)]
+    c = np.array([[1], [2], [0], [0]], np.uint32)
+    out = O.bb_dft("dft", c)
+    om = L.orc_bb_two_adic_generator(2)
+    assert out[:, 0].tolist() == [(1 + 2 * L.orc_bb_pow(om, j)) % O.BB_P for j in range(4)]
+
+
+def test_lde_vs_reference(golden):
+    for case in golden["lde"]:
+        h = 1 << case["log_h"]
+        if case["field"] == "bb":
+            t = O.bb_random_matrix(h, case["w"], case["seed"])
+            out = O.bb_coset_lde(t, case["log_blowup"], case["shift"], bool(case["bitrev"]))
+        else:
+            t = O.gl_random_matrix(h, case["w"], case["seed"])
+            out = O.gl_coset_lde(t, case["log_blowup"], case["shift"], bool(case["bitrev"]))
+        _check(out, case["out"])
+
+
+def test_lde_threads_identical():
+    t = O.bb_random_matrix(1 << 9, 13, 4)
+    a = O.bb_coset_lde(t, 2, nthreads=1)
+    b = O.bb_coset_lde(t, 2, nthreads=4)
+    assert np.array_equal(a, b)
+
+
+def test_lde_low_degree_property():
+    # The LDE of h evaluations has degree < h: re-interpolating the natural-order
+    # LDE on the coset yields zero coefficients above h.
+    t = O.bb_random_matrix(1 << 5, 3, 9)
+    lde = O.bb_coset_lde(t, 2, shift=31, bitrev=False)
+    coeffs = O.bb_dft("coset_idft", lde, 31)
+    assert not coeffs[1 << 5:].any()
+
+
+# ---------------------------------------------------------------- Poseidon2 / sponge
+def _p2(kind):
+    return {"bb16": O.bb16_params, "bb16zero": O.bb16_zero_params,
+            "bb16zero_generic": O.bb16_zero_params, "gl8": O.gl8_params}[kind]()
+
+
+def test_permutation_vs_reference(golden):
+    for case in golden["perm"]:
+        p = _p2(case["kind"])
+        for i, o in zip(case["inputs"], case["outputs"]):
+            assert [int(x) for x in O.permute(p, np.array(i, dtype=np.uint64))] == o
+
+
+def test_generic_and_pod_poseidon2_agree(golden):
+    by = {c["kind"]: c for c in golden["perm"]}
+    assert by["bb16zero"]["outputs"] == by["bb16zero_generic"]["outputs"]
+
+
+def test_sponge_vs_reference(golden):
+    for case in golden["hash"]:
+        p = _p2(case["kind"])
+        if case["kind"] == "gl8":
+            data = O.gl_random_matrix(1, case["len"], case["seed"]) if case["len"] else np.zeros(0, np.uint64)
+        else:
+            data = O.bb_random_matrix(1, case["len"], case["seed"]) if case["len"] else np.zeros(0, np.uint32)
+        assert [int(x) for x in O.hash_iter(p, data)] == case["digest"]
+
+
+def test_sponge_edge_semantics_mock_free():
+    # padding_free_sponge.hpp:63-87: empty input -> zero digest without a
+    # permutation; a partial last chunk keeps the previous rate positions.
+    p = O.bb16_params()
+    assert not O.hash_iter(p, np.zeros(0, np.uint32)).any()
+    x = np.arange(1, 12, dtype=np.uint32)
+    st = np.zeros(16, np.uint32)
+    st[:8] = x[:8]
+    st = O.permute(p, st)
+    st[:3] = x[8:]
+    st = O.permute(p, st)
+    assert O.hash_iter(p, x).tolist() == st[:8].tolist()
+
+
+def test_compress_vs_reference(golden):
+    for case in golden["compress"]:
+        p = _p2(case["kind"])
+        if case["kind"] == "gl8":
+            m = O.gl_random_matrix(2, 4, case["seed"])
+        else:
+            m = O.bb_random_matrix(2, 8, case["seed"])
+        assert [int(x) for x in O.compress(p, m[0], m[1])] == case["digest"]
+
+
+# ---------------------------------------------------------------- Merkle
+def _mats(kind, shapes, seed):
+    out = []
+    for i, s in enumerate(shapes):
+        h, w = (int(v) for v in s.split("x"))
+        if kind == "gl8":
+            out.append(O.gl_random_matrix(h, w, seed + i))
+        else:
+            out.append(O.bb_random_matrix(h, w, seed + i))
+    return out
+
+
+def test_mixed_height_mmcs_vs_reference(golden):
+    for case in golden["mmcs"]:
+        p = _p2(case["kind"])
+        layers = O.mmcs_commit(p, _mats(case["kind"], case["shapes"], case["seed"]), case["cap_height"])
+        assert [len(l) for l in layers] == case["sizes"]
+        for got, want in zip(layers, case["layers"]):
+            assert [[int(x) for x in d] for d in got] == want
+
+
+def test_commit_matrix_vs_reference(golden):
+    p = O.bb16_params()
+    for case in golden["commit_matrix"]:
+        m = O.bb_random_matrix(case["h"], case["w"], case["seed"])
+        layers = O.commit_matrix(p, m)
+        assert [len(l) for l in layers] == case["sizes"]
+        for got, want in zip(layers, case["layers"]):
+            assert got.tolist() == want
+
+
+def test_lde_commit_vs_reference(golden):
+    p = O.bb16_params()
+    for case in golden["commit"]:
+        t = O.bb_random_matrix(1 << case["log_h"], case["w"], case["seed"])
+        lde = O.bb_coset_lde(t, case["log_blowup"], case["shift"], True)
+        layers = O.mmcs_commit(p, [lde], case["cap_height"])
+        assert [len(l) for l in layers] == case["sizes"]
+        assert layers[-1].tolist() == case["cap"]
+        assert _sha(np.concatenate([l.reshape(-1) for l in layers])) == case["layers_sha256"]
+
+
+def test_pcs_commit_vs_reference(golden):
+    p = O.bb16_params()
+    for case in golden["pcs_commit"]:
+        traces = []
+        for i, s in enumerate(case["shapes"]):
+            lh, w = (int(v) for v in s.split("x"))
+            traces.append(O.bb_random_matrix(1 << lh, w, case["seed"] + i))
+        root, _ = O.pcs_commit(p, traces, case["log_blowup"], case["shift"])
+        assert root.tolist() == case["root"]
+
+
+# ---------------------------------------------------------------- FRI fold
+def test_fold_vs_reference(golden):
+    for case in golden["fold"]:
+        lh = case["log_height"]
+        raw = O.mt19937(case["seed"], 4 * (1 << lh) + 4) % np.uint32(O.BB_P)
+        vals = raw[: 4 * (1 << lh)].reshape(-1, 4)
+        beta = case["beta"]
+        if case["beta_mode"] == 0:
+            assert raw[4 * (1 << lh):].tolist() == beta
+        out = O.fold_matrix_bb4(vals, lh, case["log_arity"], beta)
+        _check(out, case["out"])
+
+
+def test_fold_arity2_closed_form():
+    # For arity 2 the reference Lagrange formula equals
+    # (e0+e1)/2 + beta*(e0-e1)/(2x) (fri_fold_cuda.hpp:81-109).
+    L = O.lib()
+    p = O.BB_P
+    lh = 6
+    raw = O.mt19937(3, 4 * (1 << lh) + 4) % np.uint32(p)
+    vals = raw[:-4].reshape(-1, 4)
+    beta = raw[-4:]
+    out = O.fold_matrix_bb4(vals, lh, 1, beta)
+    inv2 = L.orc_bb_inv(2)
+    om = L.orc_bb_two_adic_generator(lh)
+    for i in range(1 << (lh - 1)):
+        x = L.orc_bb_pow(om, int("{:0{}b}".format(i, lh - 1)[::-1], 2) if lh > 1 else 0)
+        e0, e1 = vals[2 * i], vals[2 * i + 1]
+        s = [(int(a) + int(b)) * inv2 % p for a, b in zip(e0, e1)]
+        d = [(int(a) - int(b)) * inv2 % p * L.orc_bb_inv(x) % p for a, b in zip(e0, e1)]
+        bd = O.bb4_mul(beta, np.array(d, np.uint32))
+        assert out[i].tolist() == [(a + int(b)) % p for a, b in zip(s, bd)]
