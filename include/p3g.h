@@ -1,0 +1,180 @@
+/*
+ * p3g.h -- C ABI of the GB300 trace-commitment library (libp3g_gb300.so).
+ *
+ * Plain pointers and sizes only.  "d_" pointers are device (HBM) pointers on
+ * the context's GPU; "h_" pointers are host memory.  `stream` is a
+ * cudaStream_t (NULL = the legacy default stream).  Every call is
+ * stream-ordered and asynchronous unless it says it returns host data, in
+ * which case it synchronises `stream` before returning.
+ *
+ * Field elements are canonical little-endian integers: BabyBear
+ * (p = 2^31 - 2^27 + 1) as uint32, Goldilocks (p = 2^64 - 2^32 + 1) as uint64,
+ * BabyBear^4 = BabyBear[x]/(x^4 - 11) as 4 x uint32 (coefficient 0 first).
+ * Matrices are row-major (RowMajorMatrix, dense_matrix.hpp:21-293 of the
+ * reference).
+ *
+ * Errors: every function returns a P3G_* status; the message of the last
+ * failure on the calling thread is available from p3g_last_error().  There is
+ * no CPU fallback: a call either runs on the GPU or fails.
+ *
+ * Threading: a context is externally synchronised (one host thread at a
+ * time); distinct contexts are independent.
+ */
+#ifndef P3G_H
+#define P3G_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define P3G_API __attribute__((visibility("default")))
+#else
+#define P3G_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define P3G_VERSION 1
+
+enum p3g_status {
+    P3G_OK = 0,
+    P3G_EINVAL = 1,      /* bad argument (reference: std::invalid_argument) */
+    P3G_ENOMEM = 2,      /* device allocation failed */
+    P3G_ECUDA = 3,       /* CUDA runtime error (reference: P3_CUDA_CHECK runtime_error) */
+    P3G_ETIMEOUT = 4,    /* a bounded device or host wait ran out */
+    P3G_EUNSUPPORTED = 5,/* shape or parameter outside what this build supports */
+    P3G_ESTATE = 6       /* missing set-up (e.g. no Poseidon2 constants) */
+};
+
+enum p3g_field {
+    P3G_BABYBEAR = 0,
+    P3G_GOLDILOCKS = 1
+};
+
+typedef struct p3g_ctx p3g_ctx;
+typedef struct p3g_tree p3g_tree;
+
+/* ------------------------------------------------------------ basics */
+P3G_API int p3g_version(void);
+P3G_API const char *p3g_status_string(int status);
+/* Copies the calling thread's last error message (NUL-terminated). */
+P3G_API int p3g_last_error(char *buf, size_t len);
+
+/* Creates a context on `device`: root-of-unity tables, a stream-ordered
+ * device memory pool.  Replaces the per-call set-up of NttCuda
+ * (ntt_cuda.hpp:272-289) and build_merkle_tree_cuda (merkle_tree_cuda.hpp:360). */
+P3G_API int p3g_ctx_create(int device, p3g_ctx **out);
+P3G_API int p3g_ctx_destroy(p3g_ctx *ctx);
+P3G_API int p3g_stream_synchronize(p3g_ctx *ctx, void *stream);
+
+/* Stream-ordered allocations from the context pool (what the library itself
+ * uses for scratch and outputs), plus copies, so that callers without a CUDA
+ * runtime binding can drive the library. */
+P3G_API int p3g_malloc(p3g_ctx *ctx, size_t bytes, void **d_ptr, void *stream);
+P3G_API int p3g_free(p3g_ctx *ctx, void *d_ptr, void *stream);
+P3G_API int p3g_memcpy_h2d(p3g_ctx *ctx, void *d_dst, const void *h_src, size_t bytes, void *stream);
+P3G_API int p3g_memcpy_d2h(p3g_ctx *ctx, void *h_dst, const void *d_src, size_t bytes, void *stream);
+
+/* ------------------------------------------------------------ Poseidon2
+ * Sets the permutation used by the MMCS calls of `field`.  Replaces
+ * poseidon2::Poseidon2Cuda<F, WIDTH, ROUNDS_F, ROUNDS_P, D> (poseidon2_cuda.hpp:37-117)
+ * together with its sponge/compression wrappers:
+ *   BabyBear:   width 16, PaddingFreeSponge rate 8, digest 8,
+ *               TruncatedPermutation<2, 8, 16> (padding_free_sponge.hpp:63-113,
+ *               truncated_permutation.hpp:61-76);
+ *   Goldilocks: width 8, rate 4, digest 4, TruncatedPermutation<2, 4, 8>.
+ * rounds_f even and <= 8, rounds_p <= 32, sbox_degree in {3, 5, 7}.
+ * initial/terminal: [rounds_f/2][width] canonical elements; internal: [rounds_p]. */
+P3G_API int p3g_set_poseidon2(p3g_ctx *ctx, int field, uint32_t width, uint32_t rounds_f,
+                      uint32_t rounds_p, uint32_t sbox_degree, const void *h_initial,
+                      const void *h_terminal, const void *h_internal);
+
+/* Batch permutation of n states (n x width elements, in place on device).
+ * Replaces poseidon2_permute_kernel (poseidon2_cuda.hpp:156-166). */
+P3G_API int p3g_poseidon2_permute(p3g_ctx *ctx, int field, void *d_states, size_t n, void *stream);
+
+/* ------------------------------------------------------------ DFT / LDE
+ * Coset low-degree extension of a batch of columns:
+ *   out = coset_lde_batch(in, log_blowup, shift)            (radix2_dit.hpp:221-233)
+ *   and, if bitrev_out, reverse_matrix_index_bits(out)      (util.hpp:33-45)
+ * in:  (1 << log_h) x width, natural order;  out: (1 << (log_h + log_blowup)) x width.
+ * Replaces NttCuda<F>::coset_lde_batch (ntt_cuda.hpp:369-378, 607-649).
+ * in and out must not overlap.  Supports log_h <= 21. */
+P3G_API int p3g_coset_lde(p3g_ctx *ctx, int field, const void *d_in, uint32_t log_h, uint32_t width,
+                  uint32_t log_blowup, uint64_t shift, int bitrev_out, void *d_out, void *stream);
+
+/* ------------------------------------------------------------ MMCS */
+typedef struct {
+    const void *d_data;   /* row-major height x width, device */
+    uint64_t height;      /* power of two */
+    uint32_t width;
+    uint32_t reserved;
+} p3g_matrix;
+
+/* Mixed-height MerkleTreeMmcs::commit (merkle_tree_mmcs.hpp:100-107,
+ * merkle_tree.hpp:84-185): stable sort by height, leaf = sponge over the
+ * concatenated rows of the tallest matrices, compress per level, inject
+ * shorter matrices, stop at 2^cap_height nodes.  The tree keeps the digest
+ * layers on the device and references (does not copy) the matrices, which
+ * must stay alive until p3g_tree_free.  h_cap_out (may be NULL) receives the
+ * cap, 2^cap_height digests (or fewer if the tree is shorter); the call then
+ * synchronises `stream`.  Replaces build_merkle_tree_cuda (merkle_tree_cuda.hpp:360-621). */
+P3G_API int p3g_mmcs_commit(p3g_ctx *ctx, int field, const p3g_matrix *mats, size_t n_mats,
+                    uint32_t cap_height, p3g_tree **tree_out, void *h_cap_out, void *stream);
+
+/* Flat single-matrix MMCS, p3_merkle::MerkleTreeMmcs::commit_matrix
+ * (fri_merkle_tree_mmcs.hpp:55-102): any height >= 1, odd layers padded with
+ * a zero digest, commitment = the root.  h_root_out (may be NULL) gets one digest. */
+P3G_API int p3g_commit_matrix(p3g_ctx *ctx, int field, const void *d_flat, uint64_t height,
+                      uint32_t width, p3g_tree **tree_out, void *h_root_out, void *stream);
+
+/* Layer geometry: number of digest layers and the number of digests in each
+ * (layer 0 = leaves; capacity of h_layer_sizes >= 64). */
+P3G_API int p3g_tree_info(const p3g_tree *tree, uint32_t *n_layers, uint64_t *h_layer_sizes,
+                  uint32_t *digest_elems);
+/* Device pointer to digest layer `layer` (digests contiguous, digest_elems each). */
+P3G_API int p3g_tree_layer_ptr(const p3g_tree *tree, uint32_t layer, const void **d_ptr);
+/* Device pointer of leaf matrix i (in commit order). */
+P3G_API int p3g_tree_leaf_ptr(const p3g_tree *tree, uint32_t i, const void **d_ptr);
+
+/* MerkleTreeMmcs::open_batch (merkle_tree_mmcs.hpp:120-152) for n queries:
+ * for each query index q, the row index/(max_h/h_i) of every matrix i (rows
+ * concatenated in commit order into h_rows, sum(width_i) elements per query)
+ * and the sibling path (n_layers-1 digests per query into h_proof).  Synchronises. */
+P3G_API int p3g_mmcs_open_batch(p3g_ctx *ctx, const p3g_tree *tree, const uint64_t *h_indices,
+                        size_t n_queries, void *h_rows, void *h_proof, void *stream);
+
+P3G_API int p3g_tree_free(p3g_ctx *ctx, p3g_tree *tree);
+
+/* ------------------------------------------------------------ commit pipeline */
+typedef struct {
+    const void *d_trace;  /* (1 << log_h) x width evaluations, device */
+    uint32_t log_h;
+    uint32_t width;
+    uint32_t log_blowup;
+    uint32_t reserved;
+    uint64_t shift;       /* coset shift, canonical */
+} p3g_trace;
+
+/* The trace-commitment hot path: for every trace, the coset LDE with rows in
+ * bit-reversed order, then one mixed-height MMCS commit over all LDEs (the
+ * LDEs are owned by the returned tree; see p3g_tree_leaf_ptr).  With one
+ * trace this is the per-trace commit; with many it is the batched commit. */
+P3G_API int p3g_commit_traces(p3g_ctx *ctx, int field, const p3g_trace *traces, size_t n_traces,
+                      uint32_t cap_height, p3g_tree **tree_out, void *h_cap_out, void *stream);
+
+/* ------------------------------------------------------------ FRI
+ * TwoAdicFriFolding<BabyBear, BabyBear4>::fold_matrix (fri_folding.hpp:200-222)
+ * with fold_row's interpolation (fri_folding.hpp:74-189); log_arity in 1..3.
+ * d_in: 2^log_height BabyBear4 values; d_out: 2^(log_height - log_arity).
+ * Replaces fold_matrix_cuda_device (fri_fold_cuda.hpp:251-277). */
+P3G_API int p3g_fold_matrix_bb4(p3g_ctx *ctx, const void *d_in, uint32_t log_height,
+                        uint32_t log_arity, const uint32_t h_beta[4], void *d_out,
+                        void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* P3G_H */

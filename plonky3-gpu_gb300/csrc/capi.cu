@@ -1,0 +1,426 @@
+// capi.cu -- the extern "C" boundary of libp3g_gb300 (declared in include/p3g.h).
+//
+// Converts C++ exceptions into P3G_* status codes and a per-thread message,
+// owns contexts (root-of-unity tables, Poseidon2 constants, a stream-ordered
+// memory pool) and trees.  No entry point falls back to the CPU.
+#include <cstring>
+#include <memory>
+#include <new>
+#include <string>
+
+#include "internal.hpp"
+
+namespace {
+thread_local std::string g_last_error;
+
+struct DeviceGuard {
+    int prev = -1, want;
+    explicit DeviceGuard(int d) : want(d) {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+        if (prev != d) P3G_CUDA(cudaSetDevice(d));
+    }
+    ~DeviceGuard() {
+        if (prev >= 0 && prev != want) cudaSetDevice(prev);
+    }
+};
+
+inline cudaStream_t S(void* s) { return static_cast<cudaStream_t>(s); }
+}  // namespace
+
+#define API_BEGIN try {
+#define API_END                                           \
+    }                                                     \
+    catch (const p3g::Error& e) {                         \
+        g_last_error = e.what();                          \
+        return e.status;                                  \
+    }                                                     \
+    catch (const std::bad_alloc&) {                       \
+        g_last_error = "host allocation failed";          \
+        return P3G_ENOMEM;                                \
+    }                                                     \
+    catch (const std::exception& e) {                     \
+        g_last_error = e.what();                          \
+        return P3G_ECUDA;                                 \
+    }                                                     \
+    return P3G_OK;
+
+void* p3g_ctx::alloc(size_t bytes, cudaStream_t st) {
+    void* p = nullptr;
+    P3G_CUDA(cudaMallocFromPoolAsync(&p, bytes ? bytes : 1, pool, st));
+    return p;
+}
+void p3g_ctx::release(void* p, cudaStream_t st) {
+    if (p) P3G_CUDA(cudaFreeAsync(p, st));
+}
+
+extern "C" {
+
+int p3g_version(void) { return P3G_VERSION; }
+
+const char* p3g_status_string(int s) {
+    switch (s) {
+        case P3G_OK: return "ok";
+        case P3G_EINVAL: return "invalid argument";
+        case P3G_ENOMEM: return "out of device memory";
+        case P3G_ECUDA: return "CUDA error";
+        case P3G_ETIMEOUT: return "timed out";
+        case P3G_EUNSUPPORTED: return "unsupported";
+        case P3G_ESTATE: return "missing set-up";
+        default: return "unknown status";
+    }
+}
+
+int p3g_last_error(char* buf, size_t len) {
+    if (!buf || len == 0) return P3G_EINVAL;
+    size_t n = std::min(len - 1, g_last_error.size());
+    std::memcpy(buf, g_last_error.data(), n);
+    buf[n] = 0;
+    return P3G_OK;
+}
+
+int p3g_ctx_create(int device, p3g_ctx** out) {
+    API_BEGIN
+    P3G_REQUIRE(out != nullptr, "ctx_create: null output");
+    int n = 0;
+    P3G_CUDA(cudaGetDeviceCount(&n));
+    P3G_REQUIRE(device >= 0 && device < n, "ctx_create: no such device");
+    DeviceGuard g(device);
+    auto ctx = std::make_unique<p3g_ctx>();
+    ctx->device = device;
+    P3G_CUDA(cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device));
+    cudaMemPoolProps props = {};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = device;
+    P3G_CUDA(cudaMemPoolCreate(&ctx->pool, &props));
+    uint64_t keep = ~uint64_t(0);
+    P3G_CUDA(cudaMemPoolSetAttribute(ctx->pool, cudaMemPoolAttrReleaseThreshold, &keep));
+    // two-level root tables g^E = lo[E mod 2^LB] * hi[E >> LB] (const form)
+    {
+        using RB = p3g::RootTab<p3g::FBB>;
+        const uint32_t g27 = p3g::bb::two_adic_generator(27);
+        std::vector<uint32_t> lo(size_t(1) << RB::LB), hi(size_t(1) << (27 - RB::LB));
+        uint32_t v = 1;
+        for (auto& x : lo) { x = p3g::bb::to_mont(v); v = p3g::bb::h_mul(v, g27); }
+        const uint32_t step = v;  // g^(2^LB)
+        v = 1;
+        for (auto& x : hi) { x = p3g::bb::to_mont(v); v = p3g::bb::h_mul(v, step); }
+        P3G_CUDA(cudaMalloc(&ctx->bb_lo, lo.size() * 4));
+        P3G_CUDA(cudaMalloc(&ctx->bb_hi, hi.size() * 4));
+        P3G_CUDA(cudaMemcpy(ctx->bb_lo, lo.data(), lo.size() * 4, cudaMemcpyHostToDevice));
+        P3G_CUDA(cudaMemcpy(ctx->bb_hi, hi.data(), hi.size() * 4, cudaMemcpyHostToDevice));
+    }
+    {
+        using RG = p3g::RootTab<p3g::FGL>;
+        const uint64_t g32 = p3g::gl::two_adic_generator(32);
+        std::vector<uint64_t> lo(size_t(1) << RG::LB), hi(size_t(1) << (32 - RG::LB));
+        uint64_t v = 1;
+        for (auto& x : lo) { x = v; v = p3g::gl::h_mul(v, g32); }
+        const uint64_t step = v;
+        v = 1;
+        for (auto& x : hi) { x = v; v = p3g::gl::h_mul(v, step); }
+        P3G_CUDA(cudaMalloc(&ctx->gl_lo, lo.size() * 8));
+        P3G_CUDA(cudaMalloc(&ctx->gl_hi, hi.size() * 8));
+        P3G_CUDA(cudaMemcpy(ctx->gl_lo, lo.data(), lo.size() * 8, cudaMemcpyHostToDevice));
+        P3G_CUDA(cudaMemcpy(ctx->gl_hi, hi.data(), hi.size() * 8, cudaMemcpyHostToDevice));
+    }
+    *out = ctx.release();
+    API_END
+}
+
+int p3g_ctx_destroy(p3g_ctx* ctx) {
+    API_BEGIN
+    if (!ctx) return P3G_OK;
+    {
+        DeviceGuard g(ctx->device);
+        cudaDeviceSynchronize();
+        cudaFree(ctx->bb_lo);
+        cudaFree(ctx->bb_hi);
+        cudaFree(ctx->gl_lo);
+        cudaFree(ctx->gl_hi);
+        if (ctx->pool) cudaMemPoolDestroy(ctx->pool);
+    }
+    delete ctx;
+    API_END
+}
+
+int p3g_stream_synchronize(p3g_ctx* ctx, void* stream) {
+    API_BEGIN
+    P3G_REQUIRE(ctx, "null context");
+    DeviceGuard g(ctx->device);
+    P3G_CUDA(cudaStreamSynchronize(S(stream)));
+    API_END
+}
+
+int p3g_malloc(p3g_ctx* ctx, size_t bytes, void** d_ptr, void* stream) {
+    API_BEGIN
+    P3G_REQUIRE(ctx && d_ptr, "malloc: null argument");
+    DeviceGuard g(ctx->device);
+    *d_ptr = ctx->alloc(bytes, S(stream));
+    API_END
+}
+
+int p3g_free(p3g_ctx* ctx, void* d_ptr, void* stream) {
+    API_BEGIN
+    P3G_REQUIRE(ctx, "free: null context");
+    DeviceGuard g(ctx->device);
+    ctx->release(d_ptr, S(stream));
+    API_END
+}
+
+int p3g_memcpy_h2d(p3g_ctx* ctx, void* d_dst, const void* h_src, size_t bytes, void* stream) {
+    API_BEGIN
+    P3G_REQUIRE(ctx && (bytes == 0 || (d_dst && h_src)), "memcpy_h2d: null argument");
+    DeviceGuard g(ctx->device);
+    if (bytes) P3G_CUDA(cudaMemcpyAsync(d_dst, h_src, bytes, cudaMemcpyHostToDevice, S(stream)));
+    API_END
+}
+
+int p3g_memcpy_d2h(p3g_ctx* ctx, void* h_dst, const void* d_src, size_t bytes, void* stream) {
+    API_BEGIN
+    P3G_REQUIRE(ctx && (bytes == 0 || (h_dst && d_src)), "memcpy_d2h: null argument");
+    DeviceGuard g(ctx->device);
+    if (bytes) P3G_CUDA(cudaMemcpyAsync(h_dst, d_src, bytes, cudaMemcpyDeviceToHost, S(stream)));
+    P3G_CUDA(cudaStreamSynchronize(S(stream)));
+    API_END
+}
+
+int p3g_set_poseidon2(p3g_ctx* ctx, int field, uint32_t width, uint32_t rounds_f, uint32_t rounds_p,
+                      uint32_t sbox_degree, const void* h_initial, const void* h_terminal, const void* h_internal) {
+    API_BEGIN
+    P3G_REQUIRE(ctx && h_initial && h_terminal && (h_internal || rounds_p == 0), "set_poseidon2: null argument");
+    P3G_REQUIRE(rounds_f % 2 == 0 && rounds_f <= 8, "set_poseidon2: rounds_f must be even and <= 8");
+    P3G_REQUIRE(rounds_p <= 32, "set_poseidon2: rounds_p must be <= 32");
+    P3G_REQUIRE(sbox_degree == 3 || sbox_degree == 5 || sbox_degree == 7, "set_poseidon2: degree must be 3, 5 or 7");
+    const uint32_t half = rounds_f / 2;
+    if (field == P3G_BABYBEAR) {
+        P3G_REQUIRE(width == 16, "set_poseidon2: BabyBear width must be 16");
+        const uint32_t* ini = static_cast<const uint32_t*>(h_initial);
+        const uint32_t* ter = static_cast<const uint32_t*>(h_terminal);
+        const uint32_t* inr = static_cast<const uint32_t*>(h_internal);
+        p3g::P2BB16 p{};
+        for (uint32_t r = 0; r < half; ++r)
+            for (uint32_t i = 0; i < 16; ++i) {
+                P3G_REQUIRE(ini[r * 16 + i] < p3g::bb::P && ter[r * 16 + i] < p3g::bb::P,
+                            "set_poseidon2: constants must be canonical");
+                p.initial[r][i] = p3g::bb::to_mont(ini[r * 16 + i]);
+                p.terminal[r][i] = p3g::bb::to_mont(ter[r * 16 + i]);
+            }
+        for (uint32_t r = 0; r < rounds_p; ++r) {
+            P3G_REQUIRE(inr[r] < p3g::bb::P, "set_poseidon2: constants must be canonical");
+            p.internal[r] = p3g::bb::to_mont(inr[r]);
+        }
+        for (uint32_t i = 0; i < 16; ++i) p.diag[i] = p3g::bb::to_mont(uint32_t((1ull << i) % p3g::bb::P));
+        ctx->p2bb = p;
+        ctx->bb_rf = int(rounds_f);
+        ctx->bb_rp = int(rounds_p);
+        ctx->bb_d = int(sbox_degree);
+        ctx->has_p2bb = true;
+    } else if (field == P3G_GOLDILOCKS) {
+        P3G_REQUIRE(width == 8, "set_poseidon2: Goldilocks width must be 8");
+        const uint64_t* ini = static_cast<const uint64_t*>(h_initial);
+        const uint64_t* ter = static_cast<const uint64_t*>(h_terminal);
+        const uint64_t* inr = static_cast<const uint64_t*>(h_internal);
+        p3g::P2GL8 p{};
+        for (uint32_t r = 0; r < half; ++r)
+            for (uint32_t i = 0; i < 8; ++i) {
+                P3G_REQUIRE(ini[r * 8 + i] < p3g::gl::P && ter[r * 8 + i] < p3g::gl::P,
+                            "set_poseidon2: constants must be canonical");
+                p.initial[r][i] = ini[r * 8 + i];
+                p.terminal[r][i] = ter[r * 8 + i];
+            }
+        for (uint32_t r = 0; r < rounds_p; ++r) {
+            P3G_REQUIRE(inr[r] < p3g::gl::P, "set_poseidon2: constants must be canonical");
+            p.internal[r] = inr[r];
+        }
+        ctx->p2gl = p;
+        ctx->gl_rf = int(rounds_f);
+        ctx->gl_rp = int(rounds_p);
+        ctx->gl_d = int(sbox_degree);
+        ctx->has_p2gl = true;
+    } else {
+        P3G_REQUIRE(false, "set_poseidon2: unknown field");
+    }
+    API_END
+}
+
+int p3g_poseidon2_permute(p3g_ctx* ctx, int field, void* d_states, size_t n, void* stream) {
+    API_BEGIN
+    P3G_REQUIRE(ctx && (n == 0 || d_states), "poseidon2_permute: null argument");
+    P3G_REQUIRE(field == P3G_BABYBEAR || field == P3G_GOLDILOCKS, "poseidon2_permute: unknown field");
+    DeviceGuard g(ctx->device);
+    p3g::permute_states(ctx, field, d_states, n, S(stream));
+    API_END
+}
+
+int p3g_coset_lde(p3g_ctx* ctx, int field, const void* d_in, uint32_t log_h, uint32_t width, uint32_t log_blowup,
+                  uint64_t shift, int bitrev_out, void* d_out, void* stream) {
+    API_BEGIN
+    P3G_REQUIRE(ctx && (width == 0 || (d_in && d_out)), "coset_lde: null argument");
+    P3G_REQUIRE(width <= (1u << 24), "coset_lde: width too large");
+    DeviceGuard g(ctx->device);
+    if (field == P3G_BABYBEAR) {
+        P3G_REQUIRE(shift < p3g::bb::P, "coset_lde: shift must be canonical");
+        p3g::lde_bb(ctx, static_cast<const uint32_t*>(d_in), int(log_h), int(width), int(log_blowup),
+                    uint32_t(shift), bitrev_out, static_cast<uint32_t*>(d_out), S(stream));
+    } else if (field == P3G_GOLDILOCKS) {
+        P3G_REQUIRE(shift < p3g::gl::P, "coset_lde: shift must be canonical");
+        p3g::lde_gl(ctx, static_cast<const uint64_t*>(d_in), int(log_h), int(width), int(log_blowup), shift,
+                    bitrev_out, static_cast<uint64_t*>(d_out), S(stream));
+    } else {
+        P3G_REQUIRE(false, "coset_lde: unknown field");
+    }
+    API_END
+}
+
+static void copy_cap(const p3g_tree* t, void* h_out, cudaStream_t st) {
+    if (!h_out) return;
+    const size_t esz = t->field == P3G_BABYBEAR ? 4 : 8;
+    const size_t last = t->layer_size.size() - 1;
+    const char* src = static_cast<const char*>(t->d_digests) + t->layer_off[last] * t->digest * esz;
+    P3G_CUDA(cudaMemcpyAsync(h_out, src, t->layer_size[last] * t->digest * esz, cudaMemcpyDeviceToHost, st));
+    P3G_CUDA(cudaStreamSynchronize(st));
+}
+
+static void free_tree(p3g_ctx* ctx, p3g_tree* t, cudaStream_t st) {
+    if (!t) return;
+    if (t->d_digests) ctx->release(t->d_digests, st);
+    for (void* p : t->owned) ctx->release(p, st);
+    delete t;
+}
+
+int p3g_mmcs_commit(p3g_ctx* ctx, int field, const p3g_matrix* mats, size_t n_mats, uint32_t cap_height,
+                    p3g_tree** tree_out, void* h_cap_out, void* stream) {
+    API_BEGIN
+    P3G_REQUIRE(ctx && mats && n_mats > 0 && tree_out, "mmcs_commit: null argument");
+    P3G_REQUIRE(field == P3G_BABYBEAR || field == P3G_GOLDILOCKS, "mmcs_commit: unknown field");
+    DeviceGuard g(ctx->device);
+    auto t = std::make_unique<p3g_tree>();
+    t->field = field;
+    t->mats.assign(mats, mats + n_mats);
+    try {
+        p3g::mmcs_build(ctx, t.get(), cap_height, S(stream));
+        copy_cap(t.get(), h_cap_out, S(stream));
+    } catch (...) {
+        if (t->d_digests) ctx->release(t->d_digests, S(stream));
+        t->d_digests = nullptr;
+        throw;
+    }
+    *tree_out = t.release();
+    API_END
+}
+
+int p3g_commit_matrix(p3g_ctx* ctx, int field, const void* d_flat, uint64_t height, uint32_t width,
+                      p3g_tree** tree_out, void* h_root_out, void* stream) {
+    API_BEGIN
+    P3G_REQUIRE(ctx && d_flat && tree_out, "commit_matrix: null argument");
+    P3G_REQUIRE(width > 0 && height > 0, "commit_matrix: bad dimensions");
+    P3G_REQUIRE(field == P3G_BABYBEAR || field == P3G_GOLDILOCKS, "commit_matrix: unknown field");
+    DeviceGuard g(ctx->device);
+    auto t = std::make_unique<p3g_tree>();
+    t->field = field;
+    t->mats.push_back(p3g_matrix{d_flat, height, width, 0});
+    try {
+        p3g::flat_build(ctx, t.get(), S(stream));
+        copy_cap(t.get(), h_root_out, S(stream));
+    } catch (...) {
+        if (t->d_digests) ctx->release(t->d_digests, S(stream));
+        t->d_digests = nullptr;
+        throw;
+    }
+    *tree_out = t.release();
+    API_END
+}
+
+int p3g_tree_info(const p3g_tree* tree, uint32_t* n_layers, uint64_t* h_layer_sizes, uint32_t* digest_elems) {
+    API_BEGIN
+    P3G_REQUIRE(tree, "tree_info: null tree");
+    if (n_layers) *n_layers = uint32_t(tree->layer_size.size());
+    if (h_layer_sizes)
+        for (size_t i = 0; i < tree->layer_size.size() && i < 64; ++i) h_layer_sizes[i] = tree->layer_size[i];
+    if (digest_elems) *digest_elems = tree->digest;
+    API_END
+}
+
+int p3g_tree_layer_ptr(const p3g_tree* tree, uint32_t layer, const void** d_ptr) {
+    API_BEGIN
+    P3G_REQUIRE(tree && d_ptr && layer < tree->layer_size.size(), "tree_layer_ptr: bad argument");
+    const size_t esz = tree->field == P3G_BABYBEAR ? 4 : 8;
+    *d_ptr = static_cast<const char*>(tree->d_digests) + tree->layer_off[layer] * tree->digest * esz;
+    API_END
+}
+
+int p3g_tree_leaf_ptr(const p3g_tree* tree, uint32_t i, const void** d_ptr) {
+    API_BEGIN
+    P3G_REQUIRE(tree && d_ptr && i < tree->mats.size(), "tree_leaf_ptr: bad argument");
+    *d_ptr = tree->mats[i].d_data;
+    API_END
+}
+
+int p3g_mmcs_open_batch(p3g_ctx* ctx, const p3g_tree* tree, const uint64_t* h_indices, size_t n_queries,
+                        void* h_rows, void* h_proof, void* stream) {
+    API_BEGIN
+    P3G_REQUIRE(ctx && tree && (n_queries == 0 || h_indices), "open_batch: null argument");
+    DeviceGuard g(ctx->device);
+    p3g::open_batch(ctx, tree, h_indices, n_queries, h_rows, h_proof, S(stream));
+    API_END
+}
+
+int p3g_tree_free(p3g_ctx* ctx, p3g_tree* tree) {
+    API_BEGIN
+    P3G_REQUIRE(ctx, "tree_free: null context");
+    DeviceGuard g(ctx->device);
+    free_tree(ctx, tree, nullptr);
+    API_END
+}
+
+int p3g_commit_traces(p3g_ctx* ctx, int field, const p3g_trace* traces, size_t n_traces, uint32_t cap_height,
+                      p3g_tree** tree_out, void* h_cap_out, void* stream) {
+    API_BEGIN
+    P3G_REQUIRE(ctx && traces && n_traces > 0 && tree_out, "commit_traces: null argument");
+    P3G_REQUIRE(field == P3G_BABYBEAR || field == P3G_GOLDILOCKS, "commit_traces: unknown field");
+    DeviceGuard g(ctx->device);
+    cudaStream_t st = S(stream);
+    auto t = std::make_unique<p3g_tree>();
+    t->field = field;
+    const size_t esz = field == P3G_BABYBEAR ? 4 : 8;
+    try {
+        for (size_t i = 0; i < n_traces; ++i) {
+            const p3g_trace& tr = traces[i];
+            P3G_REQUIRE(tr.width == 0 || tr.d_trace, "commit_traces: null trace");
+            const uint64_t H = uint64_t(1) << (tr.log_h + tr.log_blowup);
+            void* lde = ctx->alloc(esz * H * tr.width, st);
+            t->owned.push_back(lde);
+            if (field == P3G_BABYBEAR) {
+                P3G_REQUIRE(tr.shift < p3g::bb::P, "commit_traces: shift must be canonical");
+                p3g::lde_bb(ctx, static_cast<const uint32_t*>(tr.d_trace), int(tr.log_h), int(tr.width),
+                            int(tr.log_blowup), uint32_t(tr.shift), 1, static_cast<uint32_t*>(lde), st);
+            } else {
+                P3G_REQUIRE(tr.shift < p3g::gl::P, "commit_traces: shift must be canonical");
+                p3g::lde_gl(ctx, static_cast<const uint64_t*>(tr.d_trace), int(tr.log_h), int(tr.width),
+                            int(tr.log_blowup), tr.shift, 1, static_cast<uint64_t*>(lde), st);
+            }
+            t->mats.push_back(p3g_matrix{lde, H, tr.width, 0});
+        }
+        p3g::mmcs_build(ctx, t.get(), cap_height, st);
+        copy_cap(t.get(), h_cap_out, st);
+    } catch (...) {
+        if (t->d_digests) ctx->release(t->d_digests, st);
+        for (void* p : t->owned) ctx->release(p, st);
+        throw;
+    }
+    *tree_out = t.release();
+    API_END
+}
+
+int p3g_fold_matrix_bb4(p3g_ctx* ctx, const void* d_in, uint32_t log_height, uint32_t log_arity,
+                        const uint32_t h_beta[4], void* d_out, void* stream) {
+    API_BEGIN
+    P3G_REQUIRE(ctx && d_in && d_out && h_beta, "fold_matrix: null argument");
+    DeviceGuard g(ctx->device);
+    p3g::fold_bb4(ctx, static_cast<const uint32_t*>(d_in), int(log_height), int(log_arity), h_beta,
+                  static_cast<uint32_t*>(d_out), S(stream));
+    API_END
+}
+
+}  // extern "C"

@@ -1,0 +1,237 @@
+// fields.cuh -- BabyBear, Goldilocks and BabyBear^4 arithmetic for sm_103a.
+//
+// Representation (all values crossing the C ABI are canonical, as in the
+// reference: baby_bear.hpp:25-88 keeps a canonical u32, goldilocks.hpp:53-59
+// compares canonical u64):
+//
+//  * BabyBear data stays canonical in [0, p).  Every multiplication on the hot
+//    path is data x constant, and constants are stored in Montgomery form
+//    (c * 2^32 mod p), so one Montgomery product mont(x, c*R) = x*c mod p
+//    returns a canonical result with no conversion of the data.  Poseidon2,
+//    which multiplies data by data, converts its state into Montgomery form
+//    on absorb and back on squeeze.
+//  * Goldilocks uses the special-form reduction of 2^64 - 2^32 + 1
+//    (2^64 = 2^32 - 1, 2^96 = -1), which is cheaper than Montgomery here.
+//  * BabyBear^4 = BabyBear[x]/(x^4 - 11), extension_field.hpp:106-131.
+#pragma once
+#include <cstdint>
+
+#ifndef P3G_HD
+#define P3G_HD __host__ __device__ __forceinline__
+#endif
+
+namespace p3g {
+
+// ===================================================================== BabyBear
+namespace bb {
+constexpr uint32_t P = 0x78000001u;
+constexpr uint32_t compute_pinv() {  // p^-1 mod 2^32 by Newton iteration
+    uint32_t x = 1;
+    for (int i = 0; i < 6; ++i) x *= 2u - P * x;
+    return x;
+}
+constexpr uint32_t PINV = compute_pinv();
+constexpr uint32_t NPINV = 0u - PINV;  // -p^-1 mod 2^32
+static_assert(uint32_t(P * PINV) == 1u, "p^-1");
+constexpr uint32_t R1 = uint32_t((uint64_t(1) << 32) % P);                // 2^32 mod p
+constexpr uint32_t R2 = uint32_t((uint64_t(R1) * uint64_t(R1)) % P);     // 2^64 mod p
+
+P3G_HD uint32_t add(uint32_t a, uint32_t b) {
+    uint32_t s = a + b;  // < 2p < 2^32
+    uint32_t t = s - P;
+    return s < t ? s : t;
+}
+P3G_HD uint32_t sub(uint32_t a, uint32_t b) {
+    uint32_t d = a - b;
+    uint32_t t = d + P;
+    return d < t ? d : t;
+}
+// Montgomery product a*b*2^-32 mod p, canonical output; a, b < p.
+P3G_HD uint32_t mmul(uint32_t a, uint32_t b) {
+    uint64_t t = uint64_t(a) * b;
+    uint32_t m = uint32_t(t) * NPINV;
+    uint64_t u = t + uint64_t(m) * P;  // low 32 bits vanish; < 2^64
+    uint32_t r = uint32_t(u >> 32);    // < 2p
+    uint32_t s = r - P;
+    return r < s ? r : s;
+}
+// Host helpers (exact, used to build constant tables).
+inline uint32_t h_mul(uint32_t a, uint32_t b) { return uint32_t((uint64_t(a) * b) % P); }
+inline uint32_t h_pow(uint32_t a, uint64_t e) {
+    uint32_t r = 1;
+    while (e) {
+        if (e & 1) r = h_mul(r, a);
+        a = h_mul(a, a);
+        e >>= 1;
+    }
+    return r;
+}
+inline uint32_t h_inv(uint32_t a) { return h_pow(a, P - 2); }
+inline uint32_t to_mont(uint32_t a) { return uint32_t((uint64_t(a) << 32) % P); }
+inline uint32_t from_mont(uint32_t a) { return h_mul(a, h_inv(R1)); }
+// Primitive 2^bits-th root of unity, baby_bear.hpp:131-145.
+inline uint32_t two_adic_generator(unsigned bits) { return h_pow(440564289u, uint64_t(1) << (27 - bits)); }
+constexpr unsigned TWO_ADICITY = 27;
+}  // namespace bb
+
+// ==================================================================== Goldilocks
+namespace gl {
+constexpr uint64_t P = 0xFFFFFFFF00000001ull;
+constexpr uint64_t EPS = 0xFFFFFFFFull;  // 2^64 mod p
+
+P3G_HD uint64_t add(uint64_t a, uint64_t b) {  // canonical in/out
+    uint64_t s = a + b;
+    if (s < a) s += EPS;          // wrapped: true sum = s + 2^64 = s + EPS (mod p), < p
+    else if (s >= P) s -= P;
+    return s;
+}
+P3G_HD uint64_t sub(uint64_t a, uint64_t b) {
+    uint64_t d = a - b;
+    if (a < b) d -= EPS;          // d + 2^64 - 2^64 + p = d - EPS
+    return d;
+}
+P3G_HD uint64_t reduce128(uint64_t lo, uint64_t hi) {
+    uint64_t hh = hi >> 32, hl = hi & EPS;
+    uint64_t t0 = lo - hh;
+    if (lo < hh) t0 -= EPS;                 // 2^96 = -1
+    uint64_t t1 = (hl << 32) - hl;          // hl * (2^32 - 1), 2^64 = 2^32 - 1
+    uint64_t t2 = t0 + t1;
+    if (t2 < t1) t2 += EPS;
+    if (t2 >= P) t2 -= P;
+    return t2;
+}
+#ifdef __CUDA_ARCH__
+__device__ __forceinline__ uint64_t mul(uint64_t a, uint64_t b) {
+    return reduce128(a * b, __umul64hi(a, b));
+}
+#else
+inline uint64_t mul(uint64_t a, uint64_t b) {
+    unsigned __int128 t = (unsigned __int128)a * b;
+    return reduce128(uint64_t(t), uint64_t(t >> 64));
+}
+#endif
+inline uint64_t h_mul(uint64_t a, uint64_t b) { return uint64_t(((unsigned __int128)a * b) % P); }
+inline uint64_t h_pow(uint64_t a, uint64_t e) {
+    uint64_t r = 1;
+    a %= P;
+    while (e) {
+        if (e & 1) r = h_mul(r, a);
+        a = h_mul(a, a);
+        e >>= 1;
+    }
+    return r;
+}
+inline uint64_t h_inv(uint64_t a) { return h_pow(a, P - 2); }
+// 7 generates F_p^*; omega_{2^bits} = 7^((p-1)/2^bits).
+inline uint64_t two_adic_generator(unsigned bits) { return h_pow(7, (P - 1) >> bits); }
+constexpr unsigned TWO_ADICITY = 32;
+}  // namespace gl
+
+// ========================================================= field traits for kernels
+// mulc(x, c): x canonical, c a stored constant ("const form"); returns x*c canonical.
+struct FBB {
+    using T = uint32_t;
+    static constexpr unsigned TWO_ADICITY = 27;
+    static P3G_HD T add(T a, T b) { return bb::add(a, b); }
+    static P3G_HD T sub(T a, T b) { return bb::sub(a, b); }
+    static P3G_HD T mulc(T a, T c) { return bb::mmul(a, c); }
+    // product of two const-form values, result in const form
+    static P3G_HD T cmul(T a, T b) { return bb::mmul(a, b); }
+    static inline T to_const(uint64_t canonical) { return bb::to_mont(uint32_t(canonical)); }
+    static inline uint64_t h_mul(uint64_t a, uint64_t b) { return bb::h_mul(uint32_t(a), uint32_t(b)); }
+    static inline uint64_t h_pow(uint64_t a, uint64_t e) { return bb::h_pow(uint32_t(a), e); }
+    static inline uint64_t h_inv(uint64_t a) { return bb::h_inv(uint32_t(a)); }
+    static inline uint64_t root(unsigned bits) { return bb::two_adic_generator(bits); }
+    static constexpr uint64_t P = bb::P;
+};
+struct FGL {
+    using T = uint64_t;
+    static constexpr unsigned TWO_ADICITY = 32;
+    static P3G_HD T add(T a, T b) { return gl::add(a, b); }
+    static P3G_HD T sub(T a, T b) { return gl::sub(a, b); }
+    static __device__ __forceinline__ T mulc(T a, T c) { return gl::mul(a, c); }
+    static __device__ __forceinline__ T cmul(T a, T b) { return gl::mul(a, b); }
+    static inline T to_const(uint64_t canonical) { return canonical; }
+    static inline uint64_t h_mul(uint64_t a, uint64_t b) { return gl::h_mul(a, b); }
+    static inline uint64_t h_pow(uint64_t a, uint64_t e) { return gl::h_pow(a, e); }
+    static inline uint64_t h_inv(uint64_t a) { return gl::h_inv(a); }
+    static inline uint64_t root(unsigned bits) { return gl::two_adic_generator(bits); }
+    static constexpr uint64_t P = gl::P;
+};
+
+// ===================================================================== BabyBear^4
+// Canonical coefficients; products via Montgomery with one operand in const form.
+struct bb4 {
+    uint32_t c[4];
+};
+// a canonical, b in Montgomery (const) form -> a*b canonical.  x^4 = 11.
+P3G_HD bb4 bb4_mul_cm(const bb4& a, const bb4& bm) {
+    constexpr uint32_t ELEVEN_M = uint32_t((uint64_t(11) << 32) % bb::P);
+    uint32_t p[7];
+#pragma unroll
+    for (int k = 0; k < 7; ++k) p[k] = 0;
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) p[i + j] = bb::add(p[i + j], bb::mmul(a.c[i], bm.c[j]));
+    bb4 r;
+    r.c[0] = bb::add(p[0], bb::mmul(p[4], ELEVEN_M));
+    r.c[1] = bb::add(p[1], bb::mmul(p[5], ELEVEN_M));
+    r.c[2] = bb::add(p[2], bb::mmul(p[6], ELEVEN_M));
+    r.c[3] = p[3];
+    return r;
+}
+P3G_HD bb4 bb4_add(const bb4& a, const bb4& b) {
+    bb4 r;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) r.c[i] = bb::add(a.c[i], b.c[i]);
+    return r;
+}
+P3G_HD bb4 bb4_sub(const bb4& a, const bb4& b) {
+    bb4 r;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) r.c[i] = bb::sub(a.c[i], b.c[i]);
+    return r;
+}
+P3G_HD bb4 bb4_scale_m(const bb4& a, uint32_t sm) {  // a * s, s in Montgomery form
+    bb4 r;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) r.c[i] = bb::mmul(a.c[i], sm);
+    return r;
+}
+P3G_HD bb4 bb4_to_mont(const bb4& a) {
+    bb4 r;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) r.c[i] = bb::mmul(a.c[i], bb::R2);
+    return r;
+}
+// Full inverse a^-1 (canonical in/out) via the Frobenius norm
+// (extension_field.hpp:396-446); any correct inverse is the same field element.
+P3G_HD uint32_t bb_pow_m(uint32_t am, uint32_t e) {  // Montgomery in/out
+    uint32_t r = bb::R1;
+    while (e) {
+        if (e & 1) r = bb::mmul(r, am);
+        am = bb::mmul(am, am);
+        e >>= 1;
+    }
+    return r;
+}
+P3G_HD bb4 bb4_inv(const bb4& a) {
+    // z = 11^((p-1)/4) = 1728404513 (a primitive 4th root of unity)
+    constexpr uint32_t Z = 1728404513u;
+    constexpr uint32_t ZM = uint32_t((uint64_t(Z) << 32) % bb::P);
+    const uint32_t z2m = bb::mmul(ZM, ZM);       // Montgomery form of z^2? (z*z*R) -> see below
+    // mmul(ZM, ZM) = z^2 * R (Montgomery form), likewise below.
+    const uint32_t z3m = bb::mmul(z2m, ZM);
+    bb4 pa = {{a.c[0], bb::mmul(a.c[1], ZM), bb::mmul(a.c[2], z2m), bb::mmul(a.c[3], z3m)}};
+    bb4 p2a = {{a.c[0], bb::mmul(a.c[1], z2m), a.c[2], bb::mmul(a.c[3], z2m)}};
+    bb4 p3a = {{a.c[0], bb::mmul(a.c[1], z3m), bb::mmul(a.c[2], z2m), bb::mmul(a.c[3], ZM)}};
+    bb4 p23 = bb4_mul_cm(p2a, bb4_to_mont(p3a));
+    bb4 num = bb4_mul_cm(pa, bb4_to_mont(p23));
+    bb4 nrm = bb4_mul_cm(a, bb4_to_mont(num));  // norm lies in the base field
+    uint32_t nm = bb::mmul(nrm.c[0], bb::R2);
+    uint32_t ninv_m = bb_pow_m(nm, bb::P - 2);
+    return bb4_scale_m(num, ninv_m);
+}
+
+}  // namespace p3g

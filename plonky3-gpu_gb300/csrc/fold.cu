@@ -1,0 +1,119 @@
+// fold.cu -- FRI fold_matrix over BabyBear^4.
+//
+// Reference: TwoAdicFriFolding<BabyBear, BabyBear4>::fold_matrix and fold_row
+// (fri_folding.hpp:74-222).  Output i interpolates the arity values
+// in[i*a .. i*a+a) at beta over the nodes t_j = x * w^bitrev(j), with
+// x = omega_{2^log_height}^bitrev(i, log_height - log_arity).
+//
+// Arity 2 uses the closed form (e0 + e1)/2 + beta (e0 - e1) / (2x), which is
+// the same field element as the reference's Lagrange sum (and also covers its
+// beta == t_j early return).  x^-1 comes from the context's root table, not a
+// per-thread exponentiation.  Arity 4 and 8 evaluate the reference's formula
+// term for term, L_i = N * a^-1 / ((beta - t_i) x^(a-1) w^-(i)) with
+// N = prod_j (beta - t_j), including its early return when beta equals a node.
+#include "internal.hpp"
+#include "ntt.cuh"
+
+namespace p3g {
+
+__device__ __forceinline__ bb4 bb4_mul(const bb4& a, const bb4& b) { return bb4_mul_cm(a, bb4_to_mont(b)); }
+
+__global__ void k_fold2(const bb4* __restrict__ in, bb4* __restrict__ out, uint64_t n, int log_height,
+                        bb4 beta_m, uint32_t inv2_m, RootTab<FBB> roots) {
+    uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int log_folded = log_height - 1;
+    const uint32_t xinv_m = roots.omega_inv(log_height, bitrev_dev(unsigned(i), log_folded));
+    const uint32_t inv2x_m = bb::mmul(xinv_m, inv2_m);
+    const bb4 e0 = in[2 * i], e1 = in[2 * i + 1];
+    const bb4 s = bb4_scale_m(bb4_add(e0, e1), inv2_m);
+    const bb4 d = bb4_scale_m(bb4_sub(e0, e1), inv2x_m);
+    out[i] = bb4_add(s, bb4_mul_cm(d, beta_m));
+}
+
+template <int LA>
+__global__ void k_fold_general(const bb4* __restrict__ in, bb4* __restrict__ out, uint64_t n, int log_height,
+                               bb4 beta, uint32_t w_c, uint32_t winv_c, uint32_t arity_inv_c, RootTab<FBB> roots) {
+    constexpr int A = 1 << LA;
+    uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int log_folded = log_height - LA;
+    const uint32_t x_m = roots.omega(log_height, bitrev_dev(unsigned(i), log_folded));
+    const uint32_t x = bb::mmul(x_m, 1u);
+    // nodes t_j = x * w^j, then bit-reversed (fri_folding.hpp:109-125)
+    uint32_t tn[A];
+    uint32_t wp = x;
+#pragma unroll
+    for (int j = 0; j < A; ++j) {
+        tn[j] = wp;
+        wp = bb::mmul(wp, w_c);
+    }
+    uint32_t t[A];
+#pragma unroll
+    for (int j = 0; j < A; ++j) t[j] = tn[bitrev_ct(unsigned(j), LA)];
+    bb4 ev[A];
+#pragma unroll
+    for (int j = 0; j < A; ++j) ev[j] = in[i * A + j];
+    const bool beta_base = beta.c[1] == 0 && beta.c[2] == 0 && beta.c[3] == 0;
+    if (beta_base) {
+        for (int j = 0; j < A; ++j)
+            if (beta.c[0] == t[j]) {
+                out[i] = ev[j];
+                return;
+            }
+    }
+    bb4 full = {{1, 0, 0, 0}};
+    bb4 bmt[A];
+#pragma unroll
+    for (int j = 0; j < A; ++j) {
+        bmt[j] = beta;
+        bmt[j].c[0] = bb::sub(beta.c[0], t[j]);
+        full = bb4_mul(full, bmt[j]);
+    }
+    // x^(a-1)
+    uint32_t xp_m = bb::mmul(x, bb::R2);  // Montgomery x
+    uint32_t xam1_m = bb::R1;
+#pragma unroll
+    for (int k = 0; k < A - 1; ++k) xam1_m = bb::mmul(xam1_m, xp_m);
+    const bb4 num = bb4_scale_m(full, arity_inv_c);
+    bb4 res = {{0, 0, 0, 0}};
+    uint32_t winv_i = bb::R1;  // Montgomery
+#pragma unroll
+    for (int j = 0; j < A; ++j) {
+        const uint32_t bd_m = bb::mmul(xam1_m, winv_i);
+        const bb4 denom = bb4_scale_m(bmt[j], bd_m);
+        const bb4 L = bb4_mul(num, bb4_inv(denom));
+        res = bb4_add(res, bb4_mul(ev[j], L));
+        winv_i = bb::mmul(winv_i, winv_c);
+    }
+    out[i] = res;
+}
+
+void fold_bb4(p3g_ctx* ctx, const uint32_t* in, int log_height, int log_arity, const uint32_t beta[4],
+              uint32_t* out, cudaStream_t st) {
+    P3G_REQUIRE(log_arity >= 1 && log_arity <= 3, "fold_matrix: log_arity must be 1, 2 or 3");
+    P3G_REQUIRE(log_arity <= log_height && log_height <= 27, "fold_matrix: bad log_height");
+    for (int k = 0; k < 4; ++k) P3G_REQUIRE(beta[k] < bb::P, "fold_matrix: beta must be canonical");
+    const uint64_t n = (uint64_t(1) << log_height) >> log_arity;
+    const bb4* din = reinterpret_cast<const bb4*>(in);
+    bb4* dout = reinterpret_cast<bb4*>(out);
+    bb4 b = {{beta[0], beta[1], beta[2], beta[3]}};
+    const unsigned grid = unsigned((n + 255) / 256);
+    if (log_arity == 1) {
+        bb4 bm = {{bb::to_mont(beta[0]), bb::to_mont(beta[1]), bb::to_mont(beta[2]), bb::to_mont(beta[3])}};
+        k_fold2<<<grid, 256, 0, st>>>(din, dout, n, log_height, bm, bb::to_mont(bb::h_inv(2)), ctx->bb_roots());
+    } else {
+        const uint32_t w = bb::two_adic_generator(unsigned(log_arity));
+        const uint32_t winv = bb::h_pow(w, (uint64_t(1) << log_arity) - 1);
+        const uint32_t ainv = bb::h_pow(bb::h_inv(2), uint64_t(log_arity));
+        if (log_arity == 2)
+            k_fold_general<2><<<grid, 256, 0, st>>>(din, dout, n, log_height, b, bb::to_mont(w), bb::to_mont(winv),
+                                                   bb::to_mont(ainv), ctx->bb_roots());
+        else
+            k_fold_general<3><<<grid, 256, 0, st>>>(din, dout, n, log_height, b, bb::to_mont(w), bb::to_mont(winv),
+                                                   bb::to_mont(ainv), ctx->bb_roots());
+    }
+    P3G_CUDA(cudaGetLastError());
+}
+
+}  // namespace p3g

@@ -1,0 +1,130 @@
+// internal.hpp -- shared host/device declarations of libp3g_gb300 (not public).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "p3g.h"
+#include "fields.cuh"
+
+namespace p3g {
+
+// ----------------------------------------------------------------- errors
+struct Error : std::runtime_error {
+    int status;
+    Error(int s, const std::string& m) : std::runtime_error(m), status(s) {}
+};
+
+#define P3G_CUDA(x)                                                                           \
+    do {                                                                                      \
+        cudaError_t e_ = (x);                                                                 \
+        if (e_ != cudaSuccess) {                                                              \
+            throw ::p3g::Error(e_ == cudaErrorMemoryAllocation ? P3G_ENOMEM : P3G_ECUDA,      \
+                               std::string(#x) + ": " + cudaGetErrorString(e_));              \
+        }                                                                                     \
+    } while (0)
+
+#define P3G_REQUIRE(cond, msg)                                  \
+    do {                                                        \
+        if (!(cond)) throw ::p3g::Error(P3G_EINVAL, (msg));     \
+    } while (0)
+
+// ----------------------------------------------------------------- roots
+// Two-level table of powers of g = omega_{2^TWO_ADICITY} in const form:
+// g^E = lo[E & (2^LB-1)] * hi[E >> LB].
+template <class F>
+struct RootTab {
+    using T = typename F::T;
+    static constexpr int LB = F::TWO_ADICITY == 27 ? 14 : 16;
+    static constexpr uint64_t MASK = (uint64_t(1) << F::TWO_ADICITY) - 1;
+    const T* lo;
+    const T* hi;
+    // g^E, E taken mod 2^TWO_ADICITY.
+    __device__ __forceinline__ T pow(uint64_t e) const {
+        e &= MASK;
+        return F::cmul(lo[e & ((uint64_t(1) << LB) - 1)], hi[e >> LB]);
+    }
+    // omega_{2^k}^e (e may exceed 2^k; reduced mod the order)
+    __device__ __forceinline__ T omega(int k, uint64_t e) const {
+        return pow(e << (F::TWO_ADICITY - k));
+    }
+    __device__ __forceinline__ T omega_inv(int k, uint64_t e) const {
+        return pow((uint64_t(0) - (e << (F::TWO_ADICITY - k))));
+    }
+};
+
+// ----------------------------------------------------------------- Poseidon2 params
+// Constants in the field's const form (BabyBear: Montgomery), passed to
+// kernels by value so that they live in the constant bank.
+struct P2BB16 {
+    uint32_t initial[4][16];
+    uint32_t terminal[4][16];
+    uint32_t internal[32];
+    uint32_t diag[16];  // 2^i in Montgomery form
+};
+struct P2GL8 {
+    uint64_t initial[4][8];
+    uint64_t terminal[4][8];
+    uint64_t internal[32];
+};
+
+}  // namespace p3g
+
+// ----------------------------------------------------------------- context
+struct p3g_ctx {
+    int device = 0;
+    int sm_count = 0;
+    cudaMemPool_t pool = nullptr;
+    // root tables (device, const form)
+    uint32_t* bb_lo = nullptr;
+    uint32_t* bb_hi = nullptr;
+    uint64_t* gl_lo = nullptr;
+    uint64_t* gl_hi = nullptr;
+    // Poseidon2
+    bool has_p2bb = false, has_p2gl = false;
+    int bb_rf = 0, bb_rp = 0, bb_d = 0;
+    int gl_rf = 0, gl_rp = 0, gl_d = 0;
+    p3g::P2BB16 p2bb{};
+    p3g::P2GL8 p2gl{};
+
+    p3g::RootTab<p3g::FBB> bb_roots() const { return {bb_lo, bb_hi}; }
+    p3g::RootTab<p3g::FGL> gl_roots() const { return {gl_lo, gl_hi}; }
+    void* alloc(size_t bytes, cudaStream_t st);
+    void release(void* p, cudaStream_t st);
+};
+
+struct p3g_tree {
+    int field = 0;
+    uint32_t digest = 8;
+    std::vector<uint64_t> layer_size;
+    std::vector<uint64_t> layer_off;  // in digests
+    void* d_digests = nullptr;        // all layers, owned
+    std::vector<p3g_matrix> mats;     // commit order
+    std::vector<void*> owned;         // device buffers owned by the tree (LDEs)
+    bool flat = false;                // commit_matrix tree (zero-padded odd layers)
+};
+
+namespace p3g {
+
+// ----------------------------------------------------------------- entry points
+// (implemented in lde.cu, merkle.cu, fold.cu; called by capi.cu)
+void lde_bb(p3g_ctx* ctx, const uint32_t* in, int log_h, int w, int log_b, uint32_t shift,
+            int bitrev_out, uint32_t* out, cudaStream_t st);
+void lde_gl(p3g_ctx* ctx, const uint64_t* in, int log_h, int w, int log_b, uint64_t shift,
+            int bitrev_out, uint64_t* out, cudaStream_t st);
+
+void mmcs_build(p3g_ctx* ctx, p3g_tree* tree, unsigned cap_height, cudaStream_t st);
+void flat_build(p3g_ctx* ctx, p3g_tree* tree, cudaStream_t st);
+void permute_states(p3g_ctx* ctx, int field, void* d_states, size_t n, cudaStream_t st);
+void open_batch(p3g_ctx* ctx, const p3g_tree* tree, const uint64_t* h_idx, size_t nq,
+                void* h_rows, void* h_proof, cudaStream_t st);
+
+void fold_bb4(p3g_ctx* ctx, const uint32_t* in, int log_height, int log_arity,
+              const uint32_t beta[4], uint32_t* out, cudaStream_t st);
+
+inline int ceil_div(int64_t a, int64_t b) { return int((a + b - 1) / b); }
+
+}  // namespace p3g

@@ -1,0 +1,362 @@
+// lde.cuh -- batched coset low-degree extension (BabyBear, Goldilocks).
+// Templates; lde_bb.cu and lde_gl.cu instantiate one field each.
+//
+// Computes, for a row-major h x w matrix of evaluations on the subgroup of
+// order h, the coset LDE of height H = h * 2^b exactly as the reference's
+// Radix2Dit::coset_lde_batch (radix2_dit.hpp:221-233: idft_batch, zero-pad,
+// coset_dft_batch) followed, when bitrev_out is set, by
+// p3_matrix::reverse_matrix_index_bits (util.hpp:33-45).
+//
+// Algebra used (exact field arithmetic, so results are bit-identical):
+//   c_k = (1/h) sum_i e_i w_h^(-ik)                 (coefficients)
+//   out[t*h + r] = LDE[bitrev_H(t*h + r)] = Y_t[bitrev_h(r)],
+//   Y_t = DFT_h(c_k * g_t^k),  g_t = shift * w_H^(bitrev_b(t)),
+// i.e. the bit-reversed LDE is 2^b independent size-h coset DFTs, each
+// produced in bit-reversed order by a DIF network, so the zero padding is
+// never materialised.
+//
+// h <= 2^10: one kernel; each CTA keeps a whole column tile in shared memory
+// (read the trace once, write the LDE once).
+// 2^10 < h <= 2^21: three passes of a four-step split h = N1 * N2:
+//   pass 1: size-N2 inverse DFTs over rows i1 + N1*i2 (stride N1), twiddle
+//           w_h^(-i1 k2), write scratch row i1 + N1*k2;
+//   pass 2: size-N1 inverse DFT over contiguous rows, then per coset t the
+//           scale c_k * g_t^k, size-N1 forward DFT and twiddle
+//           g_t^(k2) w_h^(k2 m1), write out row t*h + bitrev(m1)*N2 + k2;
+//   pass 3: size-N2 forward DFT over contiguous N2-row blocks, in place.
+#pragma once
+#include "internal.hpp"
+#include "ntt.cuh"
+
+namespace p3g {
+
+template <class F>
+struct LdeCfg;
+template <>
+struct LdeCfg<FBB> {
+    static constexpr int C = 16;     // columns per tile: 64-byte row segments
+    static constexpr int MAXT = 512;
+    static constexpr uint32_t ONE_C = bb::R1;
+};
+template <>
+struct LdeCfg<FGL> {
+    static constexpr int C = 8;
+    static constexpr int MAXT = 256;
+    static constexpr uint64_t ONE_C = 1;
+};
+
+constexpr int LDE_SINGLE_MAX = 10;  // single-kernel LDE up to h = 2^10
+constexpr int LDE_PASS_MAX = 21;    // three-pass LDE up to h = 2^21
+
+// out[i] = scale * base^i, all in const form.
+template <class F>
+__global__ void k_pow_table(typename F::T* out, typename F::T base, typename F::T scale, int n) {
+    using T = typename F::T;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    T r = LdeCfg<F>::ONE_C, b = base;
+    unsigned e = unsigned(i);
+    while (e) {
+        if (e & 1) r = F::cmul(r, b);
+        b = F::cmul(b, b);
+        e >>= 1;
+    }
+    out[i] = F::cmul(r, scale);
+}
+
+// h = 1: the LDE of a constant polynomial is constant.
+template <class F>
+__global__ void k_broadcast_row(const typename F::T* in, typename F::T* out, int w, int rows) {
+    int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= int64_t(rows) * w) return;
+    out[i] = in[i % w];
+}
+
+template <class F, int LOGN>
+struct Tile {
+    using T = typename F::T;
+    static constexpr int C = LdeCfg<F>::C;
+    using Shape = DftShape<LOGN, C, LdeCfg<F>::MAXT>;
+    static constexpr int N = 1 << LOGN;
+    static constexpr int TPC = Shape::TPC;
+    static constexpr int THREADS = Shape::THREADS;
+};
+
+// ------------------------------------------------------------ single kernel
+template <class F, int LOGN>
+__global__ void __launch_bounds__(Tile<F, LOGN>::THREADS)
+k_lde_single(const typename F::T* __restrict__ in, typename F::T* __restrict__ out, int w,
+             int log_b, int bitrev_out, const typename F::T* __restrict__ sq, RootTab<F> roots) {
+    using TL = Tile<F, LOGN>;
+    using T = typename F::T;
+    constexpr int N = TL::N, C = TL::C, TPC = TL::TPC, NT = TL::THREADS;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* tw = reinterpret_cast<T*>(smem_raw);
+    T* pre = tw + N;
+    T* A = pre + N;
+    T* B = A + N * C;
+    const int tid = threadIdx.x, c = tid % C, t = tid / C;
+    const int col = blockIdx.y * C + c;
+    const bool ok = col < w;
+    const int logH = LOGN + log_b;
+
+    for (int e = tid; e < N; e += NT) tw[e] = roots.omega_inv(LOGN, e);
+    for (int i = t; i < N; i += TPC) A[i * C + c] = ok ? in[size_t(i) * w + col] : T(0);
+    __syncthreads();
+    cta_dif<F, LOGN, C, TPC, 1>(A, tw, t, c);
+    for (int e = tid; e < N; e += NT) tw[e] = roots.omega(LOGN, e);
+    for (int tc = 0; tc < (1 << log_b); ++tc) {
+        const uint64_t u = bitrev_dev(unsigned(tc), log_b);
+        for (int k = tid; k < N; k += NT) pre[k] = F::cmul(sq[k], roots.omega(logH, u * k));
+        __syncthreads();
+        for (int k = t; k < N; k += TPC) B[k * C + c] = F::mulc(A[bitrev_dev(k, LOGN) * C + c], pre[k]);
+        __syncthreads();
+        cta_dif<F, LOGN, C, TPC, 0>(B, tw, t, c);
+        if (ok) {
+            for (int s = t; s < N; s += TPC) {
+                uint64_t row = uint64_t(tc) * N + s;
+                if (!bitrev_out) row = bitrev_dev(unsigned(row), logH);
+                out[row * w + col] = B[s * C + c];
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// ------------------------------------------------------------ pass 1 (LOGN = n2)
+template <class F, int LOGN>
+__global__ void __launch_bounds__(Tile<F, LOGN>::THREADS)
+k_lde_pass1(const typename F::T* __restrict__ in, typename F::T* __restrict__ scratch, int w, int n1,
+            RootTab<F> roots) {
+    using TL = Tile<F, LOGN>;
+    using T = typename F::T;
+    constexpr int N = TL::N, C = TL::C, TPC = TL::TPC, NT = TL::THREADS;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* tw = reinterpret_cast<T*>(smem_raw);
+    T* post = tw + N;
+    T* A = post + N;
+    const int tid = threadIdx.x, c = tid % C, t = tid / C;
+    const int col = blockIdx.y * C + c;
+    const bool ok = col < w;
+    const int64_t i1 = blockIdx.x;
+    const int64_t N1 = int64_t(1) << n1;
+    const int n = n1 + LOGN;
+
+    for (int e = tid; e < N; e += NT) {
+        tw[e] = roots.omega_inv(LOGN, e);
+        post[e] = roots.omega_inv(n, uint64_t(i1) * bitrev_dev(e, LOGN));
+    }
+    for (int i = t; i < N; i += TPC) A[i * C + c] = ok ? in[(i1 + N1 * i) * w + col] : T(0);
+    __syncthreads();
+    cta_dif<F, LOGN, C, TPC, 1>(A, tw, t, c);
+    if (ok) {
+        for (int p = t; p < N; p += TPC)
+            scratch[(i1 + N1 * int64_t(bitrev_dev(p, LOGN))) * w + col] = F::mulc(A[p * C + c], post[p]);
+    }
+}
+
+// ------------------------------------------------------------ pass 2 (LOGN = n1)
+template <class F, int LOGN>
+__global__ void __launch_bounds__(Tile<F, LOGN>::THREADS)
+k_lde_pass2(const typename F::T* __restrict__ scratch, typename F::T* __restrict__ dst, int w, int n2,
+            int log_b, const typename F::T* __restrict__ sp, const typename F::T* __restrict__ sq,
+            RootTab<F> roots) {
+    using TL = Tile<F, LOGN>;
+    using T = typename F::T;
+    constexpr int N = TL::N, C = TL::C, TPC = TL::TPC, NT = TL::THREADS;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* tw = reinterpret_cast<T*>(smem_raw);
+    T* pre = tw + N;
+    T* post = pre + N;
+    T* A = post + N;
+    T* B = A + N * C;
+    const int tid = threadIdx.x, c = tid % C, t = tid / C;
+    const int col = blockIdx.y * C + c;
+    const bool ok = col < w;
+    const int64_t k2 = blockIdx.x;
+    const int64_t N2 = int64_t(1) << n2;
+    const int n = LOGN + n2;
+    const int64_t h = int64_t(1) << n;
+    const int logH = n + log_b;
+
+    for (int e = tid; e < N; e += NT) tw[e] = roots.omega_inv(LOGN, e);
+    for (int i = t; i < N; i += TPC) A[i * C + c] = ok ? scratch[(int64_t(N) * k2 + i) * w + col] : T(0);
+    __syncthreads();
+    cta_dif<F, LOGN, C, TPC, 1>(A, tw, t, c);
+    for (int e = tid; e < N; e += NT) tw[e] = roots.omega(LOGN, e);
+    const T sqk2 = sq[k2];
+    for (int tc = 0; tc < (1 << log_b); ++tc) {
+        const uint64_t u = bitrev_dev(unsigned(tc), log_b);
+        for (int k = tid; k < N; k += NT) {
+            pre[k] = F::cmul(sp[k], roots.omega(logH, u * uint64_t(N2) * k));
+            post[k] = F::cmul(sqk2, roots.omega(logH, uint64_t(k2) * (u + (uint64_t(bitrev_dev(k, LOGN)) << log_b))));
+        }
+        __syncthreads();
+        for (int k = t; k < N; k += TPC) B[k * C + c] = F::mulc(A[bitrev_dev(k, LOGN) * C + c], pre[k]);
+        __syncthreads();
+        cta_dif<F, LOGN, C, TPC, 0>(B, tw, t, c);
+        if (ok) {
+            for (int s = t; s < N; s += TPC)
+                dst[(tc * h + s * N2 + k2) * w + col] = F::mulc(B[s * C + c], post[s]);
+        }
+        __syncthreads();
+    }
+}
+
+// ------------------------------------------------------------ pass 3 (LOGN = n2)
+template <class F, int LOGN>
+__global__ void __launch_bounds__(Tile<F, LOGN>::THREADS)
+k_lde_pass3(const typename F::T* src, typename F::T* out, int w, int n1, int log_b, int bitrev_out,
+            RootTab<F> roots) {
+    using TL = Tile<F, LOGN>;
+    using T = typename F::T;
+    constexpr int N = TL::N, C = TL::C, TPC = TL::TPC, NT = TL::THREADS;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* tw = reinterpret_cast<T*>(smem_raw);
+    T* A = tw + N;
+    const int tid = threadIdx.x, c = tid % C, t = tid / C;
+    const int col = blockIdx.y * C + c;
+    const bool ok = col < w;
+    const int64_t blk = blockIdx.x;
+    const int n = n1 + LOGN;
+    const int logH = n + log_b;
+    const int64_t base = blk * N;  // = t*h + s1*N2
+
+    for (int e = tid; e < N; e += NT) tw[e] = roots.omega(LOGN, e);
+    for (int i = t; i < N; i += TPC) A[i * C + c] = ok ? src[(base + i) * w + col] : T(0);
+    __syncthreads();
+    cta_dif<F, LOGN, C, TPC, 0>(A, tw, t, c);
+    if (ok) {
+        for (int s = t; s < N; s += TPC) {
+            uint64_t row = uint64_t(base + s);
+            if (!bitrev_out) row = bitrev_dev(unsigned(row), logH);
+            out[row * w + col] = A[s * C + c];
+        }
+    }
+}
+
+// ------------------------------------------------------------ host side
+template <class Kern>
+static void set_smem(Kern k, size_t bytes) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    P3G_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(bytes)));
+    (void)dev;
+}
+
+template <class F, int LOGN>
+static void launch_single(const typename F::T* in, typename F::T* out, int w, int log_b, int br,
+                          const typename F::T* sq, RootTab<F> roots, cudaStream_t st) {
+    using TL = Tile<F, LOGN>;
+    size_t smem = (2 * TL::N + 2 * TL::N * TL::C) * sizeof(typename F::T);
+    auto k = k_lde_single<F, LOGN>;
+    set_smem(k, smem);
+    dim3 grid(1, ceil_div(w, TL::C));
+    k<<<grid, TL::THREADS, smem, st>>>(in, out, w, log_b, br, sq, roots);
+    P3G_CUDA(cudaGetLastError());
+}
+template <class F, int LOGN>
+static void launch_pass1(const typename F::T* in, typename F::T* scr, int w, int n1, RootTab<F> roots,
+                         cudaStream_t st) {
+    using TL = Tile<F, LOGN>;
+    size_t smem = (2 * TL::N + TL::N * TL::C) * sizeof(typename F::T);
+    auto k = k_lde_pass1<F, LOGN>;
+    set_smem(k, smem);
+    dim3 grid(1u << n1, ceil_div(w, TL::C));
+    k<<<grid, TL::THREADS, smem, st>>>(in, scr, w, n1, roots);
+    P3G_CUDA(cudaGetLastError());
+}
+template <class F, int LOGN>
+static void launch_pass2(const typename F::T* scr, typename F::T* dst, int w, int n2, int log_b,
+                         const typename F::T* sp, const typename F::T* sq, RootTab<F> roots, cudaStream_t st) {
+    using TL = Tile<F, LOGN>;
+    size_t smem = (3 * TL::N + 2 * TL::N * TL::C) * sizeof(typename F::T);
+    auto k = k_lde_pass2<F, LOGN>;
+    set_smem(k, smem);
+    dim3 grid(1u << n2, ceil_div(w, TL::C));
+    k<<<grid, TL::THREADS, smem, st>>>(scr, dst, w, n2, log_b, sp, sq, roots);
+    P3G_CUDA(cudaGetLastError());
+}
+template <class F, int LOGN>
+static void launch_pass3(const typename F::T* src, typename F::T* out, int w, int n1, int log_b, int br,
+                         RootTab<F> roots, cudaStream_t st) {
+    using TL = Tile<F, LOGN>;
+    size_t smem = (TL::N + TL::N * TL::C) * sizeof(typename F::T);
+    auto k = k_lde_pass3<F, LOGN>;
+    set_smem(k, smem);
+    dim3 grid(1u << (n1 + log_b), ceil_div(w, TL::C));
+    k<<<grid, TL::THREADS, smem, st>>>(src, out, w, n1, log_b, br, roots);
+    P3G_CUDA(cudaGetLastError());
+}
+
+#define P3G_CASES_1_11(M) M(1) M(2) M(3) M(4) M(5) M(6) M(7) M(8) M(9) M(10) M(11)
+
+template <class F>
+static void pow_table(typename F::T* out, uint64_t base, uint64_t scale, int n, cudaStream_t st) {
+    k_pow_table<F><<<ceil_div(n, 256), 256, 0, st>>>(out, F::to_const(base), F::to_const(scale), n);
+    P3G_CUDA(cudaGetLastError());
+}
+
+template <class F>
+static void lde_impl(p3g_ctx* ctx, const typename F::T* in, int log_h, int w, int log_b, uint64_t shift,
+                     int bitrev_out, typename F::T* out, cudaStream_t st, RootTab<F> roots) {
+    using T = typename F::T;
+    P3G_REQUIRE(log_h >= 0 && log_b >= 0, "coset_lde: negative size");
+    P3G_REQUIRE(log_h + log_b <= int(F::TWO_ADICITY), "coset_lde: log_h + log_blowup exceeds two-adicity");
+    if (log_h > LDE_PASS_MAX) throw Error(P3G_EUNSUPPORTED, "coset_lde: log_h > 21 is not supported");
+    P3G_REQUIRE(shift % F::P != 0, "coset_lde: shift must be non-zero");
+    if (w == 0) return;
+    shift %= F::P;
+    const int64_t h = int64_t(1) << log_h;
+    if (log_h == 0) {
+        int64_t total = (int64_t(1) << log_b) * w;
+        k_broadcast_row<F><<<ceil_div(total, 256), 256, 0, st>>>(in, out, w, int(1 << log_b));
+        P3G_CUDA(cudaGetLastError());
+        return;
+    }
+    const uint64_t inv_h = F::h_inv(uint64_t(h) % F::P);
+    if (log_h <= LDE_SINGLE_MAX) {
+        T* sq = static_cast<T*>(ctx->alloc(sizeof(T) * h, st));
+        pow_table<F>(sq, shift, inv_h, int(h), st);
+        switch (log_h) {
+#define C_(L) case L: launch_single<F, L>(in, out, w, log_b, bitrev_out, sq, roots, st); break;
+            C_(1) C_(2) C_(3) C_(4) C_(5) C_(6) C_(7) C_(8) C_(9) C_(10)
+#undef C_
+        }
+        ctx->release(sq, st);
+        return;
+    }
+    const int n2 = (log_h + 1) / 2, n1 = log_h - n2;
+    const int64_t N1 = int64_t(1) << n1, N2 = int64_t(1) << n2;
+    const int64_t H = h << log_b;
+    T* sp = static_cast<T*>(ctx->alloc(sizeof(T) * N1, st));
+    T* sq = static_cast<T*>(ctx->alloc(sizeof(T) * N2, st));
+    T* scr = static_cast<T*>(ctx->alloc(sizeof(T) * size_t(h) * w, st));
+    T* mid = bitrev_out ? out : static_cast<T*>(ctx->alloc(sizeof(T) * size_t(H) * w, st));
+    pow_table<F>(sp, F::h_pow(shift, uint64_t(N2)), inv_h, int(N1), st);
+    pow_table<F>(sq, shift, 1, int(N2), st);
+    switch (n2) {
+#define C_(L) case L: launch_pass1<F, L>(in, scr, w, n1, roots, st); break;
+        P3G_CASES_1_11(C_)
+#undef C_
+        default: throw Error(P3G_EUNSUPPORTED, "coset_lde: pass-1 size");
+    }
+    switch (n1) {
+#define C_(L) case L: launch_pass2<F, L>(scr, mid, w, n2, log_b, sp, sq, roots, st); break;
+        P3G_CASES_1_11(C_)
+#undef C_
+        default: throw Error(P3G_EUNSUPPORTED, "coset_lde: pass-2 size");
+    }
+    switch (n2) {
+#define C_(L) case L: launch_pass3<F, L>(mid, out, w, n1, log_b, bitrev_out, roots, st); break;
+        P3G_CASES_1_11(C_)
+#undef C_
+        default: throw Error(P3G_EUNSUPPORTED, "coset_lde: pass-3 size");
+    }
+    ctx->release(scr, st);
+    ctx->release(sp, st);
+    ctx->release(sq, st);
+    if (!bitrev_out) ctx->release(mid, st);
+}
+
+}  // namespace p3g

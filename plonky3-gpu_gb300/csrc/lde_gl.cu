@@ -1,0 +1,11 @@
+// lde_gl.cu -- Goldilocks instantiation of the coset LDE (lde.cuh).
+#include "lde.cuh"
+
+namespace p3g {
+
+void lde_gl(p3g_ctx* ctx, const uint64_t* in, int log_h, int w, int log_b, uint64_t shift, int bitrev_out,
+            uint64_t* out, cudaStream_t st) {
+    lde_impl<FGL>(ctx, in, log_h, w, log_b, shift, bitrev_out, out, st, ctx->gl_roots());
+}
+
+}  // namespace p3g

@@ -1,0 +1,272 @@
+// merkle.cu -- Poseidon2 MerkleTreeMmcs commit on the GPU.
+//
+// Mixed-height tree, as the reference's build_merkle_tree
+// (merkle_tree.hpp:84-185): matrices are stable-sorted by height (desc);
+// leaf i = PaddingFreeSponge over the concatenation of row i of every tallest
+// matrix (padding_free_sponge.hpp:63-113, overwrite absorb, a partial last
+// chunk is permuted, empty input gives the zero digest); each level
+// compresses pairs with TruncatedPermutation (truncated_permutation.hpp:61-76)
+// and, where some matrices have the level's height, replaces node i by
+// compress(node i, hash(row i of those matrices)); the tree stops at
+// 2^cap_height nodes.
+//
+// The leaf kernel reads every row straight from HBM (one thread per row, no
+// host-side concatenation) with the Poseidon2 state in registers; one kernel
+// per level computes the compressions and the injection together.  All digest
+// layers stay resident on the device for openings.
+#include <algorithm>
+#include <numeric>
+#include <type_traits>
+
+#include "merkle.cuh"
+
+namespace p3g {
+
+extern template struct Launch<HBB, 7, 8, 13>;
+extern template struct Launch<HBB, 7, 8, 22>;
+extern template struct Launch<HBB, 5, 8, 14>;
+extern template struct Launch<HGL, 7, 8, 22>;
+
+// Opening: query q gathers row index/(max_h/h_i) of each matrix and the
+// sibling digest of every layer below the top (merkle_tree_mmcs.hpp:120-152).
+struct OpenMat {
+    const void* ptr;
+    uint64_t height;
+    uint32_t width;
+    uint32_t row_off;  // element offset in the query's row block
+};
+template <class T>
+__global__ void k_open(const OpenMat* mats, int nmats, uint64_t max_h, const uint64_t* idx, const T* digests,
+                       const uint64_t* layer_off, const uint64_t* layer_size, int nproof, int dig, int flat,
+                       T* rows_out, uint32_t row_elems, T* proof_out) {
+    const int q = blockIdx.x;
+    const uint64_t index = idx[q];
+    for (int m = 0; m < nmats; ++m) {
+        const OpenMat om = mats[m];
+        const uint64_t row = flat ? index : index / (max_h / om.height);
+        const T* src = static_cast<const T*>(om.ptr) + row * om.width;
+        for (uint32_t c = threadIdx.x; c < om.width; c += blockDim.x)
+            rows_out[uint64_t(q) * row_elems + om.row_off + c] = src[c];
+    }
+    for (int l = threadIdx.x; l < nproof; l += blockDim.x) {
+        const uint64_t sib = (index >> l) ^ 1;
+        for (int e = 0; e < dig; ++e) {
+            T v = 0;
+            if (sib < layer_size[l]) v = digests[(layer_off[l] + sib) * dig + e];
+            proof_out[(uint64_t(q) * nproof + l) * dig + e] = v;
+        }
+    }
+}
+
+template <class H>
+struct LeafFn {
+    const typename H::Params* p;
+    const Group<typename H::T>* g;
+    typename H::T* out;
+    uint64_t rows;
+    cudaStream_t st;
+    template <int D, int RF, int RP>
+    void operator()() const { Launch<H, D, RF, RP>::leaf(*p, *g, out, rows, st); }
+};
+template <class H>
+struct LevelFn {
+    const typename H::Params* p;
+    const typename H::T* child;
+    uint64_t nchild;
+    typename H::T* parent;
+    uint64_t npar;
+    const typename H::T* inj;
+    cudaStream_t st;
+    template <int D, int RF, int RP>
+    void operator()() const { Launch<H, D, RF, RP>::level(*p, child, nchild, parent, npar, inj, st); }
+};
+template <class H>
+struct PermFn {
+    const typename H::Params* p;
+    typename H::T* s;
+    uint64_t n;
+    cudaStream_t st;
+    template <int D, int RF, int RP>
+    void operator()() const { Launch<H, D, RF, RP>::permute(*p, s, n, st); }
+};
+
+// Calls fn.template operator()<D, RF, RP>() for a supported round schedule.
+template <class Fn>
+static void dispatch_bb(const p3g_ctx* ctx, const Fn& fn) {
+    if (!ctx->has_p2bb) throw Error(P3G_ESTATE, "Poseidon2 constants for BabyBear are not set");
+    const int d = ctx->bb_d, rf = ctx->bb_rf, rp = ctx->bb_rp;
+    if (rf == 8 && d == 7 && rp == 13) return fn.template operator()<7, 8, 13>();
+    if (rf == 8 && d == 7 && rp == 22) return fn.template operator()<7, 8, 22>();
+    if (rf == 8 && d == 5 && rp == 14) return fn.template operator()<5, 8, 14>();
+    throw Error(P3G_EUNSUPPORTED, "BabyBear Poseidon2 schedule not built (supported: x^7 8+13, x^7 8+22, x^5 8+14)");
+}
+template <class Fn>
+static void dispatch_gl(const p3g_ctx* ctx, const Fn& fn) {
+    if (!ctx->has_p2gl) throw Error(P3G_ESTATE, "Poseidon2 constants for Goldilocks are not set");
+    const int d = ctx->gl_d, rf = ctx->gl_rf, rp = ctx->gl_rp;
+    if (rf == 8 && d == 7 && rp == 22) return fn.template operator()<7, 8, 22>();
+    throw Error(P3G_EUNSUPPORTED, "Goldilocks Poseidon2 schedule not built (supported: x^7 8+22)");
+}
+
+template <class T>
+static Group<T> make_group(const std::vector<p3g_matrix>& mats, const std::vector<size_t>& idx) {
+    Group<T> g;
+    if (idx.size() > size_t(MAXG)) throw Error(P3G_EUNSUPPORTED, "more than 64 matrices of one height");
+    g.n = int(idx.size());
+    for (size_t i = 0; i < idx.size(); ++i) {
+        g.ptr[i] = static_cast<const T*>(mats[idx[i]].d_data);
+        g.w[i] = mats[idx[i]].width;
+    }
+    g.vec = 0;
+    if (g.n == 1 && sizeof(T) == 4 && (g.w[0] % 4) == 0 && (reinterpret_cast<uintptr_t>(g.ptr[0]) % 16) == 0)
+        g.vec = 1;
+    return g;
+}
+
+template <class H>
+static void build_tree(p3g_ctx* ctx, p3g_tree* tree, unsigned cap_height, const typename H::Params& p,
+                       cudaStream_t st, bool flat) {
+    using T = typename H::T;
+    const auto& mats = tree->mats;
+    const size_t n = mats.size();
+    tree->digest = H::DIG;
+    std::vector<size_t> order(n);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(),
+                     [&](size_t a, size_t b) { return mats[a].height > mats[b].height; });
+    const uint64_t max_h = mats[order[0]].height;
+    // layer geometry
+    tree->layer_size.clear();
+    tree->layer_off.clear();
+    uint64_t total = 0, sz = max_h;
+    tree->layer_size.push_back(sz);
+    tree->layer_off.push_back(0);
+    total += sz;
+    if (flat) {
+        while (sz > 1) {
+            sz = (sz + 1) / 2;
+            tree->layer_off.push_back(total);
+            tree->layer_size.push_back(sz);
+            total += sz;
+        }
+    } else {
+        const uint64_t cap = uint64_t(1) << cap_height;
+        while (sz > cap) {
+            sz /= 2;
+            tree->layer_off.push_back(total);
+            tree->layer_size.push_back(sz);
+            total += sz;
+        }
+    }
+    T* dig = static_cast<T*>(ctx->alloc(sizeof(T) * H::DIG * total, st));
+    tree->d_digests = dig;
+
+    size_t next = 0;
+    auto collect = [&](uint64_t h) {
+        std::vector<size_t> g;
+        while (next < n && mats[order[next]].height == h) g.push_back(order[next++]);
+        return g;
+    };
+    auto tall = collect(max_h);
+    Group<T> g0 = make_group<T>(mats, tall);
+    auto run = [&](const auto& fnobj) {
+        if constexpr (std::is_same<H, HBB>::value) dispatch_bb(ctx, fnobj);
+        else dispatch_gl(ctx, fnobj);
+    };
+    run(LeafFn<H>{&p, &g0, dig, max_h, st});
+    T* inj_buf = nullptr;  // row hashes of the matrices injected at a level
+    for (size_t l = 1; l < tree->layer_size.size(); ++l) {
+        const uint64_t level = tree->layer_size[l];
+        const T* inj = nullptr;
+        if (!flat) {
+            auto gi = collect(level);
+            if (!gi.empty()) {
+                Group<T> ig = make_group<T>(mats, gi);
+                if (!inj_buf) inj_buf = static_cast<T*>(ctx->alloc(sizeof(T) * H::DIG * level, st));
+                run(LeafFn<H>{&p, &ig, inj_buf, level, st});
+                inj = inj_buf;
+            }
+        }
+        run(LevelFn<H>{&p, dig + tree->layer_off[l - 1] * H::DIG, tree->layer_size[l - 1],
+                       dig + tree->layer_off[l] * H::DIG, level, inj, st});
+    }
+    if (inj_buf) ctx->release(inj_buf, st);
+}
+
+void mmcs_build(p3g_ctx* ctx, p3g_tree* tree, unsigned cap_height, cudaStream_t st) {
+    P3G_REQUIRE(!tree->mats.empty(), "mmcs_commit: need at least one matrix");
+    for (const auto& m : tree->mats) {
+        P3G_REQUIRE(m.height > 0 && (m.height & (m.height - 1)) == 0, "mmcs_commit: matrix height must be a power of two");
+        P3G_REQUIRE(m.width == 0 || m.d_data != nullptr, "mmcs_commit: null matrix data");
+    }
+    P3G_REQUIRE(cap_height < 63, "mmcs_commit: cap_height too large");
+    tree->flat = false;
+    if (tree->field == P3G_BABYBEAR) build_tree<HBB>(ctx, tree, cap_height, ctx->p2bb, st, false);
+    else build_tree<HGL>(ctx, tree, cap_height, ctx->p2gl, st, false);
+}
+
+void flat_build(p3g_ctx* ctx, p3g_tree* tree, cudaStream_t st) {
+    P3G_REQUIRE(tree->mats.size() == 1, "commit_matrix: one matrix");
+    P3G_REQUIRE(tree->mats[0].height > 0 && tree->mats[0].width > 0, "commit_matrix: bad dimensions");
+    tree->flat = true;
+    if (tree->field == P3G_BABYBEAR) build_tree<HBB>(ctx, tree, 0, ctx->p2bb, st, true);
+    else build_tree<HGL>(ctx, tree, 0, ctx->p2gl, st, true);
+}
+
+void permute_states(p3g_ctx* ctx, int field, void* d_states, size_t n, cudaStream_t st) {
+    if (field == P3G_BABYBEAR)
+        dispatch_bb(ctx, PermFn<HBB>{&ctx->p2bb, static_cast<uint32_t*>(d_states), n, st});
+    else
+        dispatch_gl(ctx, PermFn<HGL>{&ctx->p2gl, static_cast<uint64_t*>(d_states), n, st});
+}
+
+void open_batch(p3g_ctx* ctx, const p3g_tree* tree, const uint64_t* h_idx, size_t nq, void* h_rows,
+                void* h_proof, cudaStream_t st) {
+    if (nq == 0) return;
+    const size_t esz = tree->field == P3G_BABYBEAR ? 4 : 8;
+    const uint64_t max_h = tree->layer_size[0];
+    for (size_t q = 0; q < nq; ++q) P3G_REQUIRE(h_idx[q] < max_h, "open_batch: index out of range");
+    std::vector<OpenMat> om(tree->mats.size());
+    uint32_t row_elems = 0;
+    for (size_t i = 0; i < om.size(); ++i) {
+        om[i] = {tree->mats[i].d_data, tree->mats[i].height, tree->mats[i].width, row_elems};
+        row_elems += tree->mats[i].width;
+    }
+    const int nproof = int(tree->layer_size.size()) - 1;
+    const size_t dig = tree->digest;
+    // one device staging block: descriptors, indices, layer tables, outputs
+    size_t off = 0;
+    auto take = [&](size_t bytes) { size_t o = off; off += (bytes + 255) / 256 * 256; return o; };
+    const size_t o_mats = take(sizeof(OpenMat) * om.size());
+    const size_t o_idx = take(8 * nq);
+    const size_t o_loff = take(8 * tree->layer_off.size());
+    const size_t o_lsz = take(8 * tree->layer_size.size());
+    const size_t rows_bytes = esz * row_elems * nq, proof_bytes = esz * dig * size_t(std::max(nproof, 0)) * nq;
+    const size_t o_rows = take(rows_bytes);
+    const size_t o_proof = take(proof_bytes);
+    char* buf = static_cast<char*>(ctx->alloc(off, st));
+    P3G_CUDA(cudaMemcpyAsync(buf + o_mats, om.data(), sizeof(OpenMat) * om.size(), cudaMemcpyHostToDevice, st));
+    P3G_CUDA(cudaMemcpyAsync(buf + o_idx, h_idx, 8 * nq, cudaMemcpyHostToDevice, st));
+    P3G_CUDA(cudaMemcpyAsync(buf + o_loff, tree->layer_off.data(), 8 * tree->layer_off.size(), cudaMemcpyHostToDevice, st));
+    P3G_CUDA(cudaMemcpyAsync(buf + o_lsz, tree->layer_size.data(), 8 * tree->layer_size.size(), cudaMemcpyHostToDevice, st));
+    if (esz == 4) {
+        k_open<uint32_t><<<unsigned(nq), 128, 0, st>>>(
+            reinterpret_cast<OpenMat*>(buf + o_mats), int(om.size()), max_h, reinterpret_cast<uint64_t*>(buf + o_idx),
+            static_cast<const uint32_t*>(tree->d_digests), reinterpret_cast<uint64_t*>(buf + o_loff),
+            reinterpret_cast<uint64_t*>(buf + o_lsz), nproof, int(dig), tree->flat ? 1 : 0,
+            reinterpret_cast<uint32_t*>(buf + o_rows), row_elems, reinterpret_cast<uint32_t*>(buf + o_proof));
+    } else {
+        k_open<uint64_t><<<unsigned(nq), 128, 0, st>>>(
+            reinterpret_cast<OpenMat*>(buf + o_mats), int(om.size()), max_h, reinterpret_cast<uint64_t*>(buf + o_idx),
+            static_cast<const uint64_t*>(tree->d_digests), reinterpret_cast<uint64_t*>(buf + o_loff),
+            reinterpret_cast<uint64_t*>(buf + o_lsz), nproof, int(dig), tree->flat ? 1 : 0,
+            reinterpret_cast<uint64_t*>(buf + o_rows), row_elems, reinterpret_cast<uint64_t*>(buf + o_proof));
+    }
+    P3G_CUDA(cudaGetLastError());
+    if (h_rows && rows_bytes) P3G_CUDA(cudaMemcpyAsync(h_rows, buf + o_rows, rows_bytes, cudaMemcpyDeviceToHost, st));
+    if (h_proof && proof_bytes) P3G_CUDA(cudaMemcpyAsync(h_proof, buf + o_proof, proof_bytes, cudaMemcpyDeviceToHost, st));
+    ctx->release(buf, st);
+    P3G_CUDA(cudaStreamSynchronize(st));
+}
+
+}  // namespace p3g

@@ -1,0 +1,175 @@
+// merkle.cuh -- Poseidon2 Merkle kernels (templates; instantiated per round
+// schedule in merkle_s*.cu so that the unrolled permutations compile in
+// parallel translation units).
+//
+// Every kernel has exactly one call site of the unrolled permutation: the
+// sponge loop fills one rate chunk per iteration, and a compression with an
+// injected row hash runs its two permutations as two iterations of one loop.
+#pragma once
+#include <type_traits>
+
+#include "internal.hpp"
+#include "poseidon2.cuh"
+
+namespace p3g {
+
+constexpr int MAXG = 64;  // matrices per equal-height group (kernel-parameter space)
+
+template <class T>
+struct Group {
+    int n = 0;
+    int vec = 0;  // single matrix, width % 4 == 0, 16-byte aligned rows (BabyBear)
+    const T* ptr[MAXG];
+    uint32_t w[MAXG];
+};
+
+// Sponge over the concatenated row r of the group (overwrite absorb,
+// padding_free_sponge.hpp:63-87); leaves the state (internal form) in s.
+template <class H, int D, int RF, int RP>
+__device__ __forceinline__ void hash_group(const Group<typename H::T>& g, uint64_t r,
+                                           const typename H::Params& p, typename H::T* s) {
+    using T = typename H::T;
+#pragma unroll
+    for (int i = 0; i < H::W; ++i) s[i] = 0;
+    int m = 0;
+    uint32_t c = 0;
+#pragma unroll 1
+    for (;;) {
+        int filled = 0;
+        if (g.n == 1) {
+            const uint32_t w = g.w[0];
+            const T* row = g.ptr[0] + r * w;
+            bool done = false;
+            if constexpr (std::is_same<T, uint32_t>::value) {
+                if (g.vec && c + 8 <= w) {
+                    const uint4* rv = reinterpret_cast<const uint4*>(row + c);
+                    uint4 a = __ldg(rv), b = __ldg(rv + 1);
+                    s[0] = H::absorb(a.x); s[1] = H::absorb(a.y); s[2] = H::absorb(a.z); s[3] = H::absorb(a.w);
+                    s[4] = H::absorb(b.x); s[5] = H::absorb(b.y); s[6] = H::absorb(b.z); s[7] = H::absorb(b.w);
+                    filled = 8;
+                    done = true;
+                }
+            }
+            if (!done) {
+#pragma unroll
+                for (int i = 0; i < H::RATE; ++i)
+                    if (c + i < w) s[i] = H::absorb(__ldg(row + c + i));
+                filled = c < w ? int(min(uint32_t(H::RATE), w - c)) : 0;
+            }
+            c += filled;
+        } else {
+#pragma unroll
+            for (int i = 0; i < H::RATE; ++i) {
+                if (filled == i) {
+                    while (m < g.n && c >= g.w[m]) {
+                        ++m;
+                        c = 0;
+                    }
+                    if (m < g.n) {
+                        s[i] = H::absorb(__ldg(g.ptr[m] + r * g.w[m] + c));
+                        ++c;
+                        filled = i + 1;
+                    }
+                }
+            }
+        }
+        if (filled == 0) break;
+        H::template perm<D, RF, RP>(s, p);
+        if (filled < H::RATE) break;
+    }
+}
+
+template <class H, int D, int RF, int RP>
+__global__ void __launch_bounds__(128) k_leaf_hash(typename H::Params p, Group<typename H::T> g,
+                                                   typename H::T* __restrict__ out, uint64_t nrows) {
+    using T = typename H::T;
+    uint64_t r = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (r >= nrows) return;
+    T s[H::W];
+    hash_group<H, D, RF, RP>(g, r, p, s);
+#pragma unroll
+    for (int i = 0; i < H::DIG; ++i) out[r * H::DIG + i] = H::squeeze(s[i]);
+}
+
+// parent[j] = compress(child[2j], child[2j+1] or the zero digest); with inj,
+// parent[j] = compress(parent[j], inj[j]) (merkle_tree.hpp:149-176,
+// fri_merkle_tree_mmcs.hpp:77-92).
+template <class H, int D, int RF, int RP>
+__global__ void __launch_bounds__(128) k_compress_level(typename H::Params p, const typename H::T* __restrict__ child,
+                                                        uint64_t nchild, typename H::T* __restrict__ parent,
+                                                        uint64_t nparent, const typename H::T* __restrict__ inj) {
+    using T = typename H::T;
+    uint64_t j = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (j >= nparent) return;
+    T s[H::W];
+    const int iters = inj ? 2 : 1;
+#pragma unroll 1
+    for (int it = 0; it < iters; ++it) {
+        if (it == 0) {
+#pragma unroll
+            for (int i = 0; i < H::W; ++i) s[i] = 0;
+#pragma unroll
+            for (int i = 0; i < H::DIG; ++i) s[i] = H::absorb(child[2 * j * H::DIG + i]);
+            if (2 * j + 1 < nchild) {
+#pragma unroll
+                for (int i = 0; i < H::DIG; ++i) s[H::DIG + i] = H::absorb(child[(2 * j + 1) * H::DIG + i]);
+            }
+        } else {
+#pragma unroll
+            for (int i = 0; i < H::DIG; ++i) s[H::DIG + i] = H::absorb(inj[j * H::DIG + i]);
+#pragma unroll
+            for (int i = 2 * H::DIG; i < H::W; ++i) s[i] = 0;
+        }
+        H::template perm<D, RF, RP>(s, p);
+    }
+#pragma unroll
+    for (int i = 0; i < H::DIG; ++i) parent[j * H::DIG + i] = H::squeeze(s[i]);
+}
+
+template <class H, int D, int RF, int RP>
+__global__ void __launch_bounds__(128) k_permute(typename H::Params p, typename H::T* states, uint64_t n) {
+    using T = typename H::T;
+    uint64_t j = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    T s[H::W];
+#pragma unroll
+    for (int i = 0; i < H::W; ++i) s[i] = H::absorb(states[j * H::W + i]);
+    H::template perm<D, RF, RP>(s, p);
+#pragma unroll
+    for (int i = 0; i < H::W; ++i) states[j * H::W + i] = H::squeeze(s[i]);
+}
+
+// Host launchers, explicitly instantiated once per schedule.
+template <class H, int D, int RF, int RP>
+struct Launch {
+    using T = typename H::T;
+    static void leaf(const typename H::Params& p, const Group<T>& g, T* out, uint64_t nrows, cudaStream_t st);
+    static void level(const typename H::Params& p, const T* child, uint64_t nchild, T* parent, uint64_t nparent,
+                      const T* inj, cudaStream_t st);
+    static void permute(const typename H::Params& p, T* states, uint64_t n, cudaStream_t st);
+};
+
+#ifdef P3G_MERKLE_INSTANTIATE
+template <class H, int D, int RF, int RP>
+void Launch<H, D, RF, RP>::leaf(const typename H::Params& p, const Group<T>& g, T* out, uint64_t nrows,
+                                cudaStream_t st) {
+    if (nrows == 0) return;
+    k_leaf_hash<H, D, RF, RP><<<unsigned((nrows + 127) / 128), 128, 0, st>>>(p, g, out, nrows);
+    P3G_CUDA(cudaGetLastError());
+}
+template <class H, int D, int RF, int RP>
+void Launch<H, D, RF, RP>::level(const typename H::Params& p, const T* child, uint64_t nchild, T* parent,
+                                 uint64_t nparent, const T* inj, cudaStream_t st) {
+    k_compress_level<H, D, RF, RP><<<unsigned((nparent + 127) / 128), 128, 0, st>>>(p, child, nchild, parent,
+                                                                                     nparent, inj);
+    P3G_CUDA(cudaGetLastError());
+}
+template <class H, int D, int RF, int RP>
+void Launch<H, D, RF, RP>::permute(const typename H::Params& p, T* states, uint64_t n, cudaStream_t st) {
+    if (n == 0) return;
+    k_permute<H, D, RF, RP><<<unsigned((n + 127) / 128), 128, 0, st>>>(p, states, n);
+    P3G_CUDA(cudaGetLastError());
+}
+#endif
+
+}  // namespace p3g

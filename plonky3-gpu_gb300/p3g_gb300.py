@@ -1,0 +1,368 @@
+"""ctypes binding of libp3g_gb300.so (the C ABI declared in include/p3g.h).
+
+This is the thin host-side mirror used by the tests, ``__graft_entry__`` and
+bench.py: every call goes through the C ABI into the CUDA library.  There is
+no CPU fallback -- if the library cannot be loaded or a call fails, an
+exception is raised.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "lib", "libp3g_gb300.so")
+
+BABYBEAR = 0
+GOLDILOCKS = 1
+BB_P = 0x78000001
+GL_P = 0xFFFFFFFF00000001
+
+EXPORTS = [
+    "p3g_version", "p3g_status_string", "p3g_last_error", "p3g_ctx_create", "p3g_ctx_destroy",
+    "p3g_stream_synchronize", "p3g_malloc", "p3g_free", "p3g_memcpy_h2d", "p3g_memcpy_d2h",
+    "p3g_set_poseidon2", "p3g_poseidon2_permute", "p3g_coset_lde", "p3g_mmcs_commit",
+    "p3g_commit_matrix", "p3g_tree_info", "p3g_tree_layer_ptr", "p3g_tree_leaf_ptr",
+    "p3g_mmcs_open_batch", "p3g_tree_free", "p3g_commit_traces", "p3g_fold_matrix_bb4",
+]
+
+
+class P3GError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"p3g status {status}: {msg}")
+        self.status = status
+
+
+class Matrix(C.Structure):
+    _fields_ = [("d_data", C.c_void_p), ("height", C.c_uint64), ("width", C.c_uint32),
+                ("reserved", C.c_uint32)]
+
+
+class Trace(C.Structure):
+    _fields_ = [("d_trace", C.c_void_p), ("log_h", C.c_uint32), ("width", C.c_uint32),
+                ("log_blowup", C.c_uint32), ("reserved", C.c_uint32), ("shift", C.c_uint64)]
+
+
+_lib = None
+
+
+def load(path: str | None = None):
+    """Loads the library; raises if it is missing (build it with build.py)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise RuntimeError(f"libp3g_gb300.so not built at {p}; run plonky3-gpu_gb300/build.py")
+    L = C.CDLL(p)
+    vp, sz, i32, u32, u64 = C.c_void_p, C.c_size_t, C.c_int, C.c_uint32, C.c_uint64
+    L.p3g_version.restype = i32
+    L.p3g_status_string.restype = C.c_char_p
+    L.p3g_status_string.argtypes = [i32]
+    L.p3g_last_error.argtypes = [C.c_char_p, sz]
+    L.p3g_ctx_create.argtypes = [i32, C.POINTER(vp)]
+    L.p3g_ctx_destroy.argtypes = [vp]
+    L.p3g_stream_synchronize.argtypes = [vp, vp]
+    L.p3g_malloc.argtypes = [vp, sz, C.POINTER(vp), vp]
+    L.p3g_free.argtypes = [vp, vp, vp]
+    L.p3g_memcpy_h2d.argtypes = [vp, vp, vp, sz, vp]
+    L.p3g_memcpy_d2h.argtypes = [vp, vp, vp, sz, vp]
+    L.p3g_set_poseidon2.argtypes = [vp, i32, u32, u32, u32, u32, vp, vp, vp]
+    L.p3g_poseidon2_permute.argtypes = [vp, i32, vp, sz, vp]
+    L.p3g_coset_lde.argtypes = [vp, i32, vp, u32, u32, u32, u64, i32, vp, vp]
+    L.p3g_mmcs_commit.argtypes = [vp, i32, C.POINTER(Matrix), sz, u32, C.POINTER(vp), vp, vp]
+    L.p3g_commit_matrix.argtypes = [vp, i32, vp, u64, u32, C.POINTER(vp), vp, vp]
+    L.p3g_tree_info.argtypes = [vp, C.POINTER(u32), C.POINTER(u64), C.POINTER(u32)]
+    L.p3g_tree_layer_ptr.argtypes = [vp, u32, C.POINTER(vp)]
+    L.p3g_tree_leaf_ptr.argtypes = [vp, u32, C.POINTER(vp)]
+    L.p3g_mmcs_open_batch.argtypes = [vp, vp, vp, sz, vp, vp, vp]
+    L.p3g_tree_free.argtypes = [vp, vp]
+    L.p3g_commit_traces.argtypes = [vp, i32, C.POINTER(Trace), sz, u32, C.POINTER(vp), vp, vp]
+    L.p3g_fold_matrix_bb4.argtypes = [vp, vp, u32, u32, vp, vp, vp]
+    for name in EXPORTS:
+        if name not in ("p3g_version", "p3g_status_string"):
+            getattr(L, name).restype = i32
+    _lib = L
+    return L
+
+
+def check(status: int):
+    if status != 0:
+        buf = C.create_string_buffer(1024)
+        load().p3g_last_error(buf, 1024)
+        raise P3GError(status, buf.value.decode(errors="replace"))
+
+
+def _np_ptr(a: np.ndarray):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+# ----------------------------------------------------------------- MT19937 (for constants)
+def mt19937(seed: int, n: int) -> list[int]:
+    """std::mt19937 outputs (the published Mersenne Twister)."""
+    mt = [0] * 624
+    mt[0] = seed & 0xFFFFFFFF
+    for i in range(1, 624):
+        mt[i] = (1812433253 * (mt[i - 1] ^ (mt[i - 1] >> 30)) + i) & 0xFFFFFFFF
+    out, idx = [], 624
+    for _ in range(n):
+        if idx >= 624:
+            for i in range(624):
+                y = (mt[i] & 0x80000000) | (mt[(i + 1) % 624] & 0x7FFFFFFF)
+                mt[i] = mt[(i + 397) % 624] ^ (y >> 1) ^ (0x9908B0DF if y & 1 else 0)
+            idx = 0
+        y = mt[idx]
+        idx += 1
+        y ^= y >> 11
+        y ^= (y << 7) & 0x9D2C5680
+        y ^= (y << 15) & 0xEFC60000
+        y ^= y >> 18
+        out.append(y & 0xFFFFFFFF)
+    return out
+
+
+def mt19937_64(seed: int, n: int) -> list[int]:
+    """std::mt19937_64 outputs."""
+    M = 0xFFFFFFFFFFFFFFFF
+    mt = [0] * 312
+    mt[0] = seed & M
+    for i in range(1, 312):
+        mt[i] = (6364136223846793005 * (mt[i - 1] ^ (mt[i - 1] >> 62)) + i) & M
+    out, idx = [], 312
+    for _ in range(n):
+        if idx >= 312:
+            for i in range(312):
+                y = (mt[i] & 0xFFFFFFFF80000000) | (mt[(i + 1) % 312] & 0x7FFFFFFF)
+                mt[i] = mt[(i + 156) % 312] ^ (y >> 1) ^ (0xB5026F5AA96619E9 if y & 1 else 0)
+            idx = 0
+        x = mt[idx]
+        idx += 1
+        x ^= (x >> 29) & 0x5555555555555555
+        x ^= (x << 17) & 0x71D67FFFEDA60000
+        x ^= (x << 37) & 0xFFF7EEE000000000
+        x ^= x >> 43
+        out.append(x & M)
+    return out
+
+
+def seeded_constants_bb16(rounds_p: int = 13):
+    """Poseidon2 BabyBear-16 constants drawn from std::mt19937(0xdeadbeef), initial and
+    terminal interleaved per (round, lane), then the partial-round constants -- the
+    convention of the reference's CUDA Merkle example."""
+    raw = mt19937(0xDEADBEEF, 2 * 4 * 16 + rounds_p)
+    ini = np.array([raw[2 * k] % BB_P for k in range(64)], np.uint32)
+    ter = np.array([raw[2 * k + 1] % BB_P for k in range(64)], np.uint32)
+    inr = np.array([raw[128 + r] % BB_P for r in range(rounds_p)], np.uint32)
+    return ini, ter, inr
+
+
+def seeded_constants_gl8(rounds_p: int = 22):
+    """Goldilocks-8 constants from std::mt19937_64(12345), same draw order."""
+    raw = mt19937_64(12345, 2 * 4 * 8 + rounds_p)
+    ini = np.array([raw[2 * k] % GL_P for k in range(32)], np.uint64)
+    ter = np.array([raw[2 * k + 1] % GL_P for k in range(32)], np.uint64)
+    inr = np.array([raw[64 + r] % GL_P for r in range(rounds_p)], np.uint64)
+    return ini, ter, inr
+
+
+# ----------------------------------------------------------------- device buffers
+class DeviceBuffer:
+    """A device allocation from the context pool."""
+
+    def __init__(self, ctx: "Context", nbytes: int, stream=None):
+        self.ctx = ctx
+        self.nbytes = nbytes
+        p = C.c_void_p()
+        check(load().p3g_malloc(ctx.handle, max(nbytes, 1), C.byref(p), stream))
+        self.ptr = p.value
+
+    def upload(self, arr: np.ndarray, stream=None):
+        a = np.ascontiguousarray(arr)
+        assert a.nbytes <= self.nbytes
+        check(load().p3g_memcpy_h2d(self.ctx.handle, self.ptr, _np_ptr(a), a.nbytes, stream))
+        return self
+
+    def download(self, dtype, shape, stream=None) -> np.ndarray:
+        out = np.empty(shape, dtype=dtype)
+        check(load().p3g_memcpy_d2h(self.ctx.handle, _np_ptr(out), self.ptr, out.nbytes, stream))
+        return out
+
+    def free(self, stream=None):
+        if self.ptr:
+            check(load().p3g_free(self.ctx.handle, self.ptr, stream))
+            self.ptr = None
+
+
+class Tree:
+    def __init__(self, ctx: "Context", handle: int, field: int):
+        self.ctx, self.handle, self.field = ctx, handle, field
+
+    def info(self):
+        n = C.c_uint32()
+        sizes = (C.c_uint64 * 64)()
+        dig = C.c_uint32()
+        check(load().p3g_tree_info(self.handle, C.byref(n), sizes, C.byref(dig)))
+        return [int(sizes[i]) for i in range(n.value)], dig.value
+
+    def layers(self):
+        sizes, dig = self.info()
+        dt = np.uint32 if self.field == BABYBEAR else np.uint64
+        out = []
+        for i, s in enumerate(sizes):
+            p = C.c_void_p()
+            check(load().p3g_tree_layer_ptr(self.handle, i, C.byref(p)))
+            arr = np.empty((s, dig), dtype=dt)
+            check(load().p3g_memcpy_d2h(self.ctx.handle, _np_ptr(arr), p, arr.nbytes, None))
+            out.append(arr)
+        return out
+
+    def leaf_ptr(self, i: int) -> int:
+        p = C.c_void_p()
+        check(load().p3g_tree_leaf_ptr(self.handle, i, C.byref(p)))
+        return p.value
+
+    def open_batch(self, indices, row_elems: int):
+        sizes, dig = self.info()
+        dt = np.uint32 if self.field == BABYBEAR else np.uint64
+        idx = np.ascontiguousarray(indices, dtype=np.uint64)
+        rows = np.zeros((idx.size, row_elems), dtype=dt)
+        proof = np.zeros((idx.size, len(sizes) - 1, dig), dtype=dt)
+        check(load().p3g_mmcs_open_batch(self.ctx.handle, self.handle, _np_ptr(idx), idx.size,
+                                         _np_ptr(rows), _np_ptr(proof), None))
+        return rows, proof
+
+    def free(self):
+        if self.handle:
+            check(load().p3g_tree_free(self.ctx.handle, self.handle))
+            self.handle = None
+
+
+class Context:
+    """Owns a p3g_ctx on one device."""
+
+    def __init__(self, device: int = 0):
+        h = C.c_void_p()
+        check(load().p3g_ctx_create(device, C.byref(h)))
+        self.handle = h.value
+
+    def close(self):
+        if self.handle:
+            check(load().p3g_ctx_destroy(self.handle))
+            self.handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def sync(self, stream=None):
+        check(load().p3g_stream_synchronize(self.handle, stream))
+
+    # -- buffers
+    def alloc(self, nbytes: int, stream=None) -> DeviceBuffer:
+        return DeviceBuffer(self, nbytes, stream)
+
+    def to_device(self, arr: np.ndarray, stream=None) -> DeviceBuffer:
+        a = np.ascontiguousarray(arr)
+        return DeviceBuffer(self, a.nbytes, stream).upload(a, stream)
+
+    # -- Poseidon2
+    def set_poseidon2(self, field: int, width: int, rounds_f: int, rounds_p: int, degree: int,
+                      initial, terminal, internal):
+        dt = np.uint32 if field == BABYBEAR else np.uint64
+        ini = np.ascontiguousarray(initial, dtype=dt).reshape(-1)
+        ter = np.ascontiguousarray(terminal, dtype=dt).reshape(-1)
+        inr = np.ascontiguousarray(internal, dtype=dt).reshape(-1)
+        if inr.size == 0:
+            inr = np.zeros(1, dt)
+        check(load().p3g_set_poseidon2(self.handle, field, width, rounds_f, rounds_p, degree,
+                                       _np_ptr(ini), _np_ptr(ter), _np_ptr(inr)))
+
+    def set_default_poseidon2(self):
+        """BabyBear-16 x^7 8+13 and Goldilocks-8 x^7 8+22 with the seeded constants."""
+        self.set_poseidon2(BABYBEAR, 16, 8, 13, 7, *seeded_constants_bb16(13))
+        self.set_poseidon2(GOLDILOCKS, 8, 8, 22, 7, *seeded_constants_gl8(22))
+
+    def permute(self, field: int, states: np.ndarray) -> np.ndarray:
+        dt = np.uint32 if field == BABYBEAR else np.uint64
+        s = np.ascontiguousarray(states, dtype=dt)
+        d = self.to_device(s)
+        check(load().p3g_poseidon2_permute(self.handle, field, d.ptr, s.shape[0], None))
+        out = d.download(dt, s.shape)
+        d.free()
+        return out
+
+    # -- LDE
+    def coset_lde_device(self, field: int, d_in: int, log_h: int, width: int, log_blowup: int,
+                         shift: int, bitrev: bool, d_out: int, stream=None):
+        check(load().p3g_coset_lde(self.handle, field, d_in, log_h, width, log_blowup, shift,
+                                   int(bitrev), d_out, stream))
+
+    def coset_lde(self, trace: np.ndarray, log_blowup: int, shift: int | None = None,
+                  bitrev: bool = True) -> np.ndarray:
+        field = BABYBEAR if trace.dtype == np.uint32 else GOLDILOCKS
+        if shift is None:
+            shift = 31 if field == BABYBEAR else 7
+        h, w = trace.shape
+        log_h = h.bit_length() - 1
+        assert 1 << log_h == h
+        din = self.to_device(trace)
+        dout = self.alloc((h << log_blowup) * w * trace.itemsize)
+        self.coset_lde_device(field, din.ptr, log_h, w, log_blowup, shift, bitrev, dout.ptr)
+        out = dout.download(trace.dtype, (h << log_blowup, w))
+        din.free()
+        dout.free()
+        return out
+
+    # -- MMCS
+    def mmcs_commit_device(self, field: int, mats, cap_height: int = 0, stream=None) -> Tree:
+        """mats: list of (device_ptr, height, width)."""
+        arr = (Matrix * len(mats))(*[Matrix(p, h, w, 0) for (p, h, w) in mats])
+        t = C.c_void_p()
+        check(load().p3g_mmcs_commit(self.handle, field, arr, len(mats), cap_height, C.byref(t), None, stream))
+        return Tree(self, t.value, field)
+
+    def mmcs_commit(self, mats, cap_height: int = 0):
+        """Host matrices in; returns (layers, tree, device buffers)."""
+        field = BABYBEAR if mats[0].dtype == np.uint32 else GOLDILOCKS
+        bufs = [self.to_device(m) for m in mats]
+        tree = self.mmcs_commit_device(field, [(b.ptr, m.shape[0], m.shape[1]) for b, m in zip(bufs, mats)],
+                                       cap_height)
+        return tree, bufs
+
+    def commit_matrix(self, mat: np.ndarray):
+        field = BABYBEAR if mat.dtype == np.uint32 else GOLDILOCKS
+        buf = self.to_device(mat)
+        t = C.c_void_p()
+        check(load().p3g_commit_matrix(self.handle, field, buf.ptr, mat.shape[0], mat.shape[1], C.byref(t),
+                                       None, None))
+        return Tree(self, t.value, field), buf
+
+    def commit_traces_device(self, field: int, traces, cap_height: int = 0, stream=None,
+                             cap_out: np.ndarray | None = None) -> Tree:
+        """traces: list of (device_ptr, log_h, width, log_blowup, shift)."""
+        arr = (Trace * len(traces))(*[Trace(p, lh, w, lb, 0, s) for (p, lh, w, lb, s) in traces])
+        t = C.c_void_p()
+        capp = _np_ptr(cap_out) if cap_out is not None else None
+        check(load().p3g_commit_traces(self.handle, field, arr, len(traces), cap_height, C.byref(t), capp, stream))
+        return Tree(self, t.value, field)
+
+    # -- FRI
+    def fold_matrix_bb4_device(self, d_in: int, log_height: int, log_arity: int, beta, d_out: int,
+                               stream=None):
+        b = np.ascontiguousarray(beta, dtype=np.uint32).reshape(4)
+        check(load().p3g_fold_matrix_bb4(self.handle, d_in, log_height, log_arity, _np_ptr(b), d_out, stream))
+
+    def fold_matrix_bb4(self, values: np.ndarray, log_height: int, log_arity: int, beta) -> np.ndarray:
+        v = np.ascontiguousarray(values, dtype=np.uint32).reshape(-1, 4)
+        din = self.to_device(v)
+        n = (1 << log_height) >> log_arity
+        dout = self.alloc(n * 16)
+        self.fold_matrix_bb4_device(din.ptr, log_height, log_arity, beta, dout.ptr)
+        out = dout.download(np.uint32, (n, 4))
+        din.free()
+        dout.free()
+        return out

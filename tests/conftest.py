@@ -20,3 +20,13 @@ def golden():
     import json
     with open(os.path.join(REPO, "tests", "golden", "golden.json")) as f:
         return json.load(f)
+
+
+@pytest.fixture(scope="session")
+def gpu_ctx():
+    """One library context on cuda:0 with the seeded Poseidon2 constants."""
+    import p3g_gb300 as P
+    ctx = P.Context(0)
+    ctx.set_default_poseidon2()
+    yield ctx
+    ctx.close()

@@ -1,0 +1,89 @@
+"""GPU parity of the coset LDE (p3g_coset_lde) against the oracle and the
+golden vectors produced by the reference's Radix2Dit::coset_lde_batch.
+Bit-exact: integer field arithmetic."""
+import hashlib
+import os
+
+import numpy as np
+import pytest
+
+import oracle as O
+import p3g_gb300 as P
+
+pytestmark = pytest.mark.gpu
+
+
+def _sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def test_lde_golden(gpu_ctx, golden):
+    for case in golden["lde"]:
+        h = 1 << case["log_h"]
+        if case["field"] == "bb":
+            t = O.bb_random_matrix(h, case["w"], case["seed"])
+        else:
+            t = O.gl_random_matrix(h, case["w"], case["seed"])
+        out = gpu_ctx.coset_lde(t, case["log_blowup"], case["shift"], bool(case["bitrev"]))
+        assert _sha(out) == case["out"]["sha256"], case
+
+
+@pytest.mark.parametrize("log_h", list(range(0, 17)))
+def test_lde_bb_all_heights(gpu_ctx, log_h):
+    rng = np.random.default_rng(log_h)
+    for w, lb in ((1, 1), (7, 2), (16, 1), (33, 3), (5, 0)):
+        if log_h + lb > 27 or (log_h >= 15 and w > 16):
+            continue
+        t = rng.integers(0, O.BB_P, size=(1 << log_h, w), dtype=np.uint32)
+        shift = int(rng.integers(1, O.BB_P))
+        for br in (True, False):
+            got = gpu_ctx.coset_lde(t, lb, shift, br)
+            want = O.bb_coset_lde(t, lb, shift, br, nthreads=os.cpu_count() or 1)
+            assert np.array_equal(got, want), (log_h, w, lb, br)
+
+
+@pytest.mark.parametrize("log_h", [1, 4, 9, 10, 11, 12, 15])
+def test_lde_gl_heights(gpu_ctx, log_h):
+    rng = np.random.default_rng(100 + log_h)
+    for w, lb in ((3, 2), (8, 1), (9, 0)):
+        t = (rng.integers(0, 2**63, size=(1 << log_h, w), dtype=np.uint64) * 2 + 1) % np.uint64(O.GL_P)
+        t = t.astype(np.uint64)
+        for br in (True, False):
+            got = gpu_ctx.coset_lde(t, lb, 7, br)
+            want = O.gl_coset_lde(t, lb, 7, br, nthreads=os.cpu_count() or 1)
+            assert np.array_equal(got, want), (log_h, w, lb, br)
+
+
+def test_lde_edge_values(gpu_ctx):
+    # all p-1, all zero, one-hot columns
+    h = 1 << 11
+    t = np.full((h, 8), O.BB_P - 1, np.uint32)
+    t[:, 1] = 0
+    t[:, 2] = 0
+    t[5, 2] = 1
+    for lb in (1, 2):
+        assert np.array_equal(gpu_ctx.coset_lde(t, lb), O.bb_coset_lde(t, lb))
+
+
+def test_lde_rejects_bad_arguments(gpu_ctx):
+    L = P.load()
+    d = gpu_ctx.alloc(64)
+    # log_h + log_blowup beyond two-adicity
+    assert L.p3g_coset_lde(gpu_ctx.handle, 0, d.ptr, 26, 1, 2, 31, 1, d.ptr, None) == 1
+    # zero shift
+    assert L.p3g_coset_lde(gpu_ctx.handle, 0, d.ptr, 2, 1, 1, 0, 1, d.ptr, None) == 1
+    # non-canonical shift
+    assert L.p3g_coset_lde(gpu_ctx.handle, 0, d.ptr, 2, 1, 1, O.BB_P, 1, d.ptr, None) == 1
+    # unknown field
+    assert L.p3g_coset_lde(gpu_ctx.handle, 7, d.ptr, 2, 1, 1, 3, 1, d.ptr, None) == 1
+    d.free()
+
+
+def test_lde_full_size_config1(gpu_ctx):
+    """2^20 x 256 BabyBear, log_blowup 1: every LDE element against the oracle
+    (multithreaded restatement of Radix2Dit)."""
+    rng = np.random.default_rng(20)
+    t = rng.integers(0, O.BB_P, size=(1 << 20, 256), dtype=np.uint32)
+    got = gpu_ctx.coset_lde(t, 1)
+    want = O.bb_coset_lde(t, 1, nthreads=os.cpu_count() or 1)
+    assert np.array_equal(got, want)
