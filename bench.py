@@ -1,0 +1,303 @@
+#!/usr/bin/env python3
+"""Benchmark of the trace-commitment hot path on GB300.
+
+Workload (default): the plain single-trace BabyBear commit -- a 2^20 x 256
+trace of uniform random elements, coset LDE with log_blowup 1 and shift 31
+(rows bit-reversed, 2^21 x 256 = 2 GiB of u32), then the Poseidon2-16
+(x^7, 8 full + 13 partial rounds, seeded constants) mixed-height MMCS commit
+to one root.  A step is one full commit of that trace.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line (rank 0).  `value` is committed LDE elements/s with the
+trace already resident in HBM (device-timed with CUDA events on the launching
+stream); `e2e` is the same metric through the C ABI with the trace in pinned
+host memory, the host->device copy and the root read-back inside the timed
+region.  `--impl reference` times the CPU restatement of the reference path
+(the oracle, built from oracle/) on the host cores, on a bounded sample of the
+same workload.  Inputs (1 GiB trace, 2 GiB LDE) are larger than L2 (129 MB),
+so no L2 flush is needed between steps.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(REPO, "plonky3-gpu_gb300"))
+
+METRIC = "committed LDE elements/s on 1 GB300, batched vs plain per-trace; p50/p99 ms"
+UNIT = "elements/s"
+LOG_H, WIDTH, LOG_B, SHIFT = 20, 256, 1, 31
+BB_P = 0x78000001
+
+
+def peaks():
+    p = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def dist_info():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """Samples nvidia-smi clocks/throttle reasons while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = os.path.join(REPO, "gpurun_out", f"clocks_{device}.csv")
+
+    def __enter__(self):
+        os.makedirs(os.path.dirname(self.path), exist_ok=True)
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait()
+            self.f.close()
+
+    def summary(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower().startswith("active")})
+        loaded = [s for s in sm if s > 0.5 * max(sm)] if sm else []
+        return {"sm_mhz": statistics.median(loaded) if loaded else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons, "samples": len(rows)}
+
+
+def cpu_sample(nthreads: int, log_h: int = 14):
+    """The oracle's commit (restated Radix2Dit LDE + Poseidon2 MMCS) on a bounded
+    sample of the workload: same width, blowup and hash, height 2^log_h."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle as O
+
+    O.build()
+    rng = np.random.default_rng(5)
+    t = rng.integers(0, BB_P, size=(1 << log_h, WIDTH), dtype=np.uint32)
+    p = O.bb16_params()
+    t0 = time.perf_counter()
+    lde = O.bb_coset_lde(t, LOG_B, SHIFT, True, nthreads=nthreads)
+    O.mmcs_commit(p, [lde], 0, nthreads=nthreads)
+    dt = time.perf_counter() - t0
+    elems = (1 << (log_h + LOG_B)) * WIDTH
+    return elems / dt, dt, f"2^{log_h} x {WIDTH} BabyBear trace, log_blowup 1, LDE + Poseidon2-16 MMCS root"
+
+
+def run_reference(args):
+    ws, rank, _ = dist_info()
+    if rank != 0:
+        return 0
+    nthreads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_sample(nthreads, 12)
+    vals, times = [], []
+    desc = ""
+    for _ in range(args.steps):
+        v, dt, desc = cpu_sample(nthreads)
+        vals.append(v)
+        times.append(dt * 1e3)
+    value = statistics.mean(vals)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": statistics.mean(times),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32 (BabyBear)",
+        "data": "synthetic",
+        "config": {"workload": "plain single-trace BabyBear commit, 2^20 x 256, log_blowup 1 (bounded CPU sample)",
+                   "sample": desc},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port", "sample": desc},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def run_ours(args):
+    import ctypes as C
+
+    import torch
+    import p3g_gb300 as P
+
+    ws, rank, local = dist_info()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.Stream(device=dev)
+    sptr = stream.cuda_stream
+
+    ctx = P.Context(local)
+    ctx.set_default_poseidon2()
+    h, H = 1 << LOG_H, 1 << (LOG_H + LOG_B)
+    elems = H * WIDTH
+    rng = np.random.default_rng(1234 + rank)
+    trace = rng.integers(0, BB_P, size=(h, WIDTH), dtype=np.uint32)
+    d_trace = ctx.to_device(trace)
+    ctx.sync()
+
+    def step(cap_out=None):
+        tree = ctx.commit_traces_device(P.BABYBEAR, [(d_trace.ptr, LOG_H, WIDTH, LOG_B, SHIFT)], 0,
+                                        stream=sptr, cap_out=cap_out)
+        tree.free(sptr)
+
+    for _ in range(max(args.warmup, 1)):
+        step()
+    torch.cuda.synchronize(dev)
+
+    # ---- device-timed region (trace resident in HBM)
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize(dev)
+    l0 = P.kernel_launches()
+    with ClockSampler(local) as clk:
+        with torch.cuda.stream(stream):
+            for i in range(args.steps):
+                evs[i].record(stream)
+                step()
+            evs[-1].record(stream)
+        torch.cuda.synchronize(dev)
+    launches = P.kernel_launches() - l0
+    step_ms = [evs[i].elapsed_time(evs[i + 1]) for i in range(args.steps)]
+    total_ms = evs[0].elapsed_time(evs[-1])
+    if ws > 1:
+        t = torch.tensor([total_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_per_step = total_ms / args.steps
+    value = ws * elems / (ms_per_step / 1e3)
+
+    # ---- stage breakdown: the LDE alone (roofline) -- same stream, CUDA events
+    d_lde = ctx.alloc(elems * 4, sptr)
+    reps = 10
+    for _ in range(2):
+        ctx.coset_lde_device(P.BABYBEAR, d_trace.ptr, LOG_H, WIDTH, LOG_B, SHIFT, True, d_lde.ptr, sptr)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize(dev)
+    e0.record(stream)
+    for _ in range(reps):
+        ctx.coset_lde_device(P.BABYBEAR, d_trace.ptr, LOG_H, WIDTH, LOG_B, SHIFT, True, d_lde.ptr, sptr)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    lde_ms = e0.elapsed_time(e1) / reps
+    d_lde.free(sptr)
+    torch.cuda.synchronize(dev)
+
+    # ---- end to end through the C ABI with the trace in pinned host memory
+    pinned = torch.empty(h * WIDTH, dtype=torch.int32, pin_memory=True)
+    pinned.numpy().view(np.uint32)[:] = trace.reshape(-1)
+    cap = np.zeros((1, 8), np.uint32)
+    e2e_ms = []
+    for i in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        P.check(P.load().p3g_memcpy_h2d(ctx.handle, d_trace.ptr, pinned.data_ptr(), h * WIDTH * 4, sptr))
+        step(cap_out=cap)  # commit + root read-back (synchronises the stream)
+        dt = (time.perf_counter() - t0) * 1e3
+        if i >= args.warmup:
+            e2e_ms.append(dt)
+    e2e_mean = statistics.mean(e2e_ms)
+    if ws > 1:
+        t = torch.tensor([e2e_mean], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_mean = float(t.item())
+
+    hbm, src = peaks()
+    lde_bytes = 4 * WIDTH * (h + H)
+    lde_gbs = lde_bytes / (lde_ms / 1e3) / 1e9
+    traffic = None
+    tpath = os.path.join(REPO, "profiles", "traffic.json")
+    if os.path.exists(tpath):
+        with open(tpath) as f:
+            traffic = json.load(f).get("lde_bb_2p20x256_b1_bytes")
+    perms = H * ((WIDTH + 7) // 8) + (H - 1)
+    hash_ms = ms_per_step - lde_ms
+    result = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step,
+        "p50_ms": float(np.percentile(step_ms, 50)), "p99_ms": float(np.percentile(step_ms, 99)),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32 (BabyBear)",
+        "data": "synthetic",
+        "config": {"workload": "plain single-trace BabyBear commit: 2^20 x 256 trace, log_blowup 1, shift 31, "
+                               "bit-reversed LDE 2^21 x 256, Poseidon2-16 (x^7, 8+13) MMCS, cap_height 0",
+                   "trace_rows": h, "trace_cols": WIDTH, "lde_rows": H, "field": "BabyBear",
+                   "l2": "inputs larger than L2 (1 GiB trace, 2 GiB LDE); no flush",
+                   "parallelism": f"replicas x{ws}"},
+        "e2e": {"value": ws * elems / (e2e_mean / 1e3), "unit": UNIT,
+                "h2d_bytes_per_step": h * WIDTH * 4, "d2h_bytes_per_step": 32,
+                "p50_ms": float(np.percentile(e2e_ms, 50)), "p99_ms": float(np.percentile(e2e_ms, 99))},
+        "gpu_launches": int(launches),
+        "clocks": clk.summary(),
+        "roofline": {"kernel": "coset LDE (3 passes, k_lde_pass1/2/3)", "bound": "hbm", "achieved": lde_gbs,
+                     "peak": hbm, "unit": "GB/s", "frac": lde_gbs / hbm, "traffic": traffic,
+                     "peak_source": src, "algorithmic_bytes": lde_bytes, "ms": lde_ms},
+        "stages": {"lde_ms": lde_ms, "merkle_ms": hash_ms, "perms": perms,
+                   "perms_per_s": perms / (hash_ms / 1e3) if hash_ms > 0 else None},
+    }
+    if rank == 0 and not args.no_cpu:
+        v, dt, desc = cpu_sample(os.cpu_count() or 1)
+        result["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
+                                  "sample": desc, "seconds": dt}
+    d_trace.free()
+    ctx.close()
+    if rank == 0:
+        print(json.dumps(result))
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

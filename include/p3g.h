@@ -61,6 +61,9 @@ P3G_API int p3g_version(void);
 P3G_API const char *p3g_status_string(int status);
 /* Copies the calling thread's last error message (NUL-terminated). */
 P3G_API int p3g_last_error(char *buf, size_t len);
+/* Number of CUDA kernels this library has launched in the process so far
+ * (instrumentation for benchmarks and tests). */
+P3G_API uint64_t p3g_kernel_launches(void);
 
 /* Creates a context on `device`: root-of-unity tables, a stream-ordered
  * device memory pool.  Replaces the per-call set-up of NttCuda
@@ -146,7 +149,9 @@ P3G_API int p3g_tree_leaf_ptr(const p3g_tree *tree, uint32_t i, const void **d_p
 P3G_API int p3g_mmcs_open_batch(p3g_ctx *ctx, const p3g_tree *tree, const uint64_t *h_indices,
                         size_t n_queries, void *h_rows, void *h_proof, void *stream);
 
-P3G_API int p3g_tree_free(p3g_ctx *ctx, p3g_tree *tree);
+/* Releases the tree's device memory (digest layers and owned LDEs) in stream
+ * order on `stream`: work already queued on `stream` may still read it. */
+P3G_API int p3g_tree_free(p3g_ctx *ctx, p3g_tree *tree, void *stream);
 
 /* ------------------------------------------------------------ commit pipeline */
 typedef struct {

@@ -3,6 +3,7 @@
 // Converts C++ exceptions into P3G_* status codes and a per-thread message,
 // owns contexts (root-of-unity tables, Poseidon2 constants, a stream-ordered
 // memory pool) and trees.  No entry point falls back to the CPU.
+#include <atomic>
 #include <cstring>
 #include <memory>
 #include <new>
@@ -12,6 +13,7 @@
 
 namespace {
 thread_local std::string g_last_error;
+std::atomic<uint64_t> g_launches{0};
 
 struct DeviceGuard {
     int prev = -1, want;
@@ -44,6 +46,10 @@ inline cudaStream_t S(void* s) { return static_cast<cudaStream_t>(s); }
     }                                                     \
     return P3G_OK;
 
+namespace p3g {
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+}  // namespace p3g
+
 void* p3g_ctx::alloc(size_t bytes, cudaStream_t st) {
     void* p = nullptr;
     P3G_CUDA(cudaMallocFromPoolAsync(&p, bytes ? bytes : 1, pool, st));
@@ -69,6 +75,8 @@ const char* p3g_status_string(int s) {
         default: return "unknown status";
     }
 }
+
+uint64_t p3g_kernel_launches(void) { return g_launches.load(std::memory_order_relaxed); }
 
 int p3g_last_error(char* buf, size_t len) {
     if (!buf || len == 0) return P3G_EINVAL;
@@ -366,11 +374,11 @@ int p3g_mmcs_open_batch(p3g_ctx* ctx, const p3g_tree* tree, const uint64_t* h_in
     API_END
 }
 
-int p3g_tree_free(p3g_ctx* ctx, p3g_tree* tree) {
+int p3g_tree_free(p3g_ctx* ctx, p3g_tree* tree, void* stream) {
     API_BEGIN
     P3G_REQUIRE(ctx, "tree_free: null context");
     DeviceGuard g(ctx->device);
-    free_tree(ctx, tree, nullptr);
+    free_tree(ctx, tree, S(stream));
     API_END
 }
 

@@ -102,16 +102,19 @@ void fold_bb4(p3g_ctx* ctx, const uint32_t* in, int log_height, int log_arity, c
     if (log_arity == 1) {
         bb4 bm = {{bb::to_mont(beta[0]), bb::to_mont(beta[1]), bb::to_mont(beta[2]), bb::to_mont(beta[3])}};
         k_fold2<<<grid, 256, 0, st>>>(din, dout, n, log_height, bm, bb::to_mont(bb::h_inv(2)), ctx->bb_roots());
+        P3G_LAUNCHED();
     } else {
         const uint32_t w = bb::two_adic_generator(unsigned(log_arity));
         const uint32_t winv = bb::h_pow(w, (uint64_t(1) << log_arity) - 1);
         const uint32_t ainv = bb::h_pow(bb::h_inv(2), uint64_t(log_arity));
-        if (log_arity == 2)
+        if (log_arity == 2) {
             k_fold_general<2><<<grid, 256, 0, st>>>(din, dout, n, log_height, b, bb::to_mont(w), bb::to_mont(winv),
                                                    bb::to_mont(ainv), ctx->bb_roots());
-        else
+        } else {
             k_fold_general<3><<<grid, 256, 0, st>>>(din, dout, n, log_height, b, bb::to_mont(w), bb::to_mont(winv),
                                                    bb::to_mont(ainv), ctx->bb_roots());
+        }
+        P3G_LAUNCHED();
     }
     P3G_CUDA(cudaGetLastError());
 }

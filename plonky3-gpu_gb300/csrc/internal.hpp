@@ -18,6 +18,11 @@ struct Error : std::runtime_error {
     Error(int s, const std::string& m) : std::runtime_error(m), status(s) {}
 };
 
+// Counts kernel launches (p3g_kernel_launches); every launch site calls
+// P3G_LAUNCHED() right after the <<<>>> launch.
+void count_launch();
+#define P3G_LAUNCHED() ::p3g::count_launch()
+
 #define P3G_CUDA(x)                                                                           \
     do {                                                                                      \
         cudaError_t e_ = (x);                                                                 \

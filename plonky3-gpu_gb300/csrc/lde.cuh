@@ -253,6 +253,7 @@ static void launch_single(const typename F::T* in, typename F::T* out, int w, in
     set_smem(k, smem);
     dim3 grid(1, ceil_div(w, TL::C));
     k<<<grid, TL::THREADS, smem, st>>>(in, out, w, log_b, br, sq, roots);
+    P3G_LAUNCHED();
     P3G_CUDA(cudaGetLastError());
 }
 template <class F, int LOGN>
@@ -264,6 +265,7 @@ static void launch_pass1(const typename F::T* in, typename F::T* scr, int w, int
     set_smem(k, smem);
     dim3 grid(1u << n1, ceil_div(w, TL::C));
     k<<<grid, TL::THREADS, smem, st>>>(in, scr, w, n1, roots);
+    P3G_LAUNCHED();
     P3G_CUDA(cudaGetLastError());
 }
 template <class F, int LOGN>
@@ -275,6 +277,7 @@ static void launch_pass2(const typename F::T* scr, typename F::T* dst, int w, in
     set_smem(k, smem);
     dim3 grid(1u << n2, ceil_div(w, TL::C));
     k<<<grid, TL::THREADS, smem, st>>>(scr, dst, w, n2, log_b, sp, sq, roots);
+    P3G_LAUNCHED();
     P3G_CUDA(cudaGetLastError());
 }
 template <class F, int LOGN>
@@ -286,6 +289,7 @@ static void launch_pass3(const typename F::T* src, typename F::T* out, int w, in
     set_smem(k, smem);
     dim3 grid(1u << (n1 + log_b), ceil_div(w, TL::C));
     k<<<grid, TL::THREADS, smem, st>>>(src, out, w, n1, log_b, br, roots);
+    P3G_LAUNCHED();
     P3G_CUDA(cudaGetLastError());
 }
 
@@ -294,6 +298,7 @@ static void launch_pass3(const typename F::T* src, typename F::T* out, int w, in
 template <class F>
 static void pow_table(typename F::T* out, uint64_t base, uint64_t scale, int n, cudaStream_t st) {
     k_pow_table<F><<<ceil_div(n, 256), 256, 0, st>>>(out, F::to_const(base), F::to_const(scale), n);
+    P3G_LAUNCHED();
     P3G_CUDA(cudaGetLastError());
 }
 
@@ -311,6 +316,7 @@ static void lde_impl(p3g_ctx* ctx, const typename F::T* in, int log_h, int w, in
     if (log_h == 0) {
         int64_t total = (int64_t(1) << log_b) * w;
         k_broadcast_row<F><<<ceil_div(total, 256), 256, 0, st>>>(in, out, w, int(1 << log_b));
+        P3G_LAUNCHED();
         P3G_CUDA(cudaGetLastError());
         return;
     }

@@ -255,12 +255,14 @@ void open_batch(p3g_ctx* ctx, const p3g_tree* tree, const uint64_t* h_idx, size_
             static_cast<const uint32_t*>(tree->d_digests), reinterpret_cast<uint64_t*>(buf + o_loff),
             reinterpret_cast<uint64_t*>(buf + o_lsz), nproof, int(dig), tree->flat ? 1 : 0,
             reinterpret_cast<uint32_t*>(buf + o_rows), row_elems, reinterpret_cast<uint32_t*>(buf + o_proof));
+        P3G_LAUNCHED();
     } else {
         k_open<uint64_t><<<unsigned(nq), 128, 0, st>>>(
             reinterpret_cast<OpenMat*>(buf + o_mats), int(om.size()), max_h, reinterpret_cast<uint64_t*>(buf + o_idx),
             static_cast<const uint64_t*>(tree->d_digests), reinterpret_cast<uint64_t*>(buf + o_loff),
             reinterpret_cast<uint64_t*>(buf + o_lsz), nproof, int(dig), tree->flat ? 1 : 0,
             reinterpret_cast<uint64_t*>(buf + o_rows), row_elems, reinterpret_cast<uint64_t*>(buf + o_proof));
+        P3G_LAUNCHED();
     }
     P3G_CUDA(cudaGetLastError());
     if (h_rows && rows_bytes) P3G_CUDA(cudaMemcpyAsync(h_rows, buf + o_rows, rows_bytes, cudaMemcpyDeviceToHost, st));

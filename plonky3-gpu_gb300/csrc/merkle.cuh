@@ -155,6 +155,7 @@ void Launch<H, D, RF, RP>::leaf(const typename H::Params& p, const Group<T>& g, 
                                 cudaStream_t st) {
     if (nrows == 0) return;
     k_leaf_hash<H, D, RF, RP><<<unsigned((nrows + 127) / 128), 128, 0, st>>>(p, g, out, nrows);
+    P3G_LAUNCHED();
     P3G_CUDA(cudaGetLastError());
 }
 template <class H, int D, int RF, int RP>
@@ -162,12 +163,14 @@ void Launch<H, D, RF, RP>::level(const typename H::Params& p, const T* child, ui
                                  uint64_t nparent, const T* inj, cudaStream_t st) {
     k_compress_level<H, D, RF, RP><<<unsigned((nparent + 127) / 128), 128, 0, st>>>(p, child, nchild, parent,
                                                                                      nparent, inj);
+    P3G_LAUNCHED();
     P3G_CUDA(cudaGetLastError());
 }
 template <class H, int D, int RF, int RP>
 void Launch<H, D, RF, RP>::permute(const typename H::Params& p, T* states, uint64_t n, cudaStream_t st) {
     if (n == 0) return;
     k_permute<H, D, RF, RP><<<unsigned((n + 127) / 128), 128, 0, st>>>(p, states, n);
+    P3G_LAUNCHED();
     P3G_CUDA(cudaGetLastError());
 }
 #endif

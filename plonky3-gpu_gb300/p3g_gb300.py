@@ -21,7 +21,7 @@ BB_P = 0x78000001
 GL_P = 0xFFFFFFFF00000001
 
 EXPORTS = [
-    "p3g_version", "p3g_status_string", "p3g_last_error", "p3g_ctx_create", "p3g_ctx_destroy",
+    "p3g_version", "p3g_status_string", "p3g_last_error", "p3g_kernel_launches", "p3g_ctx_create", "p3g_ctx_destroy",
     "p3g_stream_synchronize", "p3g_malloc", "p3g_free", "p3g_memcpy_h2d", "p3g_memcpy_d2h",
     "p3g_set_poseidon2", "p3g_poseidon2_permute", "p3g_coset_lde", "p3g_mmcs_commit",
     "p3g_commit_matrix", "p3g_tree_info", "p3g_tree_layer_ptr", "p3g_tree_leaf_ptr",
@@ -62,6 +62,8 @@ def load(path: str | None = None):
     L.p3g_status_string.restype = C.c_char_p
     L.p3g_status_string.argtypes = [i32]
     L.p3g_last_error.argtypes = [C.c_char_p, sz]
+    L.p3g_kernel_launches.restype = u64
+    L.p3g_kernel_launches.argtypes = []
     L.p3g_ctx_create.argtypes = [i32, C.POINTER(vp)]
     L.p3g_ctx_destroy.argtypes = [vp]
     L.p3g_stream_synchronize.argtypes = [vp, vp]
@@ -78,14 +80,18 @@ def load(path: str | None = None):
     L.p3g_tree_layer_ptr.argtypes = [vp, u32, C.POINTER(vp)]
     L.p3g_tree_leaf_ptr.argtypes = [vp, u32, C.POINTER(vp)]
     L.p3g_mmcs_open_batch.argtypes = [vp, vp, vp, sz, vp, vp, vp]
-    L.p3g_tree_free.argtypes = [vp, vp]
+    L.p3g_tree_free.argtypes = [vp, vp, vp]
     L.p3g_commit_traces.argtypes = [vp, i32, C.POINTER(Trace), sz, u32, C.POINTER(vp), vp, vp]
     L.p3g_fold_matrix_bb4.argtypes = [vp, vp, u32, u32, vp, vp, vp]
     for name in EXPORTS:
-        if name not in ("p3g_version", "p3g_status_string"):
+        if name not in ("p3g_version", "p3g_status_string", "p3g_kernel_launches"):
             getattr(L, name).restype = i32
     _lib = L
     return L
+
+
+def kernel_launches() -> int:
+    return int(load().p3g_kernel_launches())
 
 
 def check(status: int):
@@ -233,9 +239,9 @@ class Tree:
                                          _np_ptr(rows), _np_ptr(proof), None))
         return rows, proof
 
-    def free(self):
+    def free(self, stream=None):
         if self.handle:
-            check(load().p3g_tree_free(self.ctx.handle, self.handle))
+            check(load().p3g_tree_free(self.ctx.handle, self.handle, stream))
             self.handle = None
 
 
