@@ -168,6 +168,7 @@ def run_ours(args):
 
     ctx = P.Context(local)
     ctx.set_default_poseidon2()
+    LOG_H, WIDTH = args.log_h, args.width
     h, H = 1 << LOG_H, 1 << (LOG_H + LOG_B)
     elems = H * WIDTH
     rng = np.random.default_rng(1234 + rank)
@@ -293,6 +294,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--log-h", type=int, default=LOG_H, help="trace log2 height (profiling cases)")
+    ap.add_argument("--width", type=int, default=WIDTH, help="trace width (profiling cases)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
