@@ -108,6 +108,23 @@ P3G_API int p3g_poseidon2_permute(p3g_ctx *ctx, int field, void *d_states, size_
 P3G_API int p3g_coset_lde(p3g_ctx *ctx, int field, const void *d_in, uint32_t log_h, uint32_t width,
                   uint32_t log_blowup, uint64_t shift, int bitrev_out, void *d_out, void *stream);
 
+/* BabyBear-only variant of p3g_coset_lde that allocates nothing and needs no
+ * context.  It has no counterpart in the reference.  It is for callers that
+ * must not enter the CUDA allocator while they prove -- a service that
+ * reserves its device memory up front so that no request can fail or
+ * fragment the heap on an allocation, or a host whose own memory manager owns
+ * the GPU -- whereas p3g_coset_lde takes its scratch from the context's pool.
+ * Scratch lives in a fixed 16 MiB device array (plus 96 KiB of root tables)
+ * that every GPU loading the library holds until exit; requests needing more
+ * scratch are rejected with P3G_EINVAL (with bit-reversed output that is
+ * about (1 << log_h) * width <= 4M elements).  The first call on a device
+ * sets the arrays up (address lookup, synchronous table copy) with that
+ * device current: make it before any stream capture.  All calls share the
+ * array, so calls that overlap on the GPU race; serialise them. */
+P3G_API int p3g_coset_lde_bb_noalloc(const void *d_in, uint32_t log_h, uint32_t width,
+                                     uint32_t log_blowup, uint32_t shift, int bitrev_out,
+                                     void *d_out, void *stream);
+
 /* ------------------------------------------------------------ MMCS */
 typedef struct {
     const void *d_data;   /* row-major height x width, device */

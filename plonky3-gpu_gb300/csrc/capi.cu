@@ -48,6 +48,7 @@ inline cudaStream_t S(void* s) { return static_cast<cudaStream_t>(s); }
 
 namespace p3g {
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+void set_last_error(const std::string& msg) { g_last_error = msg; }
 }  // namespace p3g
 
 void* p3g_ctx::alloc(size_t bytes, cudaStream_t st) {

@@ -18,6 +18,9 @@ struct Error : std::runtime_error {
     Error(int s, const std::string& m) : std::runtime_error(m), status(s) {}
 };
 
+// Records the calling thread's last error message (read by p3g_last_error).
+void set_last_error(const std::string& msg);
+
 // Counts kernel launches (p3g_kernel_launches); every launch site calls
 // P3G_LAUNCHED() right after the <<<>>> launch.
 void count_launch();

@@ -26,6 +26,7 @@ EXPORTS = [
     "p3g_set_poseidon2", "p3g_poseidon2_permute", "p3g_coset_lde", "p3g_mmcs_commit",
     "p3g_commit_matrix", "p3g_tree_info", "p3g_tree_layer_ptr", "p3g_tree_leaf_ptr",
     "p3g_mmcs_open_batch", "p3g_tree_free", "p3g_commit_traces", "p3g_fold_matrix_bb4",
+    "p3g_coset_lde_bb_noalloc",
 ]
 
 
@@ -83,6 +84,7 @@ def load(path: str | None = None):
     L.p3g_tree_free.argtypes = [vp, vp, vp]
     L.p3g_commit_traces.argtypes = [vp, i32, C.POINTER(Trace), sz, u32, C.POINTER(vp), vp, vp]
     L.p3g_fold_matrix_bb4.argtypes = [vp, vp, u32, u32, vp, vp, vp]
+    L.p3g_coset_lde_bb_noalloc.argtypes = [vp, u32, u32, u32, u32, i32, vp, vp]
     for name in EXPORTS:
         if name not in ("p3g_version", "p3g_status_string", "p3g_kernel_launches"):
             getattr(L, name).restype = i32
