@@ -47,13 +47,35 @@ P3G_HD uint32_t sub(uint32_t a, uint32_t b) {
     return d < t ? d : t;
 }
 // Montgomery product a*b*2^-32 mod p, canonical output; a, b < p.
+// Signed-remainder form: q = lo(ab) * p^-1 mod 2^32 makes ab - qp divisible by
+// 2^32, and r = hi(ab) - hi(qp) lies in (-p, p); one conditional + p.  (Of the
+// formulations measured on GB300 this one had the highest throughput.)
 P3G_HD uint32_t mmul(uint32_t a, uint32_t b) {
     uint64_t t = uint64_t(a) * b;
-    uint32_t m = uint32_t(t) * NPINV;
-    uint64_t u = t + uint64_t(m) * P;  // low 32 bits vanish; < 2^64
-    uint32_t r = uint32_t(u >> 32);    // < 2p
-    uint32_t s = r - P;
+    uint32_t q = uint32_t(t) * PINV;
+#ifdef __CUDA_ARCH__
+    uint32_t qh = __umulhi(q, P);
+#else
+    uint32_t qh = uint32_t((uint64_t(q) * P) >> 32);
+#endif
+    uint32_t r = uint32_t(t >> 32) - qh;
+    uint32_t s = r + P;
     return r < s ? r : s;
+}
+// Signed Montgomery product for chains: a, b in (-p, p) as int32, result in
+// (-p, p) with no correction (|ab| < p^2 < p*2^31 keeps the remainder bounded).
+#ifdef __CUDA_ARCH__
+__device__ __forceinline__ int32_t smul(int32_t a, int32_t b) {
+    int64_t t = int64_t(a) * b;
+    uint32_t q = uint32_t(t) * PINV;
+    int32_t qh = __mulhi(int32_t(q), int32_t(P));
+    return int32_t(t >> 32) - qh;
+}
+#endif
+// (-p, p) -> [0, p)
+P3G_HD uint32_t canon(int32_t r) {
+    uint32_t u = uint32_t(r), v = u + P;
+    return u < v ? u : v;
 }
 // Host helpers (exact, used to build constant tables).
 inline uint32_t h_mul(uint32_t a, uint32_t b) { return uint32_t((uint64_t(a) * b) % P); }

@@ -16,12 +16,37 @@
 namespace p3g {
 
 // ------------------------------------------------------------------ BabyBear 16
+// x^d on a Montgomery-form value in [0, p): the chain of products stays in
+// signed (-p, p) form and is brought back to [0, p) once.
 __device__ __forceinline__ uint32_t bb_sbox(uint32_t x, int d) {
-    uint32_t x2 = bb::mmul(x, x);
-    if (d == 3) return bb::mmul(x2, x);
-    if (d == 5) return bb::mmul(bb::mmul(x2, x2), x);
-    uint32_t x3 = bb::mmul(x2, x), x4 = bb::mmul(x2, x2);
-    return bb::mmul(x3, x4);  // d == 7 (field.hpp:105-127 operation order)
+    const int32_t xs = int32_t(x);
+    const int32_t x2 = bb::smul(xs, xs);
+    if (d == 3) return bb::canon(bb::smul(x2, xs));
+    const int32_t x4 = bb::smul(x2, x2);
+    if (d == 5) return bb::canon(bb::smul(x4, xs));
+    const int32_t x3 = bb::smul(x2, xs);
+    return bb::canon(bb::smul(x3, x4));  // d == 7: x^2, x^3, x^4, x^7 (field.hpp:105-127)
+}
+
+// Shoup constants floor(2^(32+i) / p) for the internal diagonal 2^i.
+namespace ct {
+constexpr uint32_t shoup_pow2(int i) { return uint32_t((uint64_t(1) << (32 + i)) / bb::P); }
+}  // namespace ct
+#define P3G_SH16 \
+    ct::shoup_pow2(0), ct::shoup_pow2(1), ct::shoup_pow2(2), ct::shoup_pow2(3), ct::shoup_pow2(4), \
+    ct::shoup_pow2(5), ct::shoup_pow2(6), ct::shoup_pow2(7), ct::shoup_pow2(8), ct::shoup_pow2(9), \
+    ct::shoup_pow2(10), ct::shoup_pow2(11), ct::shoup_pow2(12), ct::shoup_pow2(13), ct::shoup_pow2(14), \
+    ct::shoup_pow2(15)
+static __constant__ uint32_t c_bb_shoup_pow2[16] = {P3G_SH16};
+
+// s * 2^i mod p for s in [0, p), 1 <= i <= 15 (Shoup: q = floor(s w' / 2^32),
+// s*2^i - q*p lies in [0, 2p)).  Multiplying the Montgomery representative by
+// the plain constant 2^i is the same as multiplying the field element.
+__device__ __forceinline__ uint32_t bb_mul_pow2(uint32_t s, int i) {
+    const uint32_t q = __umulhi(s, c_bb_shoup_pow2[i]);
+    const uint32_t r = (s << i) - q * bb::P;
+    const uint32_t t = r - bb::P;
+    return r < t ? r : t;
 }
 
 template <class T, T (*ADD)(T, T)>
@@ -73,7 +98,7 @@ __device__ __forceinline__ void p2_bb16(uint32_t* s, const P2BB16& p) {
         for (int i = 1; i < 16; ++i) sum = bb::add(sum, s[i]);
         s[0] = bb::add(s[0], sum);  // diag[0] = 1
 #pragma unroll
-        for (int i = 1; i < 16; ++i) s[i] = bb::add(bb::mmul(s[i], p.diag[i]), sum);
+        for (int i = 1; i < 16; ++i) s[i] = bb::add(bb_mul_pow2(s[i], i), sum);
     }
 #pragma unroll
     for (int r = 0; r < RF / 2; ++r) {
@@ -129,7 +154,7 @@ struct HBB {
     using Params = P2BB16;
     static constexpr int W = 16, RATE = 8, DIG = 8;
     static __device__ __forceinline__ T absorb(T canonical) { return bb::mmul(canonical, bb::R2); }
-    static __device__ __forceinline__ T squeeze(T m) { return bb::mmul(m, 1u); }
+    static __device__ __forceinline__ T squeeze(T m) { return bb::canon(bb::smul(int32_t(m), 1)); }
     template <int D, int RF, int RP>
     static __device__ __forceinline__ void perm(T* s, const Params& p) { p2_bb16<D, RF, RP>(s, p); }
 };
