@@ -64,14 +64,12 @@ P3G_HD uint32_t mmul(uint32_t a, uint32_t b) {
 }
 // Signed Montgomery product for chains: a, b in (-p, p) as int32, result in
 // (-p, p) with no correction (|ab| < p^2 < p*2^31 keeps the remainder bounded).
-#ifdef __CUDA_ARCH__
 __device__ __forceinline__ int32_t smul(int32_t a, int32_t b) {
     int64_t t = int64_t(a) * b;
     uint32_t q = uint32_t(t) * PINV;
     int32_t qh = __mulhi(int32_t(q), int32_t(P));
     return int32_t(t >> 32) - qh;
 }
-#endif
 // (-p, p) -> [0, p)
 P3G_HD uint32_t canon(int32_t r) {
     uint32_t u = uint32_t(r), v = u + P;
