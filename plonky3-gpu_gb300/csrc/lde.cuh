@@ -15,7 +15,7 @@
 // produced in bit-reversed order by a DIF network, so the zero padding is
 // never materialised.
 //
-// h <= 2^10: one kernel; each CTA keeps a whole column tile in shared memory
+// h <= 2^10: one kernel; each CTA keeps a whole column tile on chip
 // (read the trace once, write the LDE once).
 // 2^10 < h <= 2^21: three passes of a four-step split h = N1 * N2:
 //   pass 1: size-N2 inverse DFTs over rows i1 + N1*i2 (stride N1), twiddle
@@ -24,6 +24,11 @@
 //           scale c_k * g_t^k, size-N1 forward DFT and twiddle
 //           g_t^(k2) w_h^(k2 m1), write out row t*h + bitrev(m1)*N2 + k2;
 //   pass 3: size-N2 forward DFT over contiguous N2-row blocks, in place.
+// Every pass reads its tile straight from global memory into the registers
+// of the first radix-32 super-stage and writes the last super-stage's
+// registers straight back; shared memory only carries the exchange between
+// super-stages (and, in pass 2, the coefficients between the inverse and the
+// forward transforms).
 #pragma once
 #include "internal.hpp"
 #include "ntt.cuh"
@@ -34,13 +39,15 @@ template <class F>
 struct LdeCfg;
 template <>
 struct LdeCfg<FBB> {
-    static constexpr int C = 16;     // columns per tile: 64-byte row segments
-    static constexpr int MAXT = 512;
+    static constexpr int C13 = 16;   // columns per tile, passes 1/3 and single (64-byte rows)
+    static constexpr int C2 = 8;     // pass 2 keeps two tiles: 32-byte rows, two CTAs per SM
+    static constexpr int MAXT = 256;
     static constexpr uint32_t ONE_C = bb::R1;
 };
 template <>
 struct LdeCfg<FGL> {
-    static constexpr int C = 8;
+    static constexpr int C13 = 8;
+    static constexpr int C2 = 4;
     static constexpr int MAXT = 256;
     static constexpr uint64_t ONE_C = 1;
 };
@@ -72,69 +79,67 @@ __global__ void k_broadcast_row(const typename F::T* in, typename F::T* out, int
     out[i] = in[i % w];
 }
 
-template <class F, int LOGN>
-struct Tile {
-    using T = typename F::T;
-    static constexpr int C = LdeCfg<F>::C;
-    using Shape = DftShape<LOGN, C, LdeCfg<F>::MAXT>;
-    static constexpr int N = 1 << LOGN;
-    static constexpr int TPC = Shape::TPC;
-    static constexpr int THREADS = Shape::THREADS;
-};
+template <class F, int LOGN, int C>
+struct Tile : DftShape<typename F::T, LOGN, C, LdeCfg<F>::MAXT> {};
 
 // ------------------------------------------------------------ single kernel
 template <class F, int LOGN>
-__global__ void __launch_bounds__(Tile<F, LOGN>::THREADS)
+__global__ void __launch_bounds__(Tile<F, LOGN, LdeCfg<F>::C13>::THREADS)
 k_lde_single(const typename F::T* __restrict__ in, typename F::T* __restrict__ out, int w,
              int log_b, int bitrev_out, const typename F::T* __restrict__ sq, RootTab<F> roots) {
-    using TL = Tile<F, LOGN>;
+    constexpr int C = LdeCfg<F>::C13;
+    using SH = Tile<F, LOGN, C>;
     using T = typename F::T;
-    constexpr int N = TL::N, C = TL::C, TPC = TL::TPC, NT = TL::THREADS;
+    constexpr int N = SH::N, TPC = SH::TPC, NT = SH::THREADS;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    T* tw = reinterpret_cast<T*>(smem_raw);
-    T* pre = tw + N;
-    T* A = pre + N;
-    T* B = A + N * C;
+    T* A = reinterpret_cast<T*>(smem_raw);
+    T* B = A + SH::TILE;
+    T* twi = B + SH::TILE;
+    T* twf = twi + N;
+    T* pre = twf + N;
     const int tid = threadIdx.x, c = tid % C, t = tid / C;
     const int col = blockIdx.y * C + c;
     const bool ok = col < w;
     const int logH = LOGN + log_b;
 
-    for (int e = tid; e < N; e += NT) tw[e] = roots.omega_inv(LOGN, e);
-    for (int i = t; i < N; i += TPC) A[i * C + c] = ok ? in[size_t(i) * w + col] : T(0);
+    for (int e = tid; e < N; e += NT) {
+        twi[e] = roots.omega_inv(LOGN, e);
+        twf[e] = roots.omega(LOGN, e);
+    }
     __syncthreads();
-    cta_dif<F, LOGN, C, TPC, 1>(A, tw, t, c);
-    for (int e = tid; e < N; e += NT) tw[e] = roots.omega(LOGN, e);
+    {
+        auto ld = [&](int i) -> T { return ok ? in[size_t(i) * w + col] : T(0); };
+        auto st = [&](int p, T v) { A[SH::addr(p, c)] = v; };
+        cta_dif<F, SH, LOGN, C, 1>(A, twi, t, c, ld, st);
+    }
     for (int tc = 0; tc < (1 << log_b); ++tc) {
         const uint64_t u = bitrev_dev(unsigned(tc), log_b);
         for (int k = tid; k < N; k += NT) pre[k] = F::cmul(sq[k], roots.omega(logH, u * k));
-        __syncthreads();
-        for (int k = t; k < N; k += TPC) B[k * C + c] = F::mulc(A[bitrev_dev(k, LOGN) * C + c], pre[k]);
-        __syncthreads();
-        cta_dif<F, LOGN, C, TPC, 0>(B, tw, t, c);
-        if (ok) {
-            for (int s = t; s < N; s += TPC) {
-                uint64_t row = uint64_t(tc) * N + s;
-                if (!bitrev_out) row = bitrev_dev(unsigned(row), logH);
-                out[row * w + col] = B[s * C + c];
-            }
-        }
-        __syncthreads();
+        __syncthreads();  // pre ready; A complete (first round) or B free (later rounds)
+        auto ld = [&](int k) -> T { return F::mulc(A[SH::addr(bitrev_dev(k, LOGN), c)], pre[k]); };
+        auto st = [&](int s, T v) {
+            uint64_t row = uint64_t(tc) * N + s;
+            if (!bitrev_out) row = bitrev_dev(unsigned(row), logH);
+            if (ok) out[row * w + col] = v;
+        };
+        cta_dif<F, SH, LOGN, C, 0>(B, twf, t, c, ld, st);
+        __syncthreads();  // pre and B reused by the next coset
     }
 }
 
 // ------------------------------------------------------------ pass 1 (LOGN = n2)
 template <class F, int LOGN>
-__global__ void __launch_bounds__(Tile<F, LOGN>::THREADS)
+__global__ void __launch_bounds__(Tile<F, LOGN, LdeCfg<F>::C13>::THREADS, 2)
 k_lde_pass1(const typename F::T* __restrict__ in, typename F::T* __restrict__ scratch, int w, int n1,
             RootTab<F> roots) {
-    using TL = Tile<F, LOGN>;
+    constexpr int C = LdeCfg<F>::C13;
+    using SH = Tile<F, LOGN, C>;
     using T = typename F::T;
-    constexpr int N = TL::N, C = TL::C, TPC = TL::TPC, NT = TL::THREADS;
+    constexpr int N = SH::N, NT = SH::THREADS;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    T* tw = reinterpret_cast<T*>(smem_raw);
+    T* A = reinterpret_cast<T*>(smem_raw);
+    T* tw = A + SH::TILE;
     T* post = tw + N;
-    T* A = post + N;
     const int tid = threadIdx.x, c = tid % C, t = tid / C;
     const int col = blockIdx.y * C + c;
     const bool ok = col < w;
@@ -146,30 +151,31 @@ k_lde_pass1(const typename F::T* __restrict__ in, typename F::T* __restrict__ sc
         tw[e] = roots.omega_inv(LOGN, e);
         post[e] = roots.omega_inv(n, uint64_t(i1) * bitrev_dev(e, LOGN));
     }
-    for (int i = t; i < N; i += TPC) A[i * C + c] = ok ? in[(i1 + N1 * i) * w + col] : T(0);
     __syncthreads();
-    cta_dif<F, LOGN, C, TPC, 1>(A, tw, t, c);
-    if (ok) {
-        for (int p = t; p < N; p += TPC)
-            scratch[(i1 + N1 * int64_t(bitrev_dev(p, LOGN))) * w + col] = F::mulc(A[p * C + c], post[p]);
-    }
+    auto ld = [&](int i) -> T { return ok ? in[(i1 + N1 * i) * w + col] : T(0); };
+    auto st = [&](int p, T v) {
+        if (ok) scratch[(i1 + N1 * int64_t(bitrev_dev(p, LOGN))) * w + col] = F::mulc(v, post[p]);
+    };
+    cta_dif<F, SH, LOGN, C, 1>(A, tw, t, c, ld, st);
 }
 
 // ------------------------------------------------------------ pass 2 (LOGN = n1)
 template <class F, int LOGN>
-__global__ void __launch_bounds__(Tile<F, LOGN>::THREADS)
+__global__ void __launch_bounds__(Tile<F, LOGN, LdeCfg<F>::C2>::THREADS, 2)
 k_lde_pass2(const typename F::T* __restrict__ scratch, typename F::T* __restrict__ dst, int w, int n2,
             int log_b, const typename F::T* __restrict__ sp, const typename F::T* __restrict__ sq,
             RootTab<F> roots) {
-    using TL = Tile<F, LOGN>;
+    constexpr int C = LdeCfg<F>::C2;
+    using SH = Tile<F, LOGN, C>;
     using T = typename F::T;
-    constexpr int N = TL::N, C = TL::C, TPC = TL::TPC, NT = TL::THREADS;
+    constexpr int N = SH::N, NT = SH::THREADS;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    T* tw = reinterpret_cast<T*>(smem_raw);
-    T* pre = tw + N;
+    T* A = reinterpret_cast<T*>(smem_raw);
+    T* B = A + SH::TILE;
+    T* twi = B + SH::TILE;
+    T* twf = twi + N;
+    T* pre = twf + N;
     T* post = pre + N;
-    T* A = post + N;
-    T* B = A + N * C;
     const int tid = threadIdx.x, c = tid % C, t = tid / C;
     const int col = blockIdx.y * C + c;
     const bool ok = col < w;
@@ -179,11 +185,16 @@ k_lde_pass2(const typename F::T* __restrict__ scratch, typename F::T* __restrict
     const int64_t h = int64_t(1) << n;
     const int logH = n + log_b;
 
-    for (int e = tid; e < N; e += NT) tw[e] = roots.omega_inv(LOGN, e);
-    for (int i = t; i < N; i += TPC) A[i * C + c] = ok ? scratch[(int64_t(N) * k2 + i) * w + col] : T(0);
+    for (int e = tid; e < N; e += NT) {
+        twi[e] = roots.omega_inv(LOGN, e);
+        twf[e] = roots.omega(LOGN, e);
+    }
     __syncthreads();
-    cta_dif<F, LOGN, C, TPC, 1>(A, tw, t, c);
-    for (int e = tid; e < N; e += NT) tw[e] = roots.omega(LOGN, e);
+    {
+        auto ld = [&](int i) -> T { return ok ? scratch[(int64_t(N) * k2 + i) * w + col] : T(0); };
+        auto st = [&](int p, T v) { A[SH::addr(p, c)] = v; };
+        cta_dif<F, SH, LOGN, C, 1>(A, twi, t, c, ld, st);
+    }
     const T sqk2 = sq[k2];
     for (int tc = 0; tc < (1 << log_b); ++tc) {
         const uint64_t u = bitrev_dev(unsigned(tc), log_b);
@@ -192,28 +203,27 @@ k_lde_pass2(const typename F::T* __restrict__ scratch, typename F::T* __restrict
             post[k] = F::cmul(sqk2, roots.omega(logH, uint64_t(k2) * (u + (uint64_t(bitrev_dev(k, LOGN)) << log_b))));
         }
         __syncthreads();
-        for (int k = t; k < N; k += TPC) B[k * C + c] = F::mulc(A[bitrev_dev(k, LOGN) * C + c], pre[k]);
-        __syncthreads();
-        cta_dif<F, LOGN, C, TPC, 0>(B, tw, t, c);
-        if (ok) {
-            for (int s = t; s < N; s += TPC)
-                dst[(tc * h + s * N2 + k2) * w + col] = F::mulc(B[s * C + c], post[s]);
-        }
+        auto ld = [&](int k) -> T { return F::mulc(A[SH::addr(bitrev_dev(k, LOGN), c)], pre[k]); };
+        auto st = [&](int s, T v) {
+            if (ok) dst[(tc * h + s * N2 + k2) * w + col] = F::mulc(v, post[s]);
+        };
+        cta_dif<F, SH, LOGN, C, 0>(B, twf, t, c, ld, st);
         __syncthreads();
     }
 }
 
 // ------------------------------------------------------------ pass 3 (LOGN = n2)
 template <class F, int LOGN>
-__global__ void __launch_bounds__(Tile<F, LOGN>::THREADS)
+__global__ void __launch_bounds__(Tile<F, LOGN, LdeCfg<F>::C13>::THREADS, 2)
 k_lde_pass3(const typename F::T* src, typename F::T* out, int w, int n1, int log_b, int bitrev_out,
             RootTab<F> roots) {
-    using TL = Tile<F, LOGN>;
+    constexpr int C = LdeCfg<F>::C13;
+    using SH = Tile<F, LOGN, C>;
     using T = typename F::T;
-    constexpr int N = TL::N, C = TL::C, TPC = TL::TPC, NT = TL::THREADS;
+    constexpr int N = SH::N, NT = SH::THREADS;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    T* tw = reinterpret_cast<T*>(smem_raw);
-    T* A = tw + N;
+    T* A = reinterpret_cast<T*>(smem_raw);
+    T* tw = A + SH::TILE;
     const int tid = threadIdx.x, c = tid % C, t = tid / C;
     const int col = blockIdx.y * C + c;
     const bool ok = col < w;
@@ -223,72 +233,67 @@ k_lde_pass3(const typename F::T* src, typename F::T* out, int w, int n1, int log
     const int64_t base = blk * N;  // = t*h + s1*N2
 
     for (int e = tid; e < N; e += NT) tw[e] = roots.omega(LOGN, e);
-    for (int i = t; i < N; i += TPC) A[i * C + c] = ok ? src[(base + i) * w + col] : T(0);
     __syncthreads();
-    cta_dif<F, LOGN, C, TPC, 0>(A, tw, t, c);
-    if (ok) {
-        for (int s = t; s < N; s += TPC) {
-            uint64_t row = uint64_t(base + s);
-            if (!bitrev_out) row = bitrev_dev(unsigned(row), logH);
-            out[row * w + col] = A[s * C + c];
-        }
-    }
+    auto ld = [&](int i) -> T { return ok ? src[(base + i) * w + col] : T(0); };
+    auto st = [&](int s, T v) {
+        uint64_t row = uint64_t(base + s);
+        if (!bitrev_out) row = bitrev_dev(unsigned(row), logH);
+        if (ok) out[row * w + col] = v;
+    };
+    cta_dif<F, SH, LOGN, C, 0>(A, tw, t, c, ld, st);
 }
 
 // ------------------------------------------------------------ host side
 template <class Kern>
 static void set_smem(Kern k, size_t bytes) {
-    int dev = 0;
-    cudaGetDevice(&dev);
     P3G_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(bytes)));
-    (void)dev;
 }
 
 template <class F, int LOGN>
 static void launch_single(const typename F::T* in, typename F::T* out, int w, int log_b, int br,
                           const typename F::T* sq, RootTab<F> roots, cudaStream_t st) {
-    using TL = Tile<F, LOGN>;
-    size_t smem = (2 * TL::N + 2 * TL::N * TL::C) * sizeof(typename F::T);
+    using SH = Tile<F, LOGN, LdeCfg<F>::C13>;
+    size_t smem = (2 * SH::TILE + 3 * SH::N) * sizeof(typename F::T);
     auto k = k_lde_single<F, LOGN>;
     set_smem(k, smem);
-    dim3 grid(1, ceil_div(w, TL::C));
-    k<<<grid, TL::THREADS, smem, st>>>(in, out, w, log_b, br, sq, roots);
+    dim3 grid(1, ceil_div(w, LdeCfg<F>::C13));
+    k<<<grid, SH::THREADS, smem, st>>>(in, out, w, log_b, br, sq, roots);
     P3G_LAUNCHED();
     P3G_CUDA(cudaGetLastError());
 }
 template <class F, int LOGN>
 static void launch_pass1(const typename F::T* in, typename F::T* scr, int w, int n1, RootTab<F> roots,
                          cudaStream_t st) {
-    using TL = Tile<F, LOGN>;
-    size_t smem = (2 * TL::N + TL::N * TL::C) * sizeof(typename F::T);
+    using SH = Tile<F, LOGN, LdeCfg<F>::C13>;
+    size_t smem = (SH::TILE + 2 * SH::N) * sizeof(typename F::T);
     auto k = k_lde_pass1<F, LOGN>;
     set_smem(k, smem);
-    dim3 grid(1u << n1, ceil_div(w, TL::C));
-    k<<<grid, TL::THREADS, smem, st>>>(in, scr, w, n1, roots);
+    dim3 grid(1u << n1, ceil_div(w, LdeCfg<F>::C13));
+    k<<<grid, SH::THREADS, smem, st>>>(in, scr, w, n1, roots);
     P3G_LAUNCHED();
     P3G_CUDA(cudaGetLastError());
 }
 template <class F, int LOGN>
 static void launch_pass2(const typename F::T* scr, typename F::T* dst, int w, int n2, int log_b,
                          const typename F::T* sp, const typename F::T* sq, RootTab<F> roots, cudaStream_t st) {
-    using TL = Tile<F, LOGN>;
-    size_t smem = (3 * TL::N + 2 * TL::N * TL::C) * sizeof(typename F::T);
+    using SH = Tile<F, LOGN, LdeCfg<F>::C2>;
+    size_t smem = (2 * SH::TILE + 4 * SH::N) * sizeof(typename F::T);
     auto k = k_lde_pass2<F, LOGN>;
     set_smem(k, smem);
-    dim3 grid(1u << n2, ceil_div(w, TL::C));
-    k<<<grid, TL::THREADS, smem, st>>>(scr, dst, w, n2, log_b, sp, sq, roots);
+    dim3 grid(1u << n2, ceil_div(w, LdeCfg<F>::C2));
+    k<<<grid, SH::THREADS, smem, st>>>(scr, dst, w, n2, log_b, sp, sq, roots);
     P3G_LAUNCHED();
     P3G_CUDA(cudaGetLastError());
 }
 template <class F, int LOGN>
 static void launch_pass3(const typename F::T* src, typename F::T* out, int w, int n1, int log_b, int br,
                          RootTab<F> roots, cudaStream_t st) {
-    using TL = Tile<F, LOGN>;
-    size_t smem = (TL::N + TL::N * TL::C) * sizeof(typename F::T);
+    using SH = Tile<F, LOGN, LdeCfg<F>::C13>;
+    size_t smem = (SH::TILE + SH::N) * sizeof(typename F::T);
     auto k = k_lde_pass3<F, LOGN>;
     set_smem(k, smem);
-    dim3 grid(1u << (n1 + log_b), ceil_div(w, TL::C));
-    k<<<grid, TL::THREADS, smem, st>>>(src, out, w, n1, log_b, br, roots);
+    dim3 grid(1u << (n1 + log_b), ceil_div(w, LdeCfg<F>::C13));
+    k<<<grid, SH::THREADS, smem, st>>>(src, out, w, n1, log_b, br, roots);
     P3G_LAUNCHED();
     P3G_CUDA(cudaGetLastError());
 }

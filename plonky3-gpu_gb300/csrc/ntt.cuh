@@ -1,21 +1,30 @@
 // ntt.cuh -- column-batched radix-2^r DFT inside one CTA.
 //
-// A CTA owns a tile of N = 2^LOGN rows x C columns of a row-major matrix in
-// shared memory (element (row i, column c) at i*C + c).  Each column is an
-// independent polynomial, so the C columns share every twiddle factor; warp
-// lanes run across columns, which keeps global accesses coalesced (C
-// consecutive words of a row) and shared-memory accesses bank-conflict free.
+// A CTA owns a tile of N = 2^LOGN rows x C columns of a row-major matrix.
+// Each column is an independent polynomial, so the C columns share every
+// twiddle factor; warp lanes run across columns, so global accesses are
+// coalesced C-word row segments.
 //
 // The size-N transform is a decimation-in-frequency network split into
-// "super-stages" of radix R = 2^r <= 32: each thread loads R elements at
-// stride M = S/R of its current sub-block (size S), runs a radix-2 DIF of size
-// R in registers with compile-time twiddles (constant-bank operands), scales
-// slot s by omega_S^(i_lo * bitrev_r(s)) and stores slot s at position
-// i_lo + M*s.  After all super-stages, position p holds X[bitrev_N(p)] -- the
-// standard natural-in / bit-reversed-out DIF order, which the callers fold
-// into their global row addressing.  This is the same transform as the
-// reference's Radix2Dit::dft_batch (radix2_dit.hpp:82-121); only the
-// evaluation order of the butterflies differs, and field arithmetic is exact.
+// "super-stages" of radix R = 2^r <= 32.  Super-stage j: each thread takes R
+// elements at stride M = S/R of its sub-block (size S), runs a radix-2 DIF of
+// size R in registers with compile-time twiddles (constant-bank operands),
+// scales slot s by omega_S^(i_lo * bitrev_r(s)) and leaves slot s at position
+// i_lo + M*s.  The first super-stage reads its elements through a caller
+// supplied `load(row)` (global memory, or a permuted shared-memory tile) and
+// the last hands its results to `store(pos, value)` (global memory, or a
+// tile): only the exchanges between super-stages go through shared memory.
+// After all super-stages, position p holds X[bitrev_N(p)] -- natural-in /
+// bit-reversed-out, which the callers fold into their global row addressing.
+// Same transform as Radix2Dit::dft_batch (radix2_dit.hpp:82-121); only the
+// order of the (exact) butterflies differs.
+//
+// Shared-memory layout: 128-byte lines; a line holds L = 128 / (C * sizeof(T))
+// row segments.  Row `row` lives in line row >> log2(L) at sub-slot
+// (row ^ hash(row)) mod L, where hash mixes the row bits that differ between
+// the rows one warp touches at once (consecutive groups, the last
+// super-stage's groups, the bit-reversed read), so those rows land on
+// distinct banks.
 #pragma once
 #include "fields.cuh"
 
@@ -111,76 +120,103 @@ __device__ __forceinline__ void reg_dif(typename F::T* x) {
 // Super-stage split of LOGN into radices <= 5.
 __host__ __device__ constexpr int ss_count(int logn) { return logn == 0 ? 0 : (logn + 4) / 5; }
 __host__ __device__ constexpr int ss_radix(int logn, int j) {
-    // ceil-balanced split: first (logn % cnt) parts get one more bit
+    // ceil-balanced split: the first (logn % cnt) parts get one more bit
     return logn / ss_count(logn) + (j < logn % ss_count(logn) ? 1 : 0);
 }
 __host__ __device__ constexpr int ss_max_radix(int logn) { return logn == 0 ? 0 : ss_radix(logn, 0); }
-
-// Threads per column for an N = 2^LOGN tile: one group of the largest radix
-// per thread, capped so that the CTA has at most MAXT threads.
-template <int LOGN, int C, int MAXT>
-struct DftShape {
-    static constexpr int N = 1 << LOGN;
-    static constexpr int TPC0 = N >> ss_max_radix(LOGN);
-    static constexpr int TPC = TPC0 * C > MAXT ? MAXT / C : TPC0;
-    static constexpr int THREADS = TPC * C;
-};
-
-// One super-stage on the smem tile: sub-blocks of size 2^LS, radix 2^LR.
-// tw[e] = omega_N^e (const form), e < N.  Thread (t, c) with t in [0, TPC).
-template <class F, int LOGN, int LS, int LR, int C, int TPC, int INV>
-__device__ __forceinline__ void super_stage(typename F::T* tile, const typename F::T* tw, int t, int c) {
-    using T = typename F::T;
-    constexpr int N = 1 << LOGN;
-    constexpr int R = 1 << LR;
-    constexpr int M = (1 << LS) >> LR;   // stride inside a sub-block
-    constexpr int GROUPS = N >> LR;      // groups per column
-    static_assert(GROUPS % TPC == 0, "groups per thread");
-    constexpr int TWS = LOGN - LS;       // omega_S = omega_N^(2^TWS)
-#pragma unroll 1
-    for (int g = t; g < GROUPS; g += TPC) {
-        const int blk = g / M, i_lo = g % M;
-        const int base = blk * (1 << LS) + i_lo;
-        T x[R];
-#pragma unroll
-        for (int k = 0; k < R; ++k) x[k] = tile[(base + M * k) * C + c];
-        reg_dif<F, LR, INV>(x);
-        if (M > 1) {
-#pragma unroll
-            for (int s = 1; s < R; ++s) {
-                const int e = (i_lo * int(bitrev_ct(unsigned(s), LR))) << TWS;
-                x[s] = F::mulc(x[s], tw[e]);
-            }
-        }
-#pragma unroll
-        for (int k = 0; k < R; ++k) tile[(base + M * k) * C + c] = x[k];
-    }
-}
-
 __host__ __device__ constexpr int ss_consumed(int logn, int j) {
     int s = 0;
     for (int i = 0; i < j; ++i) s += ss_radix(logn, i);
     return s;
 }
+__host__ __device__ constexpr int cmax(int a, int b) { return a > b ? a : b; }
+__host__ __device__ constexpr int ilog2(int x) { return x <= 1 ? 0 : 1 + ilog2(x >> 1); }
 
-template <class F, int LOGN, int C, int TPC, int INV, int J>
-struct SSChain {
-    static __device__ __forceinline__ void run(typename F::T* tile, const typename F::T* tw, int t, int c) {
-        if constexpr (J < ss_count(LOGN)) {
-            constexpr int LR = ss_radix(LOGN, J);
-            constexpr int LS = LOGN - ss_consumed(LOGN, J);  // sub-block size before this stage
-            super_stage<F, LOGN, LS, LR, C, TPC, INV>(tile, tw, t, c);
-            __syncthreads();
-            SSChain<F, LOGN, C, TPC, INV, J + 1>::run(tile, tw, t, c);
+// Tile geometry: N = 2^LOGN rows x C columns, at most MAXT threads.
+template <class T, int LOGN, int C, int MAXT>
+struct DftShape {
+    static constexpr int N = 1 << LOGN;
+    static constexpr int TPC0 = N >> ss_max_radix(LOGN);
+    static constexpr int TPC = TPC0 * C > MAXT ? MAXT / C : TPC0;  // threads per column
+    static constexpr int THREADS = TPC * C;
+    // swizzled shared-memory layout
+    static constexpr int LINE = 128 / int(sizeof(T));   // elements per 128-byte line
+    static constexpr int RPL = LINE / C >= 1 ? LINE / C : 1;  // row segments per line
+    static constexpr int LG = ilog2(RPL);
+    static constexpr int RL = ss_count(LOGN) ? ss_radix(LOGN, ss_count(LOGN) - 1) : 0;
+    static constexpr int SH1 = cmax(RL, LG);
+    static constexpr int SH2 = cmax(LOGN - LG, LG);
+    static constexpr int TILE = N * C;  // elements
+    static __device__ __forceinline__ int addr(int row, int c) {
+        if constexpr (RPL == 1) {
+            return row * C + c;
+        } else {
+            const int sub = (row ^ (row >> SH1) ^ (row >> SH2)) & (RPL - 1);
+            return (row >> LG) * LINE + sub * C + c;
         }
     }
 };
 
-// Full in-CTA DIF: tile natural order in, bit-reversed out.  Requires a
-// __syncthreads() before the call (tile filled) and ends with one.
-template <class F, int LOGN, int C, int TPC, int INV>
-__device__ __forceinline__ void cta_dif(typename F::T* tile, const typename F::T* tw, int t, int c) {
-    if constexpr (LOGN > 0) SSChain<F, LOGN, C, TPC, INV, 0>::run(tile, tw, t, c);
+// One super-stage J.  tw[e] = omega_N^e (const form), e < N.
+template <class F, class SH, int LOGN, int J, int C, int INV, class Load, class Store>
+__device__ __forceinline__ void super_stage(typename F::T* tile, const typename F::T* tw, int t, int c,
+                                            Load& load, Store& store) {
+    using T = typename F::T;
+    constexpr int CNT = ss_count(LOGN);
+    constexpr int LR = ss_radix(LOGN, J);
+    constexpr int LS = LOGN - ss_consumed(LOGN, J);
+    constexpr int R = 1 << LR;
+    constexpr int M = (1 << LS) >> LR;
+    constexpr int GROUPS = (1 << LOGN) >> LR;
+    constexpr int TWS = LOGN - LS;  // omega_S = omega_N^(2^TWS)
+    constexpr bool FIRST = J == 0, LAST = J == CNT - 1;
+    static_assert(GROUPS % SH::TPC == 0, "groups per thread");
+#pragma unroll 1
+    for (int g = t; g < GROUPS; g += SH::TPC) {
+        const int blk = g / M, i_lo = g % M;
+        const int base = blk * (1 << LS) + i_lo;
+        T x[R];
+#pragma unroll
+        for (int k = 0; k < R; ++k) {
+            if constexpr (FIRST) x[k] = load(base + M * k);
+            else x[k] = tile[SH::addr(base + M * k, c)];
+        }
+        reg_dif<F, LR, INV>(x);
+        if constexpr (LAST) {
+#pragma unroll
+            for (int k = 0; k < R; ++k) store(base + k, x[k]);  // M == 1
+        } else {
+#pragma unroll
+            for (int s = 1; s < R; ++s) {
+                const int e = (i_lo * int(bitrev_ct(unsigned(s), LR))) << TWS;
+                x[s] = F::mulc(x[s], tw[e]);
+            }
+#pragma unroll
+            for (int k = 0; k < R; ++k) tile[SH::addr(base + M * k, c)] = x[k];
+        }
+    }
+}
+
+template <class F, class SH, int LOGN, int C, int INV, int J>
+struct SSChain {
+    template <class Load, class Store>
+    static __device__ __forceinline__ void run(typename F::T* tile, const typename F::T* tw, int t, int c,
+                                               Load& load, Store& store) {
+        if constexpr (J < ss_count(LOGN)) {
+            super_stage<F, SH, LOGN, J, C, INV>(tile, tw, t, c, load, store);
+            if constexpr (J + 1 < ss_count(LOGN)) __syncthreads();
+            SSChain<F, SH, LOGN, C, INV, J + 1>::run(tile, tw, t, c, load, store);
+        }
+    }
+};
+
+// Full in-CTA DIF on one column per thread group: element at natural row i
+// comes from load(i); store(p, v) receives X[bitrev_N(p)].  `tile` is the
+// exchange buffer (SH::TILE elements).  Callers synchronise around it.
+template <class F, class SH, int LOGN, int C, int INV, class Load, class Store>
+__device__ __forceinline__ void cta_dif(typename F::T* tile, const typename F::T* tw, int t, int c, Load& load,
+                                        Store& store) {
+    SSChain<F, SH, LOGN, C, INV, 0>::run(tile, tw, t, c, load, store);
 }
 
 }  // namespace p3g
