@@ -82,6 +82,122 @@ __global__ void k_broadcast_row(const typename F::T* in, typename F::T* out, int
 template <class F, int LOGN, int C>
 struct Tile : DftShape<typename F::T, LOGN, C, LdeCfg<F>::MAXT> {};
 
+// ---- group loads (first super-stage) and stores (last super-stage)
+// Global rows i -> p0[i * s] (p0 already offset to this thread's column).
+template <class T>
+struct GLoad {
+    const T* p0;
+    int64_t s;
+    bool ok;
+    template <int R, int M>
+    __device__ __forceinline__ void group(int base, T* x) const {
+        const T* q = p0 + base * s;
+        const int64_t st = int64_t(M) * s;
+#pragma unroll
+        for (int k = 0; k < R; ++k) {
+            x[k] = ok ? __ldg(q) : T(0);
+            q += st;
+        }
+    }
+};
+// Shared tile row bitrev(i), times pre[i] (coefficients -> twisted coefficients).
+template <class F, class SH, int LOGN>
+struct PermLoad {
+    using T = typename F::T;
+    const T* A;
+    const T* pre;
+    int c;
+    template <int R, int M>
+    __device__ __forceinline__ void group(int base, T* x) const {
+#pragma unroll
+        for (int k = 0; k < R; ++k) {
+            const int i = base + M * k;
+            x[k] = F::mulc(A[SH::addr(bitrev_dev(unsigned(i), LOGN), c)], pre[i]);
+        }
+    }
+};
+// Shared tile, natural positions.
+template <class T, class SH>
+struct TileStore {
+    T* A;
+    int c;
+    template <int LR>
+    __device__ __forceinline__ void group(int base, const T* x) const {
+#pragma unroll
+        for (int k = 0; k < (1 << LR); ++k) A[SH::addr(base + k, c)] = x[k];
+    }
+};
+// Global position p -> p0[p * s] (optionally times post[p]).
+template <class F, bool POST>
+struct GStore {
+    using T = typename F::T;
+    T* p0;
+    int64_t s;
+    const T* post;
+    bool ok;
+    template <int LR>
+    __device__ __forceinline__ void group(int base, const T* x) const {
+        if (!ok) return;
+        T* q = p0 + base * s;
+#pragma unroll
+        for (int k = 0; k < (1 << LR); ++k) {
+            *q = POST ? F::mulc(x[k], post[base + k]) : x[k];
+            q += s;
+        }
+    }
+};
+// Global position p -> p0[bitrev_N(p) * s] * post[p] (pass 1: scratch rows
+// i1 + N1*k2).  With p = g*R + k, bitrev_N(p) = bitrev_r(k) * 2^(N-r) +
+// bitrev_(N-r)(g): walk k in bit-reversed order so the pointer only advances.
+template <class F, int LOGN>
+struct BitrevStore {
+    using T = typename F::T;
+    T* p0;
+    int64_t s;
+    const T* post;
+    bool ok;
+    template <int LR>
+    __device__ __forceinline__ void group(int base, const T* x) const {
+        if (!ok) return;
+        const int g = base >> LR;
+        T* q = p0 + int64_t(bitrev_dev(unsigned(g), LOGN - LR)) * s;
+        const int64_t st = s << (LOGN - LR);
+#pragma unroll
+        for (int j = 0; j < (1 << LR); ++j) {
+            const int k = int(bitrev_ct(unsigned(j), LR));
+            *q = F::mulc(x[k], post[base + k]);
+            q += st;
+        }
+    }
+};
+// Global LDE rows for the final pass: bit-reversed order is contiguous;
+// natural order scatters each position to bitrev_H(row).
+template <class T>
+struct OutStore {
+    T* out;     // column-offset base
+    int64_t w;
+    int64_t row0;
+    int logH;
+    bool bitrev;
+    bool ok;
+    template <int LR>
+    __device__ __forceinline__ void group(int base, const T* x) const {
+        if (!ok) return;
+        if (bitrev) {
+            T* q = out + (row0 + base) * w;
+#pragma unroll
+            for (int k = 0; k < (1 << LR); ++k) {
+                *q = x[k];
+                q += w;
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < (1 << LR); ++k)
+                out[int64_t(bitrev_dev(unsigned(row0 + base + k), logH)) * w] = x[k];
+        }
+    }
+};
+
 // ------------------------------------------------------------ single kernel
 template <class F, int LOGN>
 __global__ void __launch_bounds__(Tile<F, LOGN, LdeCfg<F>::C13>::THREADS)
@@ -108,20 +224,16 @@ k_lde_single(const typename F::T* __restrict__ in, typename F::T* __restrict__ o
     }
     __syncthreads();
     {
-        auto ld = [&](int i) -> T { return ok ? in[size_t(i) * w + col] : T(0); };
-        auto st = [&](int p, T v) { A[SH::addr(p, c)] = v; };
+        GLoad<T> ld{in + col, w, ok};
+        TileStore<T, SH> st{A, c};
         cta_dif<F, SH, LOGN, C, 1>(A, twi, t, c, ld, st);
     }
     for (int tc = 0; tc < (1 << log_b); ++tc) {
         const uint64_t u = bitrev_dev(unsigned(tc), log_b);
         for (int k = tid; k < N; k += NT) pre[k] = F::cmul(sq[k], roots.omega(logH, u * k));
         __syncthreads();  // pre ready; A complete (first round) or B free (later rounds)
-        auto ld = [&](int k) -> T { return F::mulc(A[SH::addr(bitrev_dev(k, LOGN), c)], pre[k]); };
-        auto st = [&](int s, T v) {
-            uint64_t row = uint64_t(tc) * N + s;
-            if (!bitrev_out) row = bitrev_dev(unsigned(row), logH);
-            if (ok) out[row * w + col] = v;
-        };
+        PermLoad<F, SH, LOGN> ld{A, pre, c};
+        OutStore<T> st{out + col, w, int64_t(tc) * N, logH, bitrev_out != 0, ok};
         cta_dif<F, SH, LOGN, C, 0>(B, twf, t, c, ld, st);
         __syncthreads();  // pre and B reused by the next coset
     }
@@ -152,10 +264,8 @@ k_lde_pass1(const typename F::T* __restrict__ in, typename F::T* __restrict__ sc
         post[e] = roots.omega_inv(n, uint64_t(i1) * bitrev_dev(e, LOGN));
     }
     __syncthreads();
-    auto ld = [&](int i) -> T { return ok ? in[(i1 + N1 * i) * w + col] : T(0); };
-    auto st = [&](int p, T v) {
-        if (ok) scratch[(i1 + N1 * int64_t(bitrev_dev(p, LOGN))) * w + col] = F::mulc(v, post[p]);
-    };
+    GLoad<T> ld{in + i1 * w + col, N1 * w, ok};
+    BitrevStore<F, LOGN> st{scratch + i1 * w + col, N1 * w, post, ok};
     cta_dif<F, SH, LOGN, C, 1>(A, tw, t, c, ld, st);
 }
 
@@ -191,8 +301,8 @@ k_lde_pass2(const typename F::T* __restrict__ scratch, typename F::T* __restrict
     }
     __syncthreads();
     {
-        auto ld = [&](int i) -> T { return ok ? scratch[(int64_t(N) * k2 + i) * w + col] : T(0); };
-        auto st = [&](int p, T v) { A[SH::addr(p, c)] = v; };
+        GLoad<T> ld{scratch + int64_t(N) * k2 * w + col, w, ok};
+        TileStore<T, SH> st{A, c};
         cta_dif<F, SH, LOGN, C, 1>(A, twi, t, c, ld, st);
     }
     const T sqk2 = sq[k2];
@@ -203,10 +313,8 @@ k_lde_pass2(const typename F::T* __restrict__ scratch, typename F::T* __restrict
             post[k] = F::cmul(sqk2, roots.omega(logH, uint64_t(k2) * (u + (uint64_t(bitrev_dev(k, LOGN)) << log_b))));
         }
         __syncthreads();
-        auto ld = [&](int k) -> T { return F::mulc(A[SH::addr(bitrev_dev(k, LOGN), c)], pre[k]); };
-        auto st = [&](int s, T v) {
-            if (ok) dst[(tc * h + s * N2 + k2) * w + col] = F::mulc(v, post[s]);
-        };
+        PermLoad<F, SH, LOGN> ld{A, pre, c};
+        GStore<F, true> st{dst + (tc * h + k2) * w + col, N2 * w, post, ok};
         cta_dif<F, SH, LOGN, C, 0>(B, twf, t, c, ld, st);
         __syncthreads();
     }
@@ -234,12 +342,8 @@ k_lde_pass3(const typename F::T* src, typename F::T* out, int w, int n1, int log
 
     for (int e = tid; e < N; e += NT) tw[e] = roots.omega(LOGN, e);
     __syncthreads();
-    auto ld = [&](int i) -> T { return ok ? src[(base + i) * w + col] : T(0); };
-    auto st = [&](int s, T v) {
-        uint64_t row = uint64_t(base + s);
-        if (!bitrev_out) row = bitrev_dev(unsigned(row), logH);
-        if (ok) out[row * w + col] = v;
-    };
+    GLoad<T> ld{src + base * w + col, w, ok};
+    OutStore<T> st{out + col, w, base, logH, bitrev_out != 0, ok};
     cta_dif<F, SH, LOGN, C, 0>(A, tw, t, c, ld, st);
 }
 

@@ -14,6 +14,9 @@
 // supplied `load(row)` (global memory, or a permuted shared-memory tile) and
 // the last hands its results to `store(pos, value)` (global memory, or a
 // tile): only the exchanges between super-stages go through shared memory.
+// Loads and stores work on whole groups (`group<R, M>(base, x)`: rows
+// base + M*k; `group<LR>(base, x)`: positions base + k) so that global
+// accesses walk one strided pointer instead of materialising R addresses.
 // After all super-stages, position p holds X[bitrev_N(p)] -- natural-in /
 // bit-reversed-out, which the callers fold into their global row addressing.
 // Same transform as Radix2Dit::dft_batch (radix2_dit.hpp:82-121); only the
@@ -176,15 +179,15 @@ __device__ __forceinline__ void super_stage(typename F::T* tile, const typename 
         const int blk = g / M, i_lo = g % M;
         const int base = blk * (1 << LS) + i_lo;
         T x[R];
+        if constexpr (FIRST) {
+            load.template group<R, M>(base, x);  // rows base + M*k
+        } else {
 #pragma unroll
-        for (int k = 0; k < R; ++k) {
-            if constexpr (FIRST) x[k] = load(base + M * k);
-            else x[k] = tile[SH::addr(base + M * k, c)];
+            for (int k = 0; k < R; ++k) x[k] = tile[SH::addr(base + M * k, c)];
         }
         reg_dif<F, LR, INV>(x);
         if constexpr (LAST) {
-#pragma unroll
-            for (int k = 0; k < R; ++k) store(base + k, x[k]);  // M == 1
+            store.template group<LR>(base, x);  // positions base + k (M == 1)
         } else {
 #pragma unroll
             for (int s = 1; s < R; ++s) {
@@ -211,7 +214,8 @@ struct SSChain {
 };
 
 // Full in-CTA DIF on one column per thread group: element at natural row i
-// comes from load(i); store(p, v) receives X[bitrev_N(p)].  `tile` is the
+// comes from the load functor; the store functor receives X[bitrev_N(p)] for
+// position p.  `tile` is the
 // exchange buffer (SH::TILE elements).  Callers synchronise around it.
 template <class F, class SH, int LOGN, int C, int INV, class Load, class Store>
 __device__ __forceinline__ void cta_dif(typename F::T* tile, const typename F::T* tw, int t, int c, Load& load,
