@@ -15,6 +15,7 @@
 //  * BabyBear^4 = BabyBear[x]/(x^4 - 11), extension_field.hpp:106-131.
 #pragma once
 #include <cstdint>
+#include <vector_types.h>
 
 #ifndef P3G_HD
 #define P3G_HD __host__ __device__ __forceinline__
@@ -149,12 +150,54 @@ constexpr unsigned TWO_ADICITY = 32;
 
 // ========================================================= field traits for kernels
 // mulc(x, c): x canonical, c a stored constant ("const form"); returns x*c canonical.
+// TW: a twiddle prepared for repeated use; mul_tw(x, tw) = x*w canonical.
+// BabyBear twiddles are Shoup pairs {w, floor(w * 2^32 / p)}: q = mulhi(x, w'),
+// x*w - q*p lies in [0, 2p) for any x < 2^32 (so a butterfly difference can
+// stay unreduced in (0, 2p)), one IMAD.HI and two IMADs.
+namespace bb {
+// floor(v * 2^32 / p) for v < p (Barrett estimate plus one correction).
+P3G_HD uint32_t shoup_companion(uint32_t v) {
+    constexpr uint64_t MU = ~uint64_t(0) / P;  // floor((2^64 - 1) / p)
+    const uint64_t x = uint64_t(v) << 32;
+#ifdef __CUDA_ARCH__
+    uint64_t q = __umul64hi(x, MU);
+#else
+    uint64_t q = uint64_t(((unsigned __int128)x * MU) >> 64);
+#endif
+    uint64_t r = x - q * P;
+    while (r >= P) {
+        r -= P;
+        ++q;
+    }
+    return uint32_t(q);
+}
+P3G_HD uint32_t shoup_mul(uint32_t x, uint32_t w, uint32_t wc) {
+#ifdef __CUDA_ARCH__
+    const uint32_t q = __umulhi(x, wc);
+#else
+    const uint32_t q = uint32_t((uint64_t(x) * wc) >> 32);
+#endif
+    const uint32_t r = x * w - q * P;  // in [0, 2p)
+    const uint32_t s = r - P;
+    return r < s ? r : s;
+}
+}  // namespace bb
+
 struct FBB {
     using T = uint32_t;
+    using TW = uint2;
     static constexpr unsigned TWO_ADICITY = 27;
     static P3G_HD T add(T a, T b) { return bb::add(a, b); }
     static P3G_HD T sub(T a, T b) { return bb::sub(a, b); }
+    // a - b + p in (0, 2p): a difference fed straight into mul_tw
+    static P3G_HD T sub_lazy(T a, T b) { return a - b + bb::P; }
     static P3G_HD T mulc(T a, T c) { return bb::mmul(a, c); }
+    static P3G_HD T mul_tw(T x, TW w) { return bb::shoup_mul(x, w.x, w.y); }
+    // Montgomery-form constant -> Shoup pair of its canonical value
+    static P3G_HD TW tw_from_const(T cm) {
+        const uint32_t v = bb::mmul(cm, 1u);
+        return make_uint2(v, bb::shoup_companion(v));
+    }
     // product of two const-form values, result in const form
     static P3G_HD T cmul(T a, T b) { return bb::mmul(a, b); }
     static inline T to_const(uint64_t canonical) { return bb::to_mont(uint32_t(canonical)); }
@@ -166,9 +209,13 @@ struct FBB {
 };
 struct FGL {
     using T = uint64_t;
+    using TW = uint64_t;
     static constexpr unsigned TWO_ADICITY = 32;
     static P3G_HD T add(T a, T b) { return gl::add(a, b); }
     static P3G_HD T sub(T a, T b) { return gl::sub(a, b); }
+    static P3G_HD T sub_lazy(T a, T b) { return gl::sub(a, b); }
+    static __device__ __forceinline__ T mul_tw(T x, TW w) { return gl::mul(x, w); }
+    static P3G_HD TW tw_from_const(T c) { return c; }
     static __device__ __forceinline__ T mulc(T a, T c) { return gl::mul(a, c); }
     static __device__ __forceinline__ T cmul(T a, T b) { return gl::mul(a, b); }
     static inline T to_const(uint64_t canonical) { return canonical; }

@@ -105,14 +105,14 @@ template <class F, class SH, int LOGN>
 struct PermLoad {
     using T = typename F::T;
     const T* A;
-    const T* pre;
+    const typename F::TW* pre;
     int c;
     template <int R, int M>
     __device__ __forceinline__ void group(int base, T* x) const {
 #pragma unroll
         for (int k = 0; k < R; ++k) {
             const int i = base + M * k;
-            x[k] = F::mulc(A[SH::addr(bitrev_dev(unsigned(i), LOGN), c)], pre[i]);
+            x[k] = F::mul_tw(A[SH::addr(bitrev_dev(unsigned(i), LOGN), c)], pre[i]);
         }
     }
 };
@@ -133,7 +133,7 @@ struct GStore {
     using T = typename F::T;
     T* p0;
     int64_t s;
-    const T* post;
+    const typename F::TW* post;
     bool ok;
     template <int LR>
     __device__ __forceinline__ void group(int base, const T* x) const {
@@ -141,7 +141,7 @@ struct GStore {
         T* q = p0 + base * s;
 #pragma unroll
         for (int k = 0; k < (1 << LR); ++k) {
-            *q = POST ? F::mulc(x[k], post[base + k]) : x[k];
+            *q = POST ? F::mul_tw(x[k], post[base + k]) : x[k];
             q += s;
         }
     }
@@ -154,7 +154,7 @@ struct BitrevStore {
     using T = typename F::T;
     T* p0;
     int64_t s;
-    const T* post;
+    const typename F::TW* post;
     bool ok;
     template <int LR>
     __device__ __forceinline__ void group(int base, const T* x) const {
@@ -165,7 +165,7 @@ struct BitrevStore {
 #pragma unroll
         for (int j = 0; j < (1 << LR); ++j) {
             const int k = int(bitrev_ct(unsigned(j), LR));
-            *q = F::mulc(x[k], post[base + k]);
+            *q = F::mul_tw(x[k], post[base + k]);
             q += st;
         }
     }
@@ -206,21 +206,22 @@ k_lde_single(const typename F::T* __restrict__ in, typename F::T* __restrict__ o
     constexpr int C = LdeCfg<F>::C13;
     using SH = Tile<F, LOGN, C>;
     using T = typename F::T;
-    constexpr int N = SH::N, TPC = SH::TPC, NT = SH::THREADS;
+    using TW = typename F::TW;
+    constexpr int N = SH::N, NT = SH::THREADS;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* A = reinterpret_cast<T*>(smem_raw);
     T* B = A + SH::TILE;
-    T* twi = B + SH::TILE;
-    T* twf = twi + N;
-    T* pre = twf + N;
+    TW* twi = reinterpret_cast<TW*>(B + SH::TILE);
+    TW* twf = twi + N;
+    TW* pre = twf + N;
     const int tid = threadIdx.x, c = tid % C, t = tid / C;
     const int col = blockIdx.y * C + c;
     const bool ok = col < w;
     const int logH = LOGN + log_b;
 
     for (int e = tid; e < N; e += NT) {
-        twi[e] = roots.omega_inv(LOGN, e);
-        twf[e] = roots.omega(LOGN, e);
+        twi[e] = F::tw_from_const(roots.omega_inv(LOGN, e));
+        twf[e] = F::tw_from_const(roots.omega(LOGN, e));
     }
     __syncthreads();
     {
@@ -230,7 +231,7 @@ k_lde_single(const typename F::T* __restrict__ in, typename F::T* __restrict__ o
     }
     for (int tc = 0; tc < (1 << log_b); ++tc) {
         const uint64_t u = bitrev_dev(unsigned(tc), log_b);
-        for (int k = tid; k < N; k += NT) pre[k] = F::cmul(sq[k], roots.omega(logH, u * k));
+        for (int k = tid; k < N; k += NT) pre[k] = F::tw_from_const(F::cmul(sq[k], roots.omega(logH, u * k)));
         __syncthreads();  // pre ready; A complete (first round) or B free (later rounds)
         PermLoad<F, SH, LOGN> ld{A, pre, c};
         OutStore<T> st{out + col, w, int64_t(tc) * N, logH, bitrev_out != 0, ok};
@@ -247,11 +248,12 @@ k_lde_pass1(const typename F::T* __restrict__ in, typename F::T* __restrict__ sc
     constexpr int C = LdeCfg<F>::C13;
     using SH = Tile<F, LOGN, C>;
     using T = typename F::T;
+    using TW = typename F::TW;
     constexpr int N = SH::N, NT = SH::THREADS;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* A = reinterpret_cast<T*>(smem_raw);
-    T* tw = A + SH::TILE;
-    T* post = tw + N;
+    TW* tw = reinterpret_cast<TW*>(A + SH::TILE);
+    TW* post = tw + N;
     const int tid = threadIdx.x, c = tid % C, t = tid / C;
     const int col = blockIdx.y * C + c;
     const bool ok = col < w;
@@ -260,8 +262,8 @@ k_lde_pass1(const typename F::T* __restrict__ in, typename F::T* __restrict__ sc
     const int n = n1 + LOGN;
 
     for (int e = tid; e < N; e += NT) {
-        tw[e] = roots.omega_inv(LOGN, e);
-        post[e] = roots.omega_inv(n, uint64_t(i1) * bitrev_dev(e, LOGN));
+        tw[e] = F::tw_from_const(roots.omega_inv(LOGN, e));
+        post[e] = F::tw_from_const(roots.omega_inv(n, uint64_t(i1) * bitrev_dev(e, LOGN)));
     }
     __syncthreads();
     GLoad<T> ld{in + i1 * w + col, N1 * w, ok};
@@ -278,14 +280,15 @@ k_lde_pass2(const typename F::T* __restrict__ scratch, typename F::T* __restrict
     constexpr int C = LdeCfg<F>::C2;
     using SH = Tile<F, LOGN, C>;
     using T = typename F::T;
+    using TW = typename F::TW;
     constexpr int N = SH::N, NT = SH::THREADS;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* A = reinterpret_cast<T*>(smem_raw);
     T* B = A + SH::TILE;
-    T* twi = B + SH::TILE;
-    T* twf = twi + N;
-    T* pre = twf + N;
-    T* post = pre + N;
+    TW* twi = reinterpret_cast<TW*>(B + SH::TILE);
+    TW* twf = twi + N;
+    TW* pre = twf + N;
+    TW* post = pre + N;
     const int tid = threadIdx.x, c = tid % C, t = tid / C;
     const int col = blockIdx.y * C + c;
     const bool ok = col < w;
@@ -296,8 +299,8 @@ k_lde_pass2(const typename F::T* __restrict__ scratch, typename F::T* __restrict
     const int logH = n + log_b;
 
     for (int e = tid; e < N; e += NT) {
-        twi[e] = roots.omega_inv(LOGN, e);
-        twf[e] = roots.omega(LOGN, e);
+        twi[e] = F::tw_from_const(roots.omega_inv(LOGN, e));
+        twf[e] = F::tw_from_const(roots.omega(LOGN, e));
     }
     __syncthreads();
     {
@@ -309,8 +312,9 @@ k_lde_pass2(const typename F::T* __restrict__ scratch, typename F::T* __restrict
     for (int tc = 0; tc < (1 << log_b); ++tc) {
         const uint64_t u = bitrev_dev(unsigned(tc), log_b);
         for (int k = tid; k < N; k += NT) {
-            pre[k] = F::cmul(sp[k], roots.omega(logH, u * uint64_t(N2) * k));
-            post[k] = F::cmul(sqk2, roots.omega(logH, uint64_t(k2) * (u + (uint64_t(bitrev_dev(k, LOGN)) << log_b))));
+            pre[k] = F::tw_from_const(F::cmul(sp[k], roots.omega(logH, u * uint64_t(N2) * k)));
+            post[k] = F::tw_from_const(
+                F::cmul(sqk2, roots.omega(logH, uint64_t(k2) * (u + (uint64_t(bitrev_dev(k, LOGN)) << log_b)))));
         }
         __syncthreads();
         PermLoad<F, SH, LOGN> ld{A, pre, c};
@@ -328,10 +332,11 @@ k_lde_pass3(const typename F::T* src, typename F::T* out, int w, int n1, int log
     constexpr int C = LdeCfg<F>::C13;
     using SH = Tile<F, LOGN, C>;
     using T = typename F::T;
+    using TW = typename F::TW;
     constexpr int N = SH::N, NT = SH::THREADS;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* A = reinterpret_cast<T*>(smem_raw);
-    T* tw = A + SH::TILE;
+    TW* tw = reinterpret_cast<TW*>(A + SH::TILE);
     const int tid = threadIdx.x, c = tid % C, t = tid / C;
     const int col = blockIdx.y * C + c;
     const bool ok = col < w;
@@ -340,7 +345,7 @@ k_lde_pass3(const typename F::T* src, typename F::T* out, int w, int n1, int log
     const int logH = n + log_b;
     const int64_t base = blk * N;  // = t*h + s1*N2
 
-    for (int e = tid; e < N; e += NT) tw[e] = roots.omega(LOGN, e);
+    for (int e = tid; e < N; e += NT) tw[e] = F::tw_from_const(roots.omega(LOGN, e));
     __syncthreads();
     GLoad<T> ld{src + base * w + col, w, ok};
     OutStore<T> st{out + col, w, base, logH, bitrev_out != 0, ok};
@@ -357,7 +362,7 @@ template <class F, int LOGN>
 static void launch_single(const typename F::T* in, typename F::T* out, int w, int log_b, int br,
                           const typename F::T* sq, RootTab<F> roots, cudaStream_t st) {
     using SH = Tile<F, LOGN, LdeCfg<F>::C13>;
-    size_t smem = (2 * SH::TILE + 3 * SH::N) * sizeof(typename F::T);
+    size_t smem = 2 * SH::TILE * sizeof(typename F::T) + 3 * SH::N * sizeof(typename F::TW);
     auto k = k_lde_single<F, LOGN>;
     set_smem(k, smem);
     dim3 grid(1, ceil_div(w, LdeCfg<F>::C13));
@@ -369,7 +374,7 @@ template <class F, int LOGN>
 static void launch_pass1(const typename F::T* in, typename F::T* scr, int w, int n1, RootTab<F> roots,
                          cudaStream_t st) {
     using SH = Tile<F, LOGN, LdeCfg<F>::C13>;
-    size_t smem = (SH::TILE + 2 * SH::N) * sizeof(typename F::T);
+    size_t smem = SH::TILE * sizeof(typename F::T) + 2 * SH::N * sizeof(typename F::TW);
     auto k = k_lde_pass1<F, LOGN>;
     set_smem(k, smem);
     dim3 grid(1u << n1, ceil_div(w, LdeCfg<F>::C13));
@@ -381,7 +386,7 @@ template <class F, int LOGN>
 static void launch_pass2(const typename F::T* scr, typename F::T* dst, int w, int n2, int log_b,
                          const typename F::T* sp, const typename F::T* sq, RootTab<F> roots, cudaStream_t st) {
     using SH = Tile<F, LOGN, LdeCfg<F>::C2>;
-    size_t smem = (2 * SH::TILE + 4 * SH::N) * sizeof(typename F::T);
+    size_t smem = 2 * SH::TILE * sizeof(typename F::T) + 4 * SH::N * sizeof(typename F::TW);
     auto k = k_lde_pass2<F, LOGN>;
     set_smem(k, smem);
     dim3 grid(1u << n2, ceil_div(w, LdeCfg<F>::C2));
@@ -393,7 +398,7 @@ template <class F, int LOGN>
 static void launch_pass3(const typename F::T* src, typename F::T* out, int w, int n1, int log_b, int br,
                          RootTab<F> roots, cudaStream_t st) {
     using SH = Tile<F, LOGN, LdeCfg<F>::C13>;
-    size_t smem = (SH::TILE + SH::N) * sizeof(typename F::T);
+    size_t smem = SH::TILE * sizeof(typename F::T) + SH::N * sizeof(typename F::TW);
     auto k = k_lde_pass3<F, LOGN>;
     set_smem(k, smem);
     dim3 grid(1u << (n1 + log_b), ceil_div(w, LdeCfg<F>::C13));

@@ -45,10 +45,13 @@ constexpr uint32_t bb_powmod(uint32_t a, uint64_t e) {
     }
     return r;
 }
-constexpr uint32_t bb_w32_m(int j, bool inv) {
+constexpr uint32_t bb_w32(int j, bool inv) {
     uint32_t w = bb_powmod(440564289u, uint64_t(1) << (27 - 5));
     if (inv) w = bb_powmod(w, bb::P - 2);
-    return uint32_t((uint64_t(bb_powmod(w, uint64_t(j))) << 32) % bb::P);
+    return bb_powmod(w, uint64_t(j));
+}
+constexpr uint32_t bb_w32_c(int j, bool inv) {  // Shoup companion floor(w * 2^32 / p)
+    return uint32_t((uint64_t(bb_w32(j, inv)) << 32) / bb::P);
 }
 constexpr uint64_t gl_mulmod(uint64_t a, uint64_t b) {
     return uint64_t((unsigned __int128)a * b % gl::P);
@@ -73,14 +76,16 @@ constexpr uint64_t gl_w32(int j, bool inv) {
     F(0, INV), F(1, INV), F(2, INV), F(3, INV), F(4, INV), F(5, INV), F(6, INV), F(7, INV), F(8, INV), \
     F(9, INV), F(10, INV), F(11, INV), F(12, INV), F(13, INV), F(14, INV), F(15, INV)
 
-// omega_32^(+-j), j < 16, in each field's constant form.
-static __constant__ uint32_t c_bb_w32[2][16] = {{P3G_W16(ct::bb_w32_m, false)}, {P3G_W16(ct::bb_w32_m, true)}};
+// omega_32^(+-j), j < 16: BabyBear as Shoup pairs (value, companion),
+// Goldilocks canonical.
+static __constant__ uint32_t c_bb_w32[2][16] = {{P3G_W16(ct::bb_w32, false)}, {P3G_W16(ct::bb_w32, true)}};
+static __constant__ uint32_t c_bb_w32c[2][16] = {{P3G_W16(ct::bb_w32_c, false)}, {P3G_W16(ct::bb_w32_c, true)}};
 static __constant__ uint64_t c_gl_w32[2][16] = {{P3G_W16(ct::gl_w32, false)}, {P3G_W16(ct::gl_w32, true)}};
 
 template <class F>
-__device__ __forceinline__ typename F::T w32(int inv, int j);
+__device__ __forceinline__ typename F::TW w32(int inv, int j);
 template <>
-__device__ __forceinline__ uint32_t w32<FBB>(int inv, int j) { return c_bb_w32[inv][j]; }
+__device__ __forceinline__ uint2 w32<FBB>(int inv, int j) { return make_uint2(c_bb_w32[inv][j], c_bb_w32c[inv][j]); }
 template <>
 __device__ __forceinline__ uint64_t w32<FGL>(int inv, int j) { return c_gl_w32[inv][j]; }
 
@@ -109,11 +114,10 @@ __device__ __forceinline__ void reg_dif(typename F::T* x) {
             for (int j = 0; j < half; ++j) {
                 typename F::T a = x[blk + j], b = x[blk + j + half];
                 x[blk + j] = F::add(a, b);
-                typename F::T d = F::sub(a, b);
                 if (j == 0) {
-                    x[blk + j + half] = d;
+                    x[blk + j + half] = F::sub(a, b);
                 } else {
-                    x[blk + j + half] = F::mulc(d, w32<F>(INV, j * (32 / (2 * half))));
+                    x[blk + j + half] = F::mul_tw(F::sub_lazy(a, b), w32<F>(INV, j * (32 / (2 * half))));
                 }
             }
         }
@@ -160,9 +164,9 @@ struct DftShape {
     }
 };
 
-// One super-stage J.  tw[e] = omega_N^e (const form), e < N.
+// One super-stage J.  tw[e] = omega_N^e (prepared twiddle), e < N.
 template <class F, class SH, int LOGN, int J, int C, int INV, class Load, class Store>
-__device__ __forceinline__ void super_stage(typename F::T* tile, const typename F::T* tw, int t, int c,
+__device__ __forceinline__ void super_stage(typename F::T* tile, const typename F::TW* tw, int t, int c,
                                             Load& load, Store& store) {
     using T = typename F::T;
     constexpr int CNT = ss_count(LOGN);
@@ -192,7 +196,7 @@ __device__ __forceinline__ void super_stage(typename F::T* tile, const typename 
 #pragma unroll
             for (int s = 1; s < R; ++s) {
                 const int e = (i_lo * int(bitrev_ct(unsigned(s), LR))) << TWS;
-                x[s] = F::mulc(x[s], tw[e]);
+                x[s] = F::mul_tw(x[s], tw[e]);
             }
 #pragma unroll
             for (int k = 0; k < R; ++k) tile[SH::addr(base + M * k, c)] = x[k];
@@ -203,7 +207,7 @@ __device__ __forceinline__ void super_stage(typename F::T* tile, const typename 
 template <class F, class SH, int LOGN, int C, int INV, int J>
 struct SSChain {
     template <class Load, class Store>
-    static __device__ __forceinline__ void run(typename F::T* tile, const typename F::T* tw, int t, int c,
+    static __device__ __forceinline__ void run(typename F::T* tile, const typename F::TW* tw, int t, int c,
                                                Load& load, Store& store) {
         if constexpr (J < ss_count(LOGN)) {
             super_stage<F, SH, LOGN, J, C, INV>(tile, tw, t, c, load, store);
@@ -218,7 +222,7 @@ struct SSChain {
 // position p.  `tile` is the
 // exchange buffer (SH::TILE elements).  Callers synchronise around it.
 template <class F, class SH, int LOGN, int C, int INV, class Load, class Store>
-__device__ __forceinline__ void cta_dif(typename F::T* tile, const typename F::T* tw, int t, int c, Load& load,
+__device__ __forceinline__ void cta_dif(typename F::T* tile, const typename F::TW* tw, int t, int c, Load& load,
                                         Store& store) {
     SSChain<F, SH, LOGN, C, INV, 0>::run(tile, tw, t, c, load, store);
 }
