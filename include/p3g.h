@@ -187,6 +187,38 @@ typedef struct {
 P3G_API int p3g_commit_traces(p3g_ctx *ctx, int field, const p3g_trace *traces, size_t n_traces,
                       uint32_t cap_height, p3g_tree **tree_out, void *h_cap_out, void *stream);
 
+/* ------------------------------------------------------------ batched commit as one graph */
+typedef struct p3g_plan p3g_plan;
+
+typedef struct {
+    const void *d_in;     /* 2^log_height BabyBear^4 values, device */
+    void *d_out;          /* 2^(log_height - log_arity) values, device */
+    uint32_t log_height;
+    uint32_t log_arity;
+    uint32_t beta[4];     /* folding challenge, canonical */
+} p3g_fold_job;
+
+/* Plans the batched commit of a fixed batch of traces (shapes and device
+ * pointers fixed; contents may change between launches): allocates every
+ * LDE, digest layer and work descriptor once and captures the whole step --
+ * all LDEs (bit-reversed rows) list-scheduled over n_streams streams, the
+ * mixed-height MMCS (merkle_tree_mmcs.hpp:100-107) and, if `fold` is given,
+ * one fold_matrix (fri_folding.hpp:200) -- into a CUDA graph.  n_streams = 0
+ * lets an autotuner pick the stream count (cached per shape; persisted to the
+ * JSON file named by the P3G_TUNE_CACHE environment variable).  The batched
+ * counterpart of TwoAdicFriPcs::commit's LDE + commit (two_adic_fri_pcs.hpp:207-266). */
+P3G_API int p3g_plan_commit(p3g_ctx *ctx, int field, const p3g_trace *traces, size_t n_traces,
+                            uint32_t cap_height, const p3g_fold_job *fold, uint32_t n_streams,
+                            p3g_plan **plan_out);
+/* Replays the plan's graph on `stream` (one cudaGraphLaunch). */
+P3G_API int p3g_plan_launch(p3g_ctx *ctx, p3g_plan *plan, void *stream);
+/* The plan's tree (use with p3g_tree_info/_layer_ptr/_leaf_ptr/p3g_mmcs_open_batch;
+ * freed by p3g_plan_destroy, not p3g_tree_free), the stream count in use and
+ * the number of kernels one launch runs. */
+P3G_API int p3g_plan_info(const p3g_plan *plan, const p3g_tree **tree, uint32_t *n_streams,
+                          uint64_t *kernels_per_launch);
+P3G_API int p3g_plan_destroy(p3g_ctx *ctx, p3g_plan *plan);
+
 /* ------------------------------------------------------------ FRI
  * TwoAdicFriFolding<BabyBear, BabyBear4>::fold_matrix (fri_folding.hpp:200-222)
  * with fold_row's interpolation (fri_folding.hpp:74-189); log_arity in 1..3.

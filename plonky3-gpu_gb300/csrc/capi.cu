@@ -293,8 +293,7 @@ static void copy_cap(const p3g_tree* t, void* h_out, cudaStream_t st) {
 
 static void free_tree(p3g_ctx* ctx, p3g_tree* t, cudaStream_t st) {
     if (!t) return;
-    if (t->d_digests) ctx->release(t->d_digests, st);
-    for (void* p : t->owned) ctx->release(p, st);
+    p3g::tree_release(ctx, t, st);
     delete t;
 }
 
@@ -311,8 +310,7 @@ int p3g_mmcs_commit(p3g_ctx* ctx, int field, const p3g_matrix* mats, size_t n_ma
         p3g::mmcs_build(ctx, t.get(), cap_height, S(stream));
         copy_cap(t.get(), h_cap_out, S(stream));
     } catch (...) {
-        if (t->d_digests) ctx->release(t->d_digests, S(stream));
-        t->d_digests = nullptr;
+        p3g::tree_release(ctx, t.get(), S(stream));
         throw;
     }
     *tree_out = t.release();
@@ -333,8 +331,7 @@ int p3g_commit_matrix(p3g_ctx* ctx, int field, const void* d_flat, uint64_t heig
         p3g::flat_build(ctx, t.get(), S(stream));
         copy_cap(t.get(), h_root_out, S(stream));
     } catch (...) {
-        if (t->d_digests) ctx->release(t->d_digests, S(stream));
-        t->d_digests = nullptr;
+        p3g::tree_release(ctx, t.get(), S(stream));
         throw;
     }
     *tree_out = t.release();
@@ -378,6 +375,7 @@ int p3g_mmcs_open_batch(p3g_ctx* ctx, const p3g_tree* tree, const uint64_t* h_in
 int p3g_tree_free(p3g_ctx* ctx, p3g_tree* tree, void* stream) {
     API_BEGIN
     P3G_REQUIRE(ctx, "tree_free: null context");
+    P3G_REQUIRE(!tree || !tree->in_plan, "tree_free: the tree belongs to a plan (p3g_plan_destroy frees it)");
     DeviceGuard g(ctx->device);
     free_tree(ctx, tree, S(stream));
     API_END
@@ -414,8 +412,7 @@ int p3g_commit_traces(p3g_ctx* ctx, int field, const p3g_trace* traces, size_t n
         p3g::mmcs_build(ctx, t.get(), cap_height, st);
         copy_cap(t.get(), h_cap_out, st);
     } catch (...) {
-        if (t->d_digests) ctx->release(t->d_digests, st);
-        for (void* p : t->owned) ctx->release(p, st);
+        p3g::tree_release(ctx, t.get(), st);
         throw;
     }
     *tree_out = t.release();

@@ -113,6 +113,13 @@ struct p3g_tree {
     std::vector<p3g_matrix> mats;     // commit order
     std::vector<void*> owned;         // device buffers owned by the tree (LDEs)
     bool flat = false;                // commit_matrix tree (zero-padded odd layers)
+    // prepared build (see tree_prepare): row-hash work descriptors and the
+    // injected-row digest buffer of every layer that has one
+    void* d_desc = nullptr;
+    std::vector<void*> inj;           // per layer, nullptr when nothing is injected
+    int hash_ngroups = 0;
+    uint64_t hash_units = 0;
+    bool in_plan = false;             // owned by a plan; p3g_tree_free refuses it
 };
 
 namespace p3g {
@@ -126,6 +133,12 @@ void lde_gl(p3g_ctx* ctx, const uint64_t* in, int log_h, int w, int log_b, uint6
 
 void mmcs_build(p3g_ctx* ctx, p3g_tree* tree, unsigned cap_height, cudaStream_t st);
 void flat_build(p3g_ctx* ctx, p3g_tree* tree, cudaStream_t st);
+// Two-phase build: tree_prepare allocates every buffer of the tree and uploads
+// its work descriptors (synchronously when `sync_upload`, e.g. before a graph
+// capture); tree_enqueue only launches kernels on `st`.
+void tree_prepare(p3g_ctx* ctx, p3g_tree* tree, unsigned cap_height, bool flat, cudaStream_t st, bool sync_upload);
+void tree_enqueue(p3g_ctx* ctx, p3g_tree* tree, cudaStream_t st);
+void tree_release(p3g_ctx* ctx, p3g_tree* tree, cudaStream_t st);
 void permute_states(p3g_ctx* ctx, int field, void* d_states, size_t n, cudaStream_t st);
 void open_batch(p3g_ctx* ctx, const p3g_tree* tree, const uint64_t* h_idx, size_t nq,
                 void* h_rows, void* h_proof, cudaStream_t st);

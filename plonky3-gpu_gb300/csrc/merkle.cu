@@ -15,6 +15,7 @@
 // per level computes the compressions and the injection together.  All digest
 // layers stay resident on the device for openings.
 #include <algorithm>
+#include <cstring>
 #include <numeric>
 #include <type_traits>
 
@@ -59,14 +60,15 @@ __global__ void k_open(const OpenMat* mats, int nmats, uint64_t max_h, const uin
 }
 
 template <class H>
-struct LeafFn {
+struct HashFn {
     const typename H::Params* p;
-    const Group<typename H::T>* g;
-    typename H::T* out;
-    uint64_t rows;
+    void* desc;
+    int ngroups;
+    uint64_t units;
+    int sm_count;
     cudaStream_t st;
     template <int D, int RF, int RP>
-    void operator()() const { Launch<H, D, RF, RP>::leaf(*p, *g, out, rows, st); }
+    void operator()() const { Launch<H, D, RF, RP>::hash_groups(*p, desc, ngroups, units, sm_count, st); }
 };
 template <class H>
 struct LevelFn {
@@ -108,109 +110,163 @@ static void dispatch_gl(const p3g_ctx* ctx, const Fn& fn) {
     throw Error(P3G_EUNSUPPORTED, "Goldilocks Poseidon2 schedule not built (supported: x^7 8+22)");
 }
 
-template <class T>
-static Group<T> make_group(const std::vector<p3g_matrix>& mats, const std::vector<size_t>& idx) {
-    Group<T> g;
-    if (idx.size() > size_t(MAXG)) throw Error(P3G_EUNSUPPORTED, "more than 64 matrices of one height");
-    g.n = int(idx.size());
-    for (size_t i = 0; i < idx.size(); ++i) {
-        g.ptr[i] = static_cast<const T*>(mats[idx[i]].d_data);
-        g.w[i] = mats[idx[i]].width;
-    }
-    g.vec = 0;
-    if (g.n == 1 && sizeof(T) == 4 && (g.w[0] % 4) == 0 && (reinterpret_cast<uintptr_t>(g.ptr[0]) % 16) == 0)
-        g.vec = 1;
-    return g;
-}
-
+// ------------------------------------------------------------------ tree build
 template <class H>
-static void build_tree(p3g_ctx* ctx, p3g_tree* tree, unsigned cap_height, const typename H::Params& p,
-                       cudaStream_t st, bool flat) {
+static void prepare(p3g_ctx* ctx, p3g_tree* tree, unsigned cap_height, bool flat, cudaStream_t st,
+                    bool sync_upload) {
     using T = typename H::T;
     const auto& mats = tree->mats;
     const size_t n = mats.size();
     tree->digest = H::DIG;
+    tree->flat = flat;
     std::vector<size_t> order(n);
     std::iota(order.begin(), order.end(), 0);
     std::stable_sort(order.begin(), order.end(),
                      [&](size_t a, size_t b) { return mats[a].height > mats[b].height; });
     const uint64_t max_h = mats[order[0]].height;
-    // layer geometry
-    tree->layer_size.clear();
-    tree->layer_off.clear();
-    uint64_t total = 0, sz = max_h;
-    tree->layer_size.push_back(sz);
-    tree->layer_off.push_back(0);
-    total += sz;
-    if (flat) {
-        while (sz > 1) {
-            sz = (sz + 1) / 2;
-            tree->layer_off.push_back(total);
-            tree->layer_size.push_back(sz);
-            total += sz;
-        }
-    } else {
-        const uint64_t cap = uint64_t(1) << cap_height;
-        while (sz > cap) {
-            sz /= 2;
-            tree->layer_off.push_back(total);
-            tree->layer_size.push_back(sz);
-            total += sz;
-        }
+    // layer geometry (merkle_tree.hpp:145-179; flat: fri_merkle_tree_mmcs.hpp:77-92)
+    tree->layer_size.assign(1, max_h);
+    tree->layer_off.assign(1, 0);
+    uint64_t total = max_h, sz = max_h;
+    const uint64_t cap = uint64_t(1) << cap_height;
+    while (flat ? sz > 1 : sz > cap) {
+        sz = flat ? (sz + 1) / 2 : sz / 2;
+        tree->layer_off.push_back(total);
+        tree->layer_size.push_back(sz);
+        total += sz;
     }
-    T* dig = static_cast<T*>(ctx->alloc(sizeof(T) * H::DIG * total, st));
-    tree->d_digests = dig;
-
+    if (!tree->d_digests) tree->d_digests = ctx->alloc(sizeof(T) * H::DIG * total, st);
+    T* dig = static_cast<T*>(tree->d_digests);
+    // equal-height groups: the tallest makes the leaves; each shorter group is
+    // injected at the level whose size equals its height
+    struct G {
+        std::vector<size_t> idx;
+        uint64_t rows;
+        T* out;
+        uint64_t cost;
+    };
+    std::vector<G> groups;
     size_t next = 0;
     auto collect = [&](uint64_t h) {
         std::vector<size_t> g;
         while (next < n && mats[order[next]].height == h) g.push_back(order[next++]);
         return g;
     };
-    auto tall = collect(max_h);
-    Group<T> g0 = make_group<T>(mats, tall);
+    tree->inj.assign(tree->layer_size.size(), nullptr);
+    groups.push_back({collect(max_h), max_h, dig, 0});
+    if (!flat) {
+        for (size_t l = 1; l < tree->layer_size.size(); ++l) {
+            auto gi = collect(tree->layer_size[l]);
+            if (gi.empty()) continue;
+            if (!tree->inj[l]) tree->inj[l] = ctx->alloc(sizeof(T) * H::DIG * tree->layer_size[l], st);
+            groups.push_back({gi, tree->layer_size[l], static_cast<T*>(tree->inj[l]), 0});
+        }
+    }
+    if (groups.size() > size_t(MAXG)) throw Error(P3G_EUNSUPPORTED, "more than 64 distinct matrix heights");
+    for (auto& g : groups) {
+        if (g.idx.size() > size_t(MAXG)) throw Error(P3G_EUNSUPPORTED, "more than 64 matrices of one height");
+        uint64_t w = 0;
+        for (size_t i : g.idx) w += mats[i].width;
+        g.cost = (w + H::RATE - 1) / H::RATE;  // permutations per row
+    }
+    // most expensive rows first, so the queue drains with cheap units
+    std::stable_sort(groups.begin(), groups.end(), [](const G& a, const G& b) { return a.cost > b.cost; });
+    std::vector<HashGroup<T>> hg;
+    std::vector<HashEntry<T>> he;
+    uint64_t units = 0;
+    for (const auto& g : groups) {
+        HashGroup<T> d{};
+        d.rows = g.rows;
+        d.unit0 = units;
+        d.out = g.out;
+        d.ent0 = uint32_t(he.size());
+        d.nent = uint32_t(g.idx.size());
+        d.vec = 0;
+        for (size_t i : g.idx) he.push_back({static_cast<const T*>(mats[i].d_data), mats[i].width, 0});
+        if (g.idx.size() == 1 && sizeof(T) == 4 && mats[g.idx[0]].width % 4 == 0 &&
+            reinterpret_cast<uintptr_t>(mats[g.idx[0]].d_data) % 16 == 0)
+            d.vec = 1;
+        hg.push_back(d);
+        units += (g.rows + HASH_ROWS - 1) / HASH_ROWS;
+    }
+    const size_t bytes = HASH_DESC_HEADER + sizeof(HashGroup<T>) * MAXG + sizeof(HashEntry<T>) * std::max<size_t>(he.size(), 1);
+    std::vector<char> host(bytes, 0);
+    std::memcpy(host.data() + HASH_DESC_HEADER, hg.data(), sizeof(HashGroup<T>) * hg.size());
+    std::memcpy(host.data() + HASH_DESC_HEADER + sizeof(HashGroup<T>) * MAXG, he.data(), sizeof(HashEntry<T>) * he.size());
+    if (!tree->d_desc) tree->d_desc = ctx->alloc(bytes, st);
+    if (sync_upload) {
+        P3G_CUDA(cudaStreamSynchronize(st));
+        P3G_CUDA(cudaMemcpy(tree->d_desc, host.data(), bytes, cudaMemcpyHostToDevice));
+    } else {
+        // pageable source: the copy is staged before cudaMemcpyAsync returns
+        P3G_CUDA(cudaMemcpyAsync(tree->d_desc, host.data(), bytes, cudaMemcpyHostToDevice, st));
+    }
+    tree->hash_ngroups = int(hg.size());
+    tree->hash_units = units;
+}
+
+template <class H>
+static void enqueue(p3g_ctx* ctx, p3g_tree* tree, const typename H::Params& p, cudaStream_t st) {
+    using T = typename H::T;
     auto run = [&](const auto& fnobj) {
         if constexpr (std::is_same<H, HBB>::value) dispatch_bb(ctx, fnobj);
         else dispatch_gl(ctx, fnobj);
     };
-    run(LeafFn<H>{&p, &g0, dig, max_h, st});
-    T* inj_buf = nullptr;  // row hashes of the matrices injected at a level
+    run(HashFn<H>{&p, tree->d_desc, tree->hash_ngroups, tree->hash_units, ctx->sm_count, st});
+    T* dig = static_cast<T*>(tree->d_digests);
     for (size_t l = 1; l < tree->layer_size.size(); ++l) {
-        const uint64_t level = tree->layer_size[l];
-        const T* inj = nullptr;
-        if (!flat) {
-            auto gi = collect(level);
-            if (!gi.empty()) {
-                Group<T> ig = make_group<T>(mats, gi);
-                if (!inj_buf) inj_buf = static_cast<T*>(ctx->alloc(sizeof(T) * H::DIG * level, st));
-                run(LeafFn<H>{&p, &ig, inj_buf, level, st});
-                inj = inj_buf;
-            }
-        }
         run(LevelFn<H>{&p, dig + tree->layer_off[l - 1] * H::DIG, tree->layer_size[l - 1],
-                       dig + tree->layer_off[l] * H::DIG, level, inj, st});
+                       dig + tree->layer_off[l] * H::DIG, tree->layer_size[l], static_cast<const T*>(tree->inj[l]), st});
     }
-    if (inj_buf) ctx->release(inj_buf, st);
+}
+
+static void validate_tree(const p3g_tree* tree, bool flat) {
+    P3G_REQUIRE(!tree->mats.empty(), "mmcs_commit: need at least one matrix");
+    for (const auto& m : tree->mats) {
+        if (!flat)
+            P3G_REQUIRE(m.height > 0 && (m.height & (m.height - 1)) == 0,
+                        "mmcs_commit: matrix height must be a power of two");
+        P3G_REQUIRE(m.width == 0 || m.d_data != nullptr, "mmcs_commit: null matrix data");
+    }
+}
+
+void tree_prepare(p3g_ctx* ctx, p3g_tree* tree, unsigned cap_height, bool flat, cudaStream_t st, bool sync_upload) {
+    validate_tree(tree, flat);
+    P3G_REQUIRE(cap_height < 63, "mmcs_commit: cap_height too large");
+    if (tree->field == P3G_BABYBEAR) {
+        if (!ctx->has_p2bb) throw Error(P3G_ESTATE, "Poseidon2 constants for BabyBear are not set");
+        prepare<HBB>(ctx, tree, cap_height, flat, st, sync_upload);
+    } else {
+        if (!ctx->has_p2gl) throw Error(P3G_ESTATE, "Poseidon2 constants for Goldilocks are not set");
+        prepare<HGL>(ctx, tree, cap_height, flat, st, sync_upload);
+    }
+}
+
+void tree_enqueue(p3g_ctx* ctx, p3g_tree* tree, cudaStream_t st) {
+    if (tree->field == P3G_BABYBEAR) enqueue<HBB>(ctx, tree, ctx->p2bb, st);
+    else enqueue<HGL>(ctx, tree, ctx->p2gl, st);
+}
+
+void tree_release(p3g_ctx* ctx, p3g_tree* tree, cudaStream_t st) {
+    if (tree->d_digests) ctx->release(tree->d_digests, st);
+    if (tree->d_desc) ctx->release(tree->d_desc, st);
+    for (void* p : tree->inj) ctx->release(p, st);
+    for (void* p : tree->owned) ctx->release(p, st);
+    tree->d_digests = tree->d_desc = nullptr;
+    tree->inj.clear();
+    tree->owned.clear();
 }
 
 void mmcs_build(p3g_ctx* ctx, p3g_tree* tree, unsigned cap_height, cudaStream_t st) {
-    P3G_REQUIRE(!tree->mats.empty(), "mmcs_commit: need at least one matrix");
-    for (const auto& m : tree->mats) {
-        P3G_REQUIRE(m.height > 0 && (m.height & (m.height - 1)) == 0, "mmcs_commit: matrix height must be a power of two");
-        P3G_REQUIRE(m.width == 0 || m.d_data != nullptr, "mmcs_commit: null matrix data");
-    }
-    P3G_REQUIRE(cap_height < 63, "mmcs_commit: cap_height too large");
-    tree->flat = false;
-    if (tree->field == P3G_BABYBEAR) build_tree<HBB>(ctx, tree, cap_height, ctx->p2bb, st, false);
-    else build_tree<HGL>(ctx, tree, cap_height, ctx->p2gl, st, false);
+    tree_prepare(ctx, tree, cap_height, false, st, false);
+    tree_enqueue(ctx, tree, st);
 }
 
 void flat_build(p3g_ctx* ctx, p3g_tree* tree, cudaStream_t st) {
     P3G_REQUIRE(tree->mats.size() == 1, "commit_matrix: one matrix");
     P3G_REQUIRE(tree->mats[0].height > 0 && tree->mats[0].width > 0, "commit_matrix: bad dimensions");
-    tree->flat = true;
-    if (tree->field == P3G_BABYBEAR) build_tree<HBB>(ctx, tree, 0, ctx->p2bb, st, true);
-    else build_tree<HGL>(ctx, tree, 0, ctx->p2gl, st, true);
+    tree_prepare(ctx, tree, 0, true, st, false);
+    tree_enqueue(ctx, tree, st);
 }
 
 void permute_states(p3g_ctx* ctx, int field, void* d_states, size_t n, cudaStream_t st) {

@@ -6,6 +6,7 @@
 // sponge loop fills one rate chunk per iteration, and a compression with an
 // injected row hash runs its two permutations as two iterations of one loop.
 #pragma once
+#include <algorithm>
 #include <type_traits>
 
 #include "internal.hpp"
@@ -79,16 +80,76 @@ __device__ __forceinline__ void hash_group(const Group<typename H::T>& g, uint64
     }
 }
 
+// ---------------------------------------------------------------- row hashing
+// All equal-height groups of a tree (the tallest group's leaves and every
+// injected group's row hashes) are hashed by one persistent kernel: work
+// units of HASH_ROWS rows are handed out through an atomic counter, units of
+// the most expensive groups first, so small groups never leave SMs idle.
+constexpr int HASH_ROWS = 256;  // rows (= threads) per work unit
+
+template <class T>
+struct HashEntry {
+    const T* ptr;
+    uint32_t width;
+    uint32_t pad;
+};
+template <class T>
+struct HashGroup {
+    uint64_t rows;
+    uint64_t unit0;  // first work unit of the group
+    T* out;          // rows x DIG digests
+    uint32_t ent0;   // entries [ent0, ent0 + nent)
+    uint32_t nent;
+    uint32_t vec;    // single matrix, width % 4 == 0, 16-byte aligned
+    uint32_t pad;
+};
+// Device descriptor block: [counter (8 bytes, zeroed per launch) | groups | entries].
+constexpr size_t HASH_DESC_HEADER = 256;
+
 template <class H, int D, int RF, int RP>
-__global__ void __launch_bounds__(128) k_leaf_hash(typename H::Params p, Group<typename H::T> g,
-                                                   typename H::T* __restrict__ out, uint64_t nrows) {
+__global__ void __launch_bounds__(HASH_ROWS) k_hash_groups(typename H::Params p, const HashGroup<typename H::T>* groups,
+                                                           int ngroups, const HashEntry<typename H::T>* ents,
+                                                           uint64_t total_units, unsigned long long* counter) {
     using T = typename H::T;
-    uint64_t r = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (r >= nrows) return;
-    T s[H::W];
-    hash_group<H, D, RF, RP>(g, r, p, s);
+    __shared__ HashGroup<T> sg[MAXG];
+    __shared__ Group<T> cur;
+    __shared__ unsigned long long unit;
+    __shared__ int cur_g;
+    for (int i = threadIdx.x; i < ngroups; i += blockDim.x) sg[i] = groups[i];
+    if (threadIdx.x == 0) cur_g = -1;
+    __syncthreads();
+#pragma unroll 1
+    for (;;) {
+        if (threadIdx.x == 0) unit = atomicAdd(counter, 1ull);
+        __syncthreads();
+        const uint64_t u = unit;
+        if (u >= total_units) return;
+        int g = 0;
+        while (g + 1 < ngroups && sg[g + 1].unit0 <= u) ++g;
+        if (g != cur_g) {  // stage the group's matrix list in shared memory
+            __syncthreads();
+            const uint32_t n = sg[g].nent;
+            for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+                cur.ptr[i] = ents[sg[g].ent0 + i].ptr;
+                cur.w[i] = ents[sg[g].ent0 + i].width;
+            }
+            if (threadIdx.x == 0) {
+                cur.n = int(n);
+                cur.vec = int(sg[g].vec);
+                cur_g = g;
+            }
+            __syncthreads();
+        }
+        const uint64_t r = (u - sg[g].unit0) * HASH_ROWS + threadIdx.x;
+        if (r < sg[g].rows) {
+            T s[H::W];
+            hash_group<H, D, RF, RP>(cur, r, p, s);
+            T* o = sg[g].out + r * H::DIG;
 #pragma unroll
-    for (int i = 0; i < H::DIG; ++i) out[r * H::DIG + i] = H::squeeze(s[i]);
+            for (int i = 0; i < H::DIG; ++i) o[i] = H::squeeze(s[i]);
+        }
+        __syncthreads();  // `unit` and `cur` are rewritten next iteration
+    }
 }
 
 // parent[j] = compress(child[2j], child[2j+1] or the zero digest); with inj,
@@ -143,7 +204,9 @@ __global__ void __launch_bounds__(128) k_permute(typename H::Params p, typename 
 template <class H, int D, int RF, int RP>
 struct Launch {
     using T = typename H::T;
-    static void leaf(const typename H::Params& p, const Group<T>& g, T* out, uint64_t nrows, cudaStream_t st);
+    // persistent hashing of all groups; `desc` = device descriptor block
+    static void hash_groups(const typename H::Params& p, void* desc, int ngroups, uint64_t total_units,
+                            int sm_count, cudaStream_t st);
     static void level(const typename H::Params& p, const T* child, uint64_t nchild, T* parent, uint64_t nparent,
                       const T* inj, cudaStream_t st);
     static void permute(const typename H::Params& p, T* states, uint64_t n, cudaStream_t st);
@@ -151,10 +214,23 @@ struct Launch {
 
 #ifdef P3G_MERKLE_INSTANTIATE
 template <class H, int D, int RF, int RP>
-void Launch<H, D, RF, RP>::leaf(const typename H::Params& p, const Group<T>& g, T* out, uint64_t nrows,
-                                cudaStream_t st) {
-    if (nrows == 0) return;
-    k_leaf_hash<H, D, RF, RP><<<unsigned((nrows + 127) / 128), 128, 0, st>>>(p, g, out, nrows);
+void Launch<H, D, RF, RP>::hash_groups(const typename H::Params& p, void* desc, int ngroups, uint64_t total_units,
+                                       int sm_count, cudaStream_t st) {
+    if (total_units == 0) return;
+    static int occ = 0;  // resident CTAs per SM (same for every device of one architecture)
+    if (occ == 0) {
+        int o = 0;
+        P3G_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_hash_groups<H, D, RF, RP>, HASH_ROWS, 0));
+        occ = o > 0 ? o : 1;
+    }
+    const int grid = occ * sm_count;
+    char* base = static_cast<char*>(desc);
+    auto* counter = reinterpret_cast<unsigned long long*>(base);
+    auto* groups = reinterpret_cast<const HashGroup<T>*>(base + HASH_DESC_HEADER);
+    auto* ents = reinterpret_cast<const HashEntry<T>*>(base + HASH_DESC_HEADER + sizeof(HashGroup<T>) * MAXG);
+    P3G_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned long long), st));
+    const int blocks = int(std::min<uint64_t>(uint64_t(grid), total_units));
+    k_hash_groups<H, D, RF, RP><<<blocks, HASH_ROWS, 0, st>>>(p, groups, ngroups, ents, total_units, counter);
     P3G_LAUNCHED();
     P3G_CUDA(cudaGetLastError());
 }

@@ -26,7 +26,8 @@ EXPORTS = [
     "p3g_set_poseidon2", "p3g_poseidon2_permute", "p3g_coset_lde", "p3g_mmcs_commit",
     "p3g_commit_matrix", "p3g_tree_info", "p3g_tree_layer_ptr", "p3g_tree_leaf_ptr",
     "p3g_mmcs_open_batch", "p3g_tree_free", "p3g_commit_traces", "p3g_fold_matrix_bb4",
-    "p3g_coset_lde_bb_noalloc",
+    "p3g_coset_lde_bb_noalloc", "p3g_plan_commit", "p3g_plan_launch", "p3g_plan_info",
+    "p3g_plan_destroy",
 ]
 
 
@@ -39,6 +40,11 @@ class P3GError(RuntimeError):
 class Matrix(C.Structure):
     _fields_ = [("d_data", C.c_void_p), ("height", C.c_uint64), ("width", C.c_uint32),
                 ("reserved", C.c_uint32)]
+
+
+class FoldJob(C.Structure):
+    _fields_ = [("d_in", C.c_void_p), ("d_out", C.c_void_p), ("log_height", C.c_uint32),
+                ("log_arity", C.c_uint32), ("beta", C.c_uint32 * 4)]
 
 
 class Trace(C.Structure):
@@ -85,6 +91,10 @@ def load(path: str | None = None):
     L.p3g_commit_traces.argtypes = [vp, i32, C.POINTER(Trace), sz, u32, C.POINTER(vp), vp, vp]
     L.p3g_fold_matrix_bb4.argtypes = [vp, vp, u32, u32, vp, vp, vp]
     L.p3g_coset_lde_bb_noalloc.argtypes = [vp, u32, u32, u32, u32, i32, vp, vp]
+    L.p3g_plan_commit.argtypes = [vp, i32, C.POINTER(Trace), sz, u32, C.POINTER(FoldJob), u32, C.POINTER(vp)]
+    L.p3g_plan_launch.argtypes = [vp, vp, vp]
+    L.p3g_plan_info.argtypes = [vp, C.POINTER(vp), C.POINTER(u32), C.POINTER(u64)]
+    L.p3g_plan_destroy.argtypes = [vp, vp]
     for name in EXPORTS:
         if name not in ("p3g_version", "p3g_status_string", "p3g_kernel_launches"):
             getattr(L, name).restype = i32
@@ -244,6 +254,38 @@ class Tree:
     def free(self, stream=None):
         if self.handle:
             check(load().p3g_tree_free(self.ctx.handle, self.handle, stream))
+            self.handle = None
+
+
+class Plan:
+    """A batched commit captured as one CUDA graph (p3g_plan_*)."""
+
+    def __init__(self, ctx: "Context", field: int, traces, cap_height: int = 0, fold=None,
+                 n_streams: int = 0):
+        self.ctx, self.field = ctx, field
+        arr = (Trace * len(traces))(*[Trace(p, lh, w, lb, 0, s) for (p, lh, w, lb, s) in traces])
+        fj = None
+        if fold is not None:
+            d_in, d_out, lh, la, beta = fold
+            fj = FoldJob(d_in, d_out, lh, la, (C.c_uint32 * 4)(*[int(b) for b in beta]))
+        h = C.c_void_p()
+        check(load().p3g_plan_commit(ctx.handle, field, arr, len(traces), cap_height,
+                                     C.byref(fj) if fj is not None else None, n_streams, C.byref(h)))
+        self.handle = h.value
+        t = C.c_void_p()
+        ns = C.c_uint32()
+        kl = C.c_uint64()
+        check(load().p3g_plan_info(self.handle, C.byref(t), C.byref(ns), C.byref(kl)))
+        self.tree = Tree(ctx, t.value, field)
+        self.n_streams = ns.value
+        self.kernels_per_launch = kl.value
+
+    def launch(self, stream=None):
+        check(load().p3g_plan_launch(self.ctx.handle, self.handle, stream))
+
+    def destroy(self):
+        if self.handle:
+            check(load().p3g_plan_destroy(self.ctx.handle, self.handle))
             self.handle = None
 
 

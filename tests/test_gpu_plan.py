@@ -1,0 +1,107 @@
+"""Batched commit captured as one CUDA graph (p3g_plan_*): every digest layer
+and the fold against the oracle, replays after refilling the trace buffers,
+the autotuned stream count, and launch accounting.  Bit-exact."""
+import os
+
+import numpy as np
+import pytest
+
+import oracle as O
+import p3g_gb300 as P
+
+pytestmark = pytest.mark.gpu
+NT = os.cpu_count() or 1
+
+
+def _batch(rng, n, lo=3, hi=11, wmax=40):
+    traces = []
+    for i in range(n):
+        lh = int(rng.integers(lo, hi + 1))
+        w = int(rng.integers(1, wmax))
+        traces.append(rng.integers(0, O.BB_P, size=(1 << lh, w), dtype=np.uint32))
+    # a repeated shape makes a multi-matrix height group
+    traces.append(rng.integers(0, O.BB_P, size=traces[0].shape, dtype=np.uint32))
+    return traces
+
+
+def _oracle_commit(traces, cap=0):
+    ldes = [O.bb_coset_lde(t, 1, 31, True, nthreads=NT) for t in traces]
+    return O.mmcs_commit(O.bb16_params(), ldes, cap, nthreads=NT), ldes
+
+
+@pytest.mark.parametrize("n_streams", [1, 4])
+def test_plan_batched_commit_and_fold(gpu_ctx, n_streams):
+    rng = np.random.default_rng(40 + n_streams)
+    traces = _batch(rng, 9)
+    bufs = [gpu_ctx.to_device(t) for t in traces]
+    lh_fold = 12
+    fv = rng.integers(0, O.BB_P, size=(1 << lh_fold, 4), dtype=np.uint32)
+    beta = rng.integers(0, O.BB_P, size=4, dtype=np.uint32)
+    d_fin = gpu_ctx.to_device(fv)
+    d_fout = gpu_ctx.alloc((1 << (lh_fold - 1)) * 16)
+    plan = P.Plan(gpu_ctx, P.BABYBEAR, [(b.ptr, t.shape[0].bit_length() - 1, t.shape[1], 1, 31)
+                                        for b, t in zip(bufs, traces)],
+                  cap_height=1, fold=(d_fin.ptr, d_fout.ptr, lh_fold, 1, beta), n_streams=n_streams)
+    assert plan.n_streams == n_streams
+    plan.launch()
+    gpu_ctx.sync()
+    want, ldes = _oracle_commit(traces, 1)
+    got = plan.tree.layers()
+    assert len(got) == len(want)
+    for g, w in zip(got, want):
+        assert np.array_equal(g, w)
+    assert np.array_equal(d_fout.download(np.uint32, ((1 << (lh_fold - 1)), 4)),
+                          O.fold_matrix_bb4(fv, lh_fold, 1, beta))
+    # replay with new trace contents in the same buffers
+    traces2 = [rng.integers(0, O.BB_P, size=t.shape, dtype=np.uint32) for t in traces]
+    for b, t in zip(bufs, traces2):
+        b.upload(t)
+    gpu_ctx.sync()
+    plan.launch()
+    gpu_ctx.sync()
+    want2, _ = _oracle_commit(traces2, 1)
+    assert np.array_equal(plan.tree.layers()[-1], want2[-1])
+    plan.destroy()
+    for b in bufs + [d_fin, d_fout]:
+        b.free()
+
+
+def test_plan_autotuned_streams_and_launch_count(gpu_ctx, tmp_path, monkeypatch):
+    monkeypatch.setenv("P3G_TUNE_CACHE", str(tmp_path / "tune.json"))
+    rng = np.random.default_rng(7)
+    traces = _batch(rng, 5, 5, 12, 20)
+    bufs = [gpu_ctx.to_device(t) for t in traces]
+    plan = P.Plan(gpu_ctx, P.BABYBEAR, [(b.ptr, t.shape[0].bit_length() - 1, t.shape[1], 1, 31)
+                                        for b, t in zip(bufs, traces)], n_streams=0)
+    assert plan.n_streams in (1, 2, 4, 8)
+    assert plan.kernels_per_launch > 0
+    before = P.kernel_launches()
+    plan.launch()
+    plan.launch()
+    gpu_ctx.sync()
+    assert P.kernel_launches() - before == 2 * plan.kernels_per_launch
+    want, _ = _oracle_commit(traces, 0)
+    assert np.array_equal(plan.tree.layers()[-1], want[-1])
+    with pytest.raises(P.P3GError):
+        plan.tree.free()
+    plan.destroy()
+    for b in bufs:
+        b.free()
+
+
+def test_plan_goldilocks(gpu_ctx):
+    rng = np.random.default_rng(8)
+    traces = [(rng.integers(0, 2**63, size=(1 << lh, w), dtype=np.uint64) * 2 % np.uint64(O.GL_P)).astype(np.uint64)
+              for lh, w in ((6, 5), (9, 3), (6, 2))]
+    bufs = [gpu_ctx.to_device(t) for t in traces]
+    plan = P.Plan(gpu_ctx, P.GOLDILOCKS, [(b.ptr, t.shape[0].bit_length() - 1, t.shape[1], 2, 7)
+                                          for b, t in zip(bufs, traces)], n_streams=2)
+    plan.launch()
+    gpu_ctx.sync()
+    ldes = [O.gl_coset_lde(t, 2, 7, True) for t in traces]
+    want = O.mmcs_commit(O.gl8_params(), ldes, 0)
+    for g, w in zip(plan.tree.layers(), want):
+        assert np.array_equal(g, w)
+    plan.destroy()
+    for b in bufs:
+        b.free()
