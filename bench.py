@@ -151,6 +151,80 @@ def run_reference(args):
     return 0
 
 
+def config3_shapes(seed: int = 3):
+    """64 BabyBear traces: log2 height uniform over {12..18}, width uniform in [8, 512]."""
+    rng = np.random.default_rng(seed)
+    return [(int(rng.integers(12, 19)), int(rng.integers(8, 513))) for _ in range(64)]
+
+
+def run_batched(P, torch, ctx, dev, stream, steps: int, warmup: int):
+    """Config 3: the 64-trace batch committed as one graph-captured plan (one
+    mixed-height MMCS) plus a fold of a 2^19-row BabyBear^4 quotient, against
+    the same work done per trace (one p3g_commit_traces per trace, then the
+    fold) on one stream.  Traces are generated on the device (seeded)."""
+    sptr = stream.cuda_stream
+    shapes = config3_shapes()
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(3)
+    bufs = [torch.randint(0, BB_P, ((1 << lh) * w,), device=dev, dtype=torch.int64, generator=gen).to(torch.int32)
+            for lh, w in shapes]
+    fin = torch.randint(0, BB_P, ((1 << 19) * 4,), device=dev, dtype=torch.int64, generator=gen).to(torch.int32)
+    fout = torch.empty((1 << 18) * 4, device=dev, dtype=torch.int32)
+    beta = [int(x) for x in np.random.default_rng(4).integers(0, BB_P, 4)]
+    traces = [(b.data_ptr(), lh, w, 1, SHIFT) for b, (lh, w) in zip(bufs, shapes)]
+    elems = sum((1 << (lh + 1)) * w for lh, w in shapes)
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    plan = P.Plan(ctx, P.BABYBEAR, traces, 0, fold=(fin.data_ptr(), fout.data_ptr(), 19, 1, beta), n_streams=0)
+    plan_s = time.perf_counter() - t0
+
+    def timed(fn, n):
+        evs = [torch.cuda.Event(enable_timing=True) for _ in range(n + 1)]
+        torch.cuda.synchronize(dev)
+        with torch.cuda.stream(stream):
+            for i in range(n):
+                evs[i].record(stream)
+                fn()
+            evs[-1].record(stream)
+        torch.cuda.synchronize(dev)
+        return [evs[i].elapsed_time(evs[i + 1]) for i in range(n)]
+
+    for _ in range(warmup):
+        plan.launch(sptr)
+    l0 = P.kernel_launches()
+    bt = timed(lambda: plan.launch(sptr), steps)
+    b_launches = (P.kernel_launches() - l0) // max(steps, 1)
+
+    def plain():
+        for tr in traces:
+            ctx.commit_traces_device(P.BABYBEAR, [tr], 0, stream=sptr).free(sptr)
+        ctx.fold_matrix_bb4_device(fin.data_ptr(), 19, 1, beta, fout.data_ptr(), stream=sptr)
+
+    for _ in range(warmup):
+        plain()
+    l0 = P.kernel_launches()
+    pt = timed(plain, steps)
+    p_launches = (P.kernel_launches() - l0) // max(steps, 1)
+    bms, pms = statistics.mean(bt), statistics.mean(pt)
+    out = {
+        "workload": "64 BabyBear traces, log2 h uniform in {12..18}, width uniform in [8, 512], log_blowup 1, "
+                    "one mixed-height Poseidon2-16 MMCS, plus fold_matrix of a 2^19-row BabyBear^4 quotient "
+                    "(log_arity 1, seeded beta)",
+        "lde_elements": elems,
+        "batched": {"value": elems / (bms / 1e3), "unit": UNIT, "ms_per_step": bms,
+                    "p50_ms": float(np.percentile(bt, 50)), "p99_ms": float(np.percentile(bt, 99)),
+                    "graph_launches_per_step": 1, "kernels_per_step": int(b_launches),
+                    "streams": plan.n_streams, "plan_seconds": plan_s},
+        "plain_per_trace": {"value": elems / (pms / 1e3), "unit": UNIT, "ms_per_step": pms,
+                            "p50_ms": float(np.percentile(pt, 50)), "p99_ms": float(np.percentile(pt, 99)),
+                            "kernels_per_step": int(p_launches)},
+        "batched_over_plain": pms / bms,
+    }
+    plan.destroy()
+    del bufs
+    return out
+
+
 def run_ours(args):
     import ctypes as C
 
@@ -274,6 +348,8 @@ def run_ours(args):
         "stages": {"lde_ms": lde_ms, "merkle_ms": hash_ms, "perms": perms,
                    "perms_per_s": perms / (hash_ms / 1e3) if hash_ms > 0 else None},
     }
+    if not args.no_batched:
+        result["config3"] = run_batched(P, torch, ctx, dev, stream, max(3, args.steps // 2), args.warmup)
     if rank == 0 and not args.no_cpu:
         v, dt, desc = cpu_sample(os.cpu_count() or 1)
         result["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
@@ -294,6 +370,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-batched", action="store_true", help="skip the 64-trace batched comparison")
     ap.add_argument("--log-h", type=int, default=LOG_H, help="trace log2 height (profiling cases)")
     ap.add_argument("--width", type=int, default=WIDTH, help="trace width (profiling cases)")
     args = ap.parse_args()

@@ -328,6 +328,48 @@ def pcs_commit(p: P2Params, traces, log_blowup: int = 1, shift: int = 1):
     return layers[-1][0], flat
 
 
+def mmcs_verify_batch(p: P2Params, cap, heights, widths, index: int, opened_rows, proof) -> bool:
+    """MerkleTreeMmcs::verify_batch (merkle_tree_mmcs.hpp:168-254): hash the
+    tallest matrices' opened rows, walk the sibling path compressing (left or
+    right by the index bit) and injecting the rows of matrices whose height
+    equals the new level size, then compare with cap[index >> levels]."""
+    n = len(heights)
+    order = sorted(range(n), key=lambda i: -heights[i])  # stable: sorted() is stable
+    max_h = heights[order[0]]
+    cap = np.asarray(cap)
+    cap_size = cap.shape[0]
+    levels, h = 0, max_h
+    while h > cap_size:
+        h //= 2
+        levels += 1
+    if len(proof) != levels:
+        return False
+    pos = 0
+
+    def collect(hh):
+        nonlocal pos
+        out = []
+        while pos < n and heights[order[pos]] == hh:
+            out.append(order[pos])
+            pos += 1
+        return out
+
+    tall = collect(max_h)
+    cur = hash_iter(p, np.concatenate([np.asarray(opened_rows[i]) for i in tall]) if tall else np.zeros(0))
+    idx = index
+    for step in range(levels):
+        sib = np.asarray(proof[step])
+        cur = compress(p, cur, sib) if idx % 2 == 0 else compress(p, sib, cur)
+        idx >>= 1
+        inj = collect(max_h >> (step + 1))
+        if inj:
+            rh = hash_iter(p, np.concatenate([np.asarray(opened_rows[i]) for i in inj]))
+            cur = compress(p, cur, rh)
+    if idx >= cap_size:
+        return False
+    return bool(np.array_equal(cur, cap[idx]))
+
+
 # ------------------------------------------------------------------ FRI fold
 def fold_matrix_bb4(values: np.ndarray, log_height: int, log_arity: int, beta,
                     nthreads: int = 1) -> np.ndarray:

@@ -272,3 +272,24 @@ def test_fold_arity2_closed_form():
         d = [(int(a) - int(b)) * inv2 % p * L.orc_bb_inv(x) % p for a, b in zip(e0, e1)]
         bd = O.bb4_mul(beta, np.array(d, np.uint32))
         assert out[i].tolist() == [(a + int(b)) % p for a, b in zip(s, bd)]
+
+
+def test_mmcs_verify_batch_against_reference_trees(golden):
+    # verify_batch restated in the oracle accepts the reference's own trees and
+    # rejects a tampered row (merkle_tree_mmcs.hpp:168-254).
+    for case in golden["mmcs"]:
+        if case["kind"] == "gl8":
+            continue
+        p = _p2(case["kind"])
+        mats = _mats(case["kind"], case["shapes"], case["seed"])
+        layers = [np.array(l, dtype=np.uint32) for l in case["layers"]]
+        heights = [m.shape[0] for m in mats]
+        max_h = max(heights)
+        for index in (0, max_h - 1, max_h // 2):
+            rows = [m[index // (max_h // m.shape[0])] for m in mats]
+            proof = [layers[l][(index >> l) ^ 1] for l in range(len(layers) - 1)]
+            assert O.mmcs_verify_batch(p, layers[-1], heights, [m.shape[1] for m in mats], index, rows, proof)
+            if rows[0].size:
+                bad = [r.copy() for r in rows]
+                bad[0][0] ^= 1
+                assert not O.mmcs_verify_batch(p, layers[-1], heights, [m.shape[1] for m in mats], index, bad, proof)
