@@ -225,6 +225,74 @@ def run_batched(P, torch, ctx, dev, stream, steps: int, warmup: int):
     return out
 
 
+def run_serving(P, torch, ctx, rates, per_rate: int, slots: int = 8):
+    """Config 4: Poisson arrivals of commit+fold requests (log2 h uniform in
+    {10..20}, width uniform in [4, 256], log_blowup in {1, 2, 3}) into the
+    continuous-batching server; each completed request gets a 32-query
+    opening on its resident LDE/tree and is then released.  Latency is from
+    the scheduled arrival to the result; elements/s counts committed LDE
+    elements over the run.  Request payloads are prefixes of one pinned host
+    buffer of random BabyBear elements."""
+    import ctypes as C
+
+    max_elems = (1 << 20) * 256
+    host = torch.randint(0, BB_P, (max_elems,), dtype=torch.int64).to(torch.int32).pin_memory()
+    hptr = host.data_ptr()
+    server = P.Server(ctx, max_slots=slots)
+    out = []
+    rid = 0
+    try:
+        for lam in rates:
+            rng = np.random.default_rng(int(lam))
+            reqs = []
+            t = 0.0
+            for _ in range(per_rate):
+                t += rng.exponential(1.0 / lam)
+                lh, w, lb = int(rng.integers(10, 21)), int(rng.integers(4, 257)), int(rng.integers(1, 4))
+                beta = [int(x) for x in rng.integers(0, BB_P, 4)]
+                reqs.append((t, lh, w, lb, beta))
+            arrival = {}
+            lat, open_ms, elems = [], [], 0
+            done = 0
+            i = 0
+            t0 = time.monotonic_ns()
+            while done < len(reqs):
+                now = (time.monotonic_ns() - t0) / 1e9
+                while i < len(reqs) and reqs[i][0] <= now:
+                    tt, lh, w, lb, beta = reqs[i]
+                    rid += 1
+                    arrival[rid] = (t0 + int(tt * 1e9), lh, w, lb)
+                    server.submit(rid, hptr, lh, w, lb, SHIFT, beta)
+                    i += 1
+                for r in server.poll():
+                    a, lh, w, lb = arrival.pop(r.id)
+                    if r.status == 0:
+                        lat.append((r.t_done_ns - a) / 1e6)
+                        elems += (1 << (lh + lb)) * w
+                        q = np.random.default_rng(r.id).integers(0, 1 << (lh + lb), 32, dtype=np.uint64)
+                        o0 = time.perf_counter()
+                        server.open(r.id, q, w, lh + lb + 1)
+                        open_ms.append((time.perf_counter() - o0) * 1e3)
+                        server.release(r.id)
+                    done += 1
+                if i < len(reqs):
+                    time.sleep(max(0.0, min(0.0005, reqs[i][0] - (time.monotonic_ns() - t0) / 1e9)))
+                else:
+                    time.sleep(0.0002)
+            wall = (time.monotonic_ns() - t0) / 1e9
+            out.append({"rate_per_s": lam, "requests": len(reqs), "completed": len(lat),
+                        "p50_ms": float(np.percentile(lat, 50)) if lat else None,
+                        "p99_ms": float(np.percentile(lat, 99)) if lat else None,
+                        "elements_per_s": elems / wall, "wall_s": wall,
+                        "open32_p50_ms": float(np.percentile(open_ms, 50)) if open_ms else None})
+    finally:
+        server.close()
+    return {"workload": "Poisson commit+fold requests: log2 h uniform in {10..20}, width uniform in [4, 256], "
+                        "log_blowup uniform in {1, 2, 3}; fold of the LDE's first four columns as BabyBear^4; "
+                        "32-query opening on the resident tree, then release",
+            "slots": slots, "points": out}
+
+
 def run_ours(args):
     import ctypes as C
 
@@ -350,6 +418,8 @@ def run_ours(args):
     }
     if not args.no_batched:
         result["config3"] = run_batched(P, torch, ctx, dev, stream, max(3, args.steps // 2), args.warmup)
+    if not args.no_serving:
+        result["config4"] = run_serving(P, torch, ctx, [50, 100, 200, 500, 1000, 2000], args.serving_requests)
     if rank == 0 and not args.no_cpu:
         v, dt, desc = cpu_sample(os.cpu_count() or 1)
         result["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
@@ -371,6 +441,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-batched", action="store_true", help="skip the 64-trace batched comparison")
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop latency sweep")
+    ap.add_argument("--serving-requests", type=int, default=200, help="requests per arrival rate")
     ap.add_argument("--log-h", type=int, default=LOG_H, help="trace log2 height (profiling cases)")
     ap.add_argument("--width", type=int, default=WIDTH, help="trace width (profiling cases)")
     args = ap.parse_args()

@@ -219,6 +219,55 @@ P3G_API int p3g_plan_info(const p3g_plan *plan, const p3g_tree **tree, uint32_t 
                           uint64_t *kernels_per_launch);
 P3G_API int p3g_plan_destroy(p3g_ctx *ctx, p3g_plan *plan);
 
+/* ------------------------------------------------------------ serving loop */
+typedef struct p3g_server p3g_server;
+
+typedef struct {
+    uint64_t id;
+    const void *h_trace;  /* (1 << log_h) x width BabyBear, host memory (pinned for
+                             asynchronous copies); valid until the result is polled */
+    uint32_t log_h;
+    uint32_t width;       /* >= 4 */
+    uint32_t log_blowup;
+    uint32_t reserved;
+    uint64_t shift;
+    uint32_t beta[4];     /* fold challenge */
+} p3g_request;
+
+typedef struct {
+    uint64_t id;
+    int32_t status;       /* P3G_OK, P3G_ENOMEM (larger than the budget), ... */
+    uint32_t reserved;
+    uint32_t root[8];     /* MMCS commitment of the bit-reversed LDE */
+    uint32_t fold_head[4];/* first value of the fold */
+    uint64_t t_submit_ns, t_admit_ns, t_done_ns;  /* steady-clock timestamps */
+} p3g_result;
+
+/* A continuous-batching commit+fold service on the context's GPU.  Requests
+ * queue in submission order; a worker thread admits the head as soon as one of
+ * `max_slots` streams is free and its device-memory footprint fits
+ * `mem_budget_bytes` (0 = 80% of the currently free memory), so requests that
+ * arrive while others run overlap on the device.  Each request: host->device
+ * copy, coset LDE (bit-reversed rows), Poseidon2 MMCS commit, and fold_matrix
+ * (log_arity 1) of the LDE's first four columns read as BabyBear^4 values.  The
+ * LDE and tree stay resident (and count against the budget) until
+ * p3g_server_release; p3g_server_open serves MerkleTreeMmcs::open_batch
+ * queries on them.  The reference has no serving layer; this mirrors its
+ * commit (merkle_tree_mmcs.hpp:100-107), open_batch (:120-152) and
+ * fold_matrix (fri_folding.hpp:200) per request. */
+P3G_API int p3g_server_create(p3g_ctx *ctx, uint32_t max_slots, uint64_t mem_budget_bytes,
+                              p3g_server **server_out);
+P3G_API int p3g_server_submit(p3g_server *server, const p3g_request *request);
+/* Moves up to max_results completed results (in completion order) to `out`. */
+P3G_API int p3g_server_poll(p3g_server *server, p3g_result *out, size_t max_results, size_t *n_out);
+P3G_API int p3g_server_pending(p3g_server *server, uint64_t *queued, uint64_t *in_flight,
+                               uint64_t *resident, uint64_t *bytes_used);
+P3G_API int p3g_server_open(p3g_server *server, uint64_t id, const uint64_t *h_indices,
+                            size_t n_queries, void *h_rows, void *h_proof);
+P3G_API int p3g_server_release(p3g_server *server, uint64_t id);
+/* Stops the worker; queued requests are dropped, in-flight ones are waited for. */
+P3G_API int p3g_server_destroy(p3g_server *server);
+
 /* ------------------------------------------------------------ FRI
  * TwoAdicFriFolding<BabyBear, BabyBear4>::fold_matrix (fri_folding.hpp:200-222)
  * with fold_row's interpolation (fri_folding.hpp:74-189); log_arity in 1..3.

@@ -27,7 +27,8 @@ EXPORTS = [
     "p3g_commit_matrix", "p3g_tree_info", "p3g_tree_layer_ptr", "p3g_tree_leaf_ptr",
     "p3g_mmcs_open_batch", "p3g_tree_free", "p3g_commit_traces", "p3g_fold_matrix_bb4",
     "p3g_coset_lde_bb_noalloc", "p3g_plan_commit", "p3g_plan_launch", "p3g_plan_info",
-    "p3g_plan_destroy",
+    "p3g_plan_destroy", "p3g_server_create", "p3g_server_submit", "p3g_server_poll",
+    "p3g_server_pending", "p3g_server_open", "p3g_server_release", "p3g_server_destroy",
 ]
 
 
@@ -45,6 +46,18 @@ class Matrix(C.Structure):
 class FoldJob(C.Structure):
     _fields_ = [("d_in", C.c_void_p), ("d_out", C.c_void_p), ("log_height", C.c_uint32),
                 ("log_arity", C.c_uint32), ("beta", C.c_uint32 * 4)]
+
+
+class Request(C.Structure):
+    _fields_ = [("id", C.c_uint64), ("h_trace", C.c_void_p), ("log_h", C.c_uint32), ("width", C.c_uint32),
+                ("log_blowup", C.c_uint32), ("reserved", C.c_uint32), ("shift", C.c_uint64),
+                ("beta", C.c_uint32 * 4)]
+
+
+class Result(C.Structure):
+    _fields_ = [("id", C.c_uint64), ("status", C.c_int32), ("reserved", C.c_uint32),
+                ("root", C.c_uint32 * 8), ("fold_head", C.c_uint32 * 4),
+                ("t_submit_ns", C.c_uint64), ("t_admit_ns", C.c_uint64), ("t_done_ns", C.c_uint64)]
 
 
 class Trace(C.Structure):
@@ -95,6 +108,13 @@ def load(path: str | None = None):
     L.p3g_plan_launch.argtypes = [vp, vp, vp]
     L.p3g_plan_info.argtypes = [vp, C.POINTER(vp), C.POINTER(u32), C.POINTER(u64)]
     L.p3g_plan_destroy.argtypes = [vp, vp]
+    L.p3g_server_create.argtypes = [vp, u32, u64, C.POINTER(vp)]
+    L.p3g_server_submit.argtypes = [vp, C.POINTER(Request)]
+    L.p3g_server_poll.argtypes = [vp, C.POINTER(Result), sz, C.POINTER(sz)]
+    L.p3g_server_pending.argtypes = [vp, C.POINTER(u64), C.POINTER(u64), C.POINTER(u64), C.POINTER(u64)]
+    L.p3g_server_open.argtypes = [vp, u64, vp, sz, vp, vp]
+    L.p3g_server_release.argtypes = [vp, u64]
+    L.p3g_server_destroy.argtypes = [vp]
     for name in EXPORTS:
         if name not in ("p3g_version", "p3g_status_string", "p3g_kernel_launches"):
             getattr(L, name).restype = i32
@@ -286,6 +306,47 @@ class Plan:
     def destroy(self):
         if self.handle:
             check(load().p3g_plan_destroy(self.ctx.handle, self.handle))
+            self.handle = None
+
+
+class Server:
+    """Continuous-batching commit+fold service (p3g_server_*)."""
+
+    def __init__(self, ctx: "Context", max_slots: int = 4, mem_budget: int = 0):
+        self.ctx = ctx
+        h = C.c_void_p()
+        check(load().p3g_server_create(ctx.handle, max_slots, mem_budget, C.byref(h)))
+        self.handle = h.value
+
+    def submit(self, rid: int, h_trace_ptr: int, log_h: int, width: int, log_blowup: int, shift: int, beta):
+        r = Request(rid, h_trace_ptr, log_h, width, log_blowup, 0, shift,
+                    (C.c_uint32 * 4)(*[int(b) for b in beta]))
+        check(load().p3g_server_submit(self.handle, C.byref(r)))
+
+    def poll(self, max_results: int = 256):
+        arr = (Result * max_results)()
+        n = C.c_size_t()
+        check(load().p3g_server_poll(self.handle, arr, max_results, C.byref(n)))
+        return [arr[i] for i in range(n.value)]
+
+    def pending(self):
+        q, f, r, b = C.c_uint64(), C.c_uint64(), C.c_uint64(), C.c_uint64()
+        check(load().p3g_server_pending(self.handle, C.byref(q), C.byref(f), C.byref(r), C.byref(b)))
+        return q.value, f.value, r.value, b.value
+
+    def open(self, rid: int, indices, width: int, nlayers: int):
+        idx = np.ascontiguousarray(indices, dtype=np.uint64)
+        rows = np.zeros((idx.size, width), np.uint32)
+        proof = np.zeros((idx.size, max(nlayers - 1, 0), 8), np.uint32)
+        check(load().p3g_server_open(self.handle, rid, _np_ptr(idx), idx.size, _np_ptr(rows), _np_ptr(proof)))
+        return rows, proof
+
+    def release(self, rid: int):
+        check(load().p3g_server_release(self.handle, rid))
+
+    def close(self):
+        if self.handle:
+            check(load().p3g_server_destroy(self.handle))
             self.handle = None
 
 
