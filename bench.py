@@ -151,6 +151,71 @@ def run_reference(args):
     return 0
 
 
+GL_P = 0xFFFFFFFF00000001
+
+
+def run_goldilocks(P, torch, ctx, dev, stream, steps: int, warmup: int, log_h: int = 18, width: int = 128,
+                   log_b: int = 2, shift: int = 7):
+    """Config 2: the plain single-trace Goldilocks commit -- a 2^18 x 128 trace
+    of uniform canonical u64 elements, coset LDE with log_blowup 2 and shift 7
+    (2^20 x 128 = 1 GiB of u64, rows bit-reversed), Poseidon2-8 (x^7, 8+22)
+    MMCS with 4-element digests.  Device-timed with the trace resident; the
+    LDE alone is timed beside it for its HBM roofline."""
+    sptr = stream.cuda_stream
+    h, H = 1 << log_h, 1 << (log_h + log_b)
+    rng = np.random.default_rng(2)
+    trace = rng.integers(0, GL_P, size=(h, width), dtype=np.uint64)
+    d_trace = ctx.to_device(trace)
+    ctx.sync()
+
+    def step():
+        ctx.commit_traces_device(P.GOLDILOCKS, [(d_trace.ptr, log_h, width, log_b, shift)], 0,
+                                 stream=sptr).free(sptr)
+
+    def timed(fn, n):
+        evs = [torch.cuda.Event(enable_timing=True) for _ in range(n + 1)]
+        torch.cuda.synchronize(dev)
+        with torch.cuda.stream(stream):
+            for i in range(n):
+                evs[i].record(stream)
+                fn()
+            evs[-1].record(stream)
+        torch.cuda.synchronize(dev)
+        return [evs[i].elapsed_time(evs[i + 1]) for i in range(n)]
+
+    for _ in range(warmup):
+        step()
+    l0 = P.kernel_launches()
+    st = timed(step, steps)
+    launches = (P.kernel_launches() - l0) // max(steps, 1)
+    d_lde = ctx.alloc(H * width * 8, sptr)
+
+    def lde():
+        ctx.coset_lde_device(P.GOLDILOCKS, d_trace.ptr, log_h, width, log_b, shift, True, d_lde.ptr, sptr)
+
+    for _ in range(2):
+        lde()
+    lt = timed(lde, 10)
+    d_lde.free(sptr)
+    torch.cuda.synchronize(dev)
+    d_trace.free()
+    ms, lde_ms = statistics.mean(st), statistics.mean(lt)
+    lde_bytes = 8 * width * (h + H)
+    hbm, src = peaks()
+    perms = H * ((width + 3) // 4) + (H - 1)
+    return {
+        "workload": f"plain single-trace Goldilocks commit: 2^{log_h} x {width} trace, log_blowup {log_b}, "
+                    f"shift {shift}, bit-reversed LDE 2^{log_h + log_b} x {width}, Poseidon2-8 (x^7, 8+22) MMCS, "
+                    "cap_height 0",
+        "value": H * width / (ms / 1e3), "unit": UNIT, "dtype": "u64 (Goldilocks)", "ms_per_step": ms,
+        "p50_ms": float(np.percentile(st, 50)), "p99_ms": float(np.percentile(st, 99)),
+        "kernels_per_step": int(launches),
+        "lde": {"ms": lde_ms, "algorithmic_bytes": lde_bytes, "achieved_gbs": lde_bytes / (lde_ms / 1e3) / 1e9,
+                "peak_gbs": hbm, "frac": lde_bytes / (lde_ms / 1e3) / 1e9 / hbm, "peak_source": src},
+        "merkle": {"ms": ms - lde_ms, "perms": perms, "perms_per_s": perms / ((ms - lde_ms) / 1e3)},
+    }
+
+
 def config3_shapes(seed: int = 3):
     """64 BabyBear traces: log2 height uniform over {12..18}, width uniform in [8, 512]."""
     rng = np.random.default_rng(seed)
@@ -416,6 +481,8 @@ def run_ours(args):
         "stages": {"lde_ms": lde_ms, "merkle_ms": hash_ms, "perms": perms,
                    "perms_per_s": perms / (hash_ms / 1e3) if hash_ms > 0 else None},
     }
+    if not args.no_goldilocks:
+        result["config2"] = run_goldilocks(P, torch, ctx, dev, stream, max(3, args.steps // 2), args.warmup)
     if not args.no_batched:
         result["config3"] = run_batched(P, torch, ctx, dev, stream, max(3, args.steps // 2), args.warmup)
     if not args.no_serving:
@@ -440,6 +507,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-goldilocks", action="store_true", help="skip the Goldilocks 2^18 x 128 commit")
     ap.add_argument("--no-batched", action="store_true", help="skip the 64-trace batched comparison")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop latency sweep")
     ap.add_argument("--serving-requests", type=int, default=200, help="requests per arrival rate")

@@ -1,0 +1,340 @@
+// p3g_adapters.hpp -- drop-in C++ adapters for the reference's commitment interfaces.
+//
+// Each adapter derives from the reference class it accelerates and replaces
+// only the hot member with a call through the C ABI (p3g.h); everything else
+// -- openings, verification, the Commitment / ProverData types -- is the
+// reference's own.  Host data in, host data out, exactly like the reference
+// (by-value RowMajorMatrix, host copies of leaves and digest layers), so the
+// adapters can be passed as template arguments wherever the reference classes
+// are:
+//
+//   GpuDft<p3_dft::Radix2Dit<BabyBear>>            coset_lde_batch      (radix2_dit.hpp:221)
+//   GpuInputMmcs<p3_merkle::MerkleTreeMmcs<...>>   commit_matrix        (fri_merkle_tree_mmcs.hpp:55)
+//   GpuMerkleTreeMmcs<p3_merkle_tree::MerkleTreeMmcs<...>> commit       (merkle_tree_mmcs.hpp:100)
+//   gpu_fold_matrix<Val, Challenge>(...)          fold_matrix           (fri_folding.hpp:200)
+//
+// e.g. TwoAdicFriPcs<BB, BB4, GpuDft<Radix2Dit<BB>>, GpuInputMmcs<FlatMmcs>, EFMmcs>.
+// The element types must be the reference's 4-byte BabyBear (value(),
+// BabyBear(uint32_t)) or 8-byte Goldilocks (as_canonical_u64(),
+// Goldilocks(uint64_t)); a BabyBear4 challenge exposes operator[] over 4
+// BabyBear coefficients.  Errors raise std::invalid_argument (bad arguments,
+// as the reference's log2_strict_usize does) or std::runtime_error (device
+// failures).  All calls use the process-wide p3g::Context.
+#pragma once
+
+#include <algorithm>
+#include <array>
+#include <cstdint>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <stdexcept>
+#include <string>
+#include <type_traits>
+#include <utility>
+#include <vector>
+
+#include "p3g.h"
+
+namespace p3g {
+
+inline void check(int status) {
+    if (status == P3G_OK) return;
+    char msg[1024];
+    p3g_last_error(msg, sizeof msg);
+    if (status == P3G_EINVAL) throw std::invalid_argument(msg);
+    throw std::runtime_error(msg);
+}
+
+template <class F>
+constexpr int field_id() {
+    static_assert(sizeof(F) == 4 || sizeof(F) == 8, "BabyBear (4 bytes) or Goldilocks (8 bytes)");
+    return sizeof(F) == 4 ? P3G_BABYBEAR : P3G_GOLDILOCKS;
+}
+template <class F>
+inline uint64_t canonical(const F& x) {
+    if constexpr (sizeof(F) == 4) return uint64_t(x.value());
+    else return x.as_canonical_u64();
+}
+template <class F>
+inline F from_canonical(uint64_t v) {
+    if constexpr (sizeof(F) == 4) return F(uint32_t(v));
+    else return F(uint64_t(v));
+}
+
+// Process-wide context (device 0 unless select_device() runs first).
+class Context {
+   public:
+    static Context& get() {
+        static Context c;
+        return c;
+    }
+    void select_device(int d) { device_ = d; }
+    p3g_ctx* handle() {
+        std::lock_guard<std::mutex> lk(mu_);
+        if (!ctx_) check(p3g_ctx_create(device_, &ctx_));
+        return ctx_;
+    }
+    // Poseidon2 constants in the reference's constructor shape (poseidon2.hpp:193):
+    // ExternalLayerConstants' initial / terminal rows and the internal constants.
+    template <class F, size_t W>
+    void set_poseidon2(const std::vector<std::array<F, W>>& initial, const std::vector<std::array<F, W>>& terminal,
+                       const std::vector<F>& internal, uint32_t degree) {
+        if (initial.size() != terminal.size()) throw std::invalid_argument("External constants size mismatch");
+        std::vector<uint64_t> ini, ter, inr;
+        for (size_t r = 0; r < initial.size(); ++r)
+            for (size_t i = 0; i < W; ++i) {
+                ini.push_back(canonical(initial[r][i]));
+                ter.push_back(canonical(terminal[r][i]));
+            }
+        for (const F& c : internal) inr.push_back(canonical(c));
+        if (inr.empty()) inr.push_back(0);
+        const uint32_t rf = uint32_t(2 * initial.size()), rp = uint32_t(internal.size());
+        if constexpr (sizeof(F) == 4) {
+            std::vector<uint32_t> a(ini.begin(), ini.end()), b(ter.begin(), ter.end()), c(inr.begin(), inr.end());
+            check(p3g_set_poseidon2(handle(), P3G_BABYBEAR, uint32_t(W), rf, rp, degree, a.data(), b.data(), c.data()));
+        } else {
+            check(p3g_set_poseidon2(handle(), P3G_GOLDILOCKS, uint32_t(W), rf, rp, degree, ini.data(), ter.data(),
+                                    inr.data()));
+        }
+    }
+    // The same from a Poseidon2Cuda<F, W, RF, RP, D> (poseidon2_cuda.hpp:38).
+    template <class F, size_t W, size_t RF, size_t RP>
+    void set_poseidon2(const F (&initial)[RF][W], const F (&terminal)[RF][W], const F (&internal)[RP],
+                       uint32_t degree) {
+        std::vector<std::array<F, W>> a(RF), b(RF);
+        for (size_t r = 0; r < RF; ++r)
+            for (size_t i = 0; i < W; ++i) {
+                a[r][i] = initial[r][i];
+                b[r][i] = terminal[r][i];
+            }
+        set_poseidon2(a, b, std::vector<F>(internal, internal + RP), degree);
+    }
+    ~Context() {
+        if (ctx_) p3g_ctx_destroy(ctx_);
+    }
+
+   private:
+    Context() = default;
+    std::mutex mu_;
+    int device_ = 0;
+    p3g_ctx* ctx_ = nullptr;
+};
+
+// Device buffer from the context pool.
+class DeviceBuffer {
+   public:
+    explicit DeviceBuffer(size_t bytes) : ctx_(Context::get().handle()) { check(p3g_malloc(ctx_, bytes, &p_, nullptr)); }
+    ~DeviceBuffer() {
+        if (p_) p3g_free(ctx_, p_, nullptr);
+    }
+    DeviceBuffer(const DeviceBuffer&) = delete;
+    DeviceBuffer& operator=(const DeviceBuffer&) = delete;
+    void* get() const { return p_; }
+    void upload(const void* h, size_t bytes) { check(p3g_memcpy_h2d(ctx_, p_, h, bytes, nullptr)); }
+    void download(void* h, size_t bytes) const { check(p3g_memcpy_d2h(ctx_, h, p_, bytes, nullptr)); }
+
+   private:
+    p3g_ctx* ctx_;
+    void* p_ = nullptr;
+};
+
+// Canonical words of a field vector (u32 for BabyBear, u64 for Goldilocks).
+template <class F>
+inline std::vector<unsigned char> to_words(const std::vector<F>& v) {
+    constexpr size_t E = sizeof(F) == 4 ? 4 : 8;
+    std::vector<unsigned char> out(v.size() * E);
+    for (size_t i = 0; i < v.size(); ++i) {
+        const uint64_t c = canonical(v[i]);
+        std::memcpy(out.data() + i * E, &c, E);  // little-endian low bytes
+    }
+    return out;
+}
+template <class F>
+inline std::vector<F> from_words(const unsigned char* p, size_t n) {
+    constexpr size_t E = sizeof(F) == 4 ? 4 : 8;
+    std::vector<F> out;
+    out.reserve(n);
+    for (size_t i = 0; i < n; ++i) {
+        uint64_t c = 0;
+        std::memcpy(&c, p + i * E, E);
+        out.push_back(from_canonical<F>(c));
+    }
+    return out;
+}
+
+// Host copy of every digest layer of a device tree, in the reference's
+// vector-of-layers shape (layer 0 = leaf digests, last = cap).
+template <class Dg>
+std::vector<std::vector<Dg>> download_layers(p3g_ctx* ctx, const p3g_tree* tree) {
+    using W = std::decay_t<decltype(std::declval<Dg&>()[0])>;
+    uint32_t nl = 0, dig = 0;
+    uint64_t sizes[64];
+    check(p3g_tree_info(tree, &nl, sizes, &dig));
+    if (dig != std::tuple_size<Dg>::value) throw std::invalid_argument("digest length mismatch");
+    constexpr size_t E = sizeof(W) == 4 ? 4 : 8;
+    std::vector<std::vector<Dg>> layers(nl);
+    for (uint32_t l = 0; l < nl; ++l) {
+        const void* dp = nullptr;
+        check(p3g_tree_layer_ptr(tree, l, &dp));
+        std::vector<unsigned char> raw(sizes[l] * dig * E);
+        check(p3g_memcpy_d2h(ctx, raw.data(), dp, raw.size(), nullptr));
+        auto flat = from_words<W>(raw.data(), sizes[l] * dig);
+        layers[l].resize(sizes[l]);
+        for (uint64_t i = 0; i < sizes[l]; ++i)
+            for (uint32_t e = 0; e < dig; ++e) layers[l][i][e] = flat[i * dig + e];
+    }
+    return layers;
+}
+
+inline size_t log2_strict(size_t n) {
+    if (n == 0 || (n & (n - 1))) throw std::invalid_argument("log2_strict_usize: value must be a non-zero power of 2");
+    size_t k = 0;
+    while ((size_t(1) << k) < n) ++k;
+    return k;
+}
+
+// ----------------------------------------------------------------- Dft
+// Radix2Dit-compatible; coset_lde_batch runs on the GPU (natural row order,
+// as radix2_dit.hpp:221-233 returns it).
+template <class Base>
+struct GpuDft : Base {
+    using Base::Base;
+    GpuDft() = default;
+    explicit GpuDft(Base b) : Base(std::move(b)) {}
+
+    template <class Mat, class F>
+    Mat coset_lde_batch(Mat mat, size_t added_bits, const F& shift) {
+        const size_t h = mat.height(), w = mat.width();
+        if (h == 0 || w == 0) return Base::coset_lde_batch(std::move(mat), added_bits, shift);
+        const size_t log_h = log2_strict(h);
+        constexpr size_t E = sizeof(F) == 4 ? 4 : 8;
+        const size_t H = h << added_bits;
+        auto words = to_words(mat.values);
+        DeviceBuffer din(words.size()), dout(H * w * E);
+        din.upload(words.data(), words.size());
+        check(p3g_coset_lde(Context::get().handle(), field_id<F>(), din.get(), uint32_t(log_h), uint32_t(w),
+                            uint32_t(added_bits), canonical(shift), 0, dout.get(), nullptr));
+        std::vector<unsigned char> out(H * w * E);
+        dout.download(out.data(), out.size());
+        return Mat(from_words<F>(out.data(), H * w), w);
+    }
+};
+
+// ----------------------------------------------------------------- flat MMCS
+// p3_merkle::MerkleTreeMmcs-compatible; commit_matrix runs on the GPU and
+// fills the reference's ProverData (flat_data, height, width, tree layers).
+template <class Base>
+struct GpuInputMmcs : Base {
+    using Base::Base;
+    explicit GpuInputMmcs(Base b) : Base(std::move(b)) {}
+    using typename Base::Commitment;
+    using typename Base::Digest;
+    using typename Base::ProverData;
+
+    template <class InputF>
+    std::pair<Commitment, ProverData> commit_matrix(const std::vector<InputF>& data, size_t width) const {
+        if (width == 0 || data.size() % width != 0) throw std::invalid_argument("commit_matrix: bad dimensions");
+        const size_t height = data.size() / width;
+        if (height == 0) throw std::invalid_argument("commit_matrix: empty matrix");
+        auto words = to_words(data);
+        DeviceBuffer d(words.size());
+        d.upload(words.data(), words.size());
+        p3g_ctx* ctx = Context::get().handle();
+        p3g_tree* tree = nullptr;
+        check(p3g_commit_matrix(ctx, field_id<InputF>(), d.get(), height, uint32_t(width), &tree, nullptr, nullptr));
+        ProverData pd;
+        pd.flat_data = data;
+        pd.height = height;
+        pd.width = width;
+        pd.tree = download_layers<Digest>(ctx, tree);
+        check(p3g_tree_free(ctx, tree, nullptr));
+        Commitment c = {pd.tree.back()[0]};
+        return {std::move(c), std::move(pd)};
+    }
+
+};
+
+// ----------------------------------------------------------------- mixed-height MMCS
+// p3_merkle_tree::MerkleTreeMmcs-compatible; commit runs on the GPU and
+// returns the reference's MerkleCap and MerkleTree (leaves + digest layers).
+template <class Base>
+struct GpuMerkleTreeMmcs : Base {
+    using typename Base::Commitment;
+    using typename Base::ProverData;
+
+    template <class Hasher, class Compressor>
+    GpuMerkleTreeMmcs(Hasher h, Compressor c, size_t cap_height = 0)
+        : Base(std::move(h), std::move(c), cap_height), cap_height_(cap_height) {}
+
+    template <class Mat>
+    std::pair<Commitment, ProverData> commit(std::vector<Mat> matrices) {
+        using F = std::decay_t<decltype(matrices[0].values[0])>;
+        constexpr size_t E = sizeof(F) == 4 ? 4 : 8;
+        if (matrices.empty()) throw std::invalid_argument("need at least one matrix");
+        std::vector<std::unique_ptr<DeviceBuffer>> bufs;
+        std::vector<p3g_matrix> descs;
+        for (const auto& m : matrices) {
+            auto words = to_words(m.values);
+            bufs.emplace_back(new DeviceBuffer(std::max<size_t>(words.size(), E)));
+            if (!words.empty()) bufs.back()->upload(words.data(), words.size());
+            descs.push_back(p3g_matrix{bufs.back()->get(), uint64_t(m.height()), uint32_t(m.width()), 0});
+        }
+        p3g_ctx* ctx = Context::get().handle();
+        p3g_tree* tree = nullptr;
+        check(p3g_mmcs_commit(ctx, field_id<F>(), descs.data(), descs.size(), uint32_t(cap_height_), &tree, nullptr,
+                              nullptr));
+        ProverData pd;
+        using Layer = std::decay_t<decltype(pd.digest_layers[0])>;
+        using Dg = typename Layer::value_type;
+        pd.digest_layers = download_layers<Dg>(ctx, tree);
+        check(p3g_tree_free(ctx, tree, nullptr));
+        pd.leaves = std::move(matrices);
+        Commitment cap(pd.digest_layers.back());
+        return {std::move(cap), std::move(pd)};
+    }
+
+   private:
+    size_t cap_height_;
+};
+
+// ----------------------------------------------------------------- fold
+// TwoAdicFriFolding<Val, Challenge>::fold_matrix (fri_folding.hpp:200) on the
+// GPU for Val = BabyBear and Challenge = BabyBear4 (or BabyBear, embedded).
+template <class Val, class Challenge>
+std::vector<Challenge> gpu_fold_matrix(size_t log_height, size_t log_arity, const Challenge& beta,
+                                       const std::vector<Challenge>& current) {
+    static_assert(sizeof(Val) == 4, "fold runs over BabyBear");
+    const size_t arity = size_t(1) << log_arity;
+    if (current.size() % arity != 0)
+        throw std::invalid_argument("fold_matrix: current.size() not divisible by arity");
+    if (current.size() != (size_t(1) << log_height))
+        throw std::invalid_argument("fold_matrix: current.size() must be 2^log_height");
+    constexpr bool EXT = sizeof(Challenge) == 16;
+    auto coeff = [](const Challenge& c, int k) -> uint32_t {
+        if constexpr (EXT) return c[k].value();
+        else return k == 0 ? c.value() : 0u;
+    };
+    std::vector<uint32_t> in(current.size() * 4);
+    for (size_t i = 0; i < current.size(); ++i)
+        for (int k = 0; k < 4; ++k) in[i * 4 + k] = coeff(current[i], k);
+    const uint32_t b[4] = {coeff(beta, 0), coeff(beta, 1), coeff(beta, 2), coeff(beta, 3)};
+    const size_t n = current.size() / arity;
+    DeviceBuffer din(in.size() * 4), dout(n * 16);
+    din.upload(in.data(), in.size() * 4);
+    check(p3g_fold_matrix_bb4(Context::get().handle(), din.get(), uint32_t(log_height), uint32_t(log_arity), b,
+                              dout.get(), nullptr));
+    std::vector<uint32_t> out(n * 4);
+    dout.download(out.data(), out.size() * 4);
+    std::vector<Challenge> res(n);
+    for (size_t i = 0; i < n; ++i) {
+        if constexpr (EXT) {
+            for (int k = 0; k < 4; ++k) res[i][k] = Val(out[i * 4 + k]);
+        } else {
+            res[i] = Challenge(out[i * 4]);
+        }
+    }
+    return res;
+}
+
+}  // namespace p3g

@@ -30,3 +30,15 @@ def gpu_ctx():
     ctx.set_default_poseidon2()
     yield ctx
     ctx.close()
+
+
+def compile_cpp(src: str, out: str, extra=()):
+    """g++ -std=c++17 of a test program against include/ and the built library;
+    returns (returncode, compiler output)."""
+    import subprocess
+    import p3g_gb300 as P
+    libdir = os.path.dirname(P.LIB_PATH)
+    cmd = ["g++", "-std=c++17", "-O2", "-Wall", "-Wextra", "-I", os.path.join(REPO, "include"), *extra,
+           os.path.join(REPO, "tests", "cpp", src), "-L", libdir, "-lp3g_gb300", f"-Wl,-rpath,{libdir}", "-o", out]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    return r.returncode, r.stdout + r.stderr

@@ -1,0 +1,147 @@
+// adapters_reference.cpp -- the reference's own prover types with the GPU
+// adapters swapped in, checked against the same types without them.
+//
+// Built against the reference's unmodified headers (dloghin/plonky3-gpu,
+// src/include) and libp3g_gb300.so; the CPU test suite compiles and links it
+// to show that the adapters drop into TwoAdicFriPcs, MerkleTreeMmcs and
+// TwoAdicFriFolding unchanged.  Run on a machine with a GPU it prints one
+// line per check and exits non-zero on any mismatch:
+//   1. TwoAdicFriPcs<BB, BB4, GpuDft<Radix2Dit>, GpuInputMmcs<flat MMCS>, ...>::commit
+//      against the stock Pcs (same commitment);
+//   2. GpuMerkleTreeMmcs<mixed-height MMCS>::commit against the stock one (all
+//      digest layers), then the stock open_batch / verify_batch on the GPU tree;
+//   3. gpu_fold_matrix against TwoAdicFriFolding<BB, BB4>::fold_matrix.
+
+#include "baby_bear.hpp"
+#include "extension_field.hpp"
+#include "dense_matrix.hpp"
+#include "radix2_dit.hpp"
+#include "util.hpp"
+#include "poseidon2_cuda.hpp"
+#include "padding_free_sponge.hpp"
+#include "truncated_permutation.hpp"
+#include "merkle_tree_mmcs.hpp"
+#include "fri_merkle_tree_mmcs.hpp"
+#include "fri_extension_mmcs.hpp"
+#include "fri_folding.hpp"
+#include "fri_params.hpp"
+#include "two_adic_fri_pcs.hpp"
+
+#include "p3g_adapters.hpp"
+
+#include <cstdio>
+#include <random>
+
+using namespace p3_field;
+using p3_matrix::RowMajorMatrix;
+using BB = BabyBear;
+using Pos = poseidon2::Poseidon2Cuda<BB, 16, 8, 13, 7>;
+
+static Pos make_pos() {
+    Pos p;
+    std::mt19937 rng(0xdeadbeef);
+    for (size_t r = 0; r < 4; ++r)
+        for (size_t i = 0; i < 16; ++i) {
+            p.initial_external_constants[r][i] = BB(uint32_t(rng() % BB::PRIME));
+            p.terminal_external_constants[r][i] = BB(uint32_t(rng() % BB::PRIME));
+        }
+    for (size_t r = 0; r < 13; ++r) p.internal_constants[r] = BB(uint32_t(rng() % BB::PRIME));
+    return p;
+}
+
+struct Wrap {
+    Pos pos;
+    void permute_mut(std::array<BB, 16>& s) const { pos.permute(s.data()); }
+};
+using Sponge = p3_symmetric::PaddingFreeSponge<Wrap, BB, 16, 8, 8>;
+using Trunc = p3_symmetric::TruncatedPermutation<Wrap, BB, 2, 8, 16>;
+using Flat = p3_merkle::MerkleTreeMmcs<BB, BB, Sponge, Trunc, 2, 8>;
+using Mixed = p3_merkle_tree::MerkleTreeMmcs<BB, BB, Sponge, Trunc, 8>;
+using EFMmcs = p3_merkle::ExtensionMmcs<BB, BabyBear4, Flat>;
+
+static RowMajorMatrix<BB> rand_matrix(size_t h, size_t w, uint32_t seed) {
+    std::mt19937 rng(seed);
+    std::vector<BB> v(h * w);
+    for (auto& e : v) e = BB(uint32_t(rng() % BB::PRIME));
+    return RowMajorMatrix<BB>(std::move(v), w);
+}
+
+static int report(const char* what, bool ok) {
+    std::printf("%s %s\n", ok ? "ok  " : "FAIL", what);
+    return ok ? 0 : 1;
+}
+
+int main() {
+    int fails = 0;
+    const Pos pos = make_pos();
+    p3g::Context::get().set_poseidon2(pos.initial_external_constants, pos.terminal_external_constants,
+                                      pos.internal_constants, 7);
+    auto flat = [&] { return Flat(Sponge(Wrap{pos}), Trunc(Wrap{pos})); };
+    const std::vector<std::pair<size_t, size_t>> shapes = {{10, 7}, {8, 3}, {10, 2}, {6, 5}};
+
+    // 1. PCS commit
+    {
+        using Cpu = p3_fri::TwoAdicFriPcs<BB, BabyBear4, p3_dft::Radix2Dit<BB>, Flat, EFMmcs>;
+        using Gpu = p3_fri::TwoAdicFriPcs<BB, BabyBear4, p3g::GpuDft<p3_dft::Radix2Dit<BB>>, p3g::GpuInputMmcs<Flat>,
+                                          EFMmcs>;
+        p3_fri::FriParameters<EFMmcs> fri_a{1, 0, 1, 10, 0, 8, EFMmcs(flat())};
+        p3_fri::FriParameters<EFMmcs> fri_b{1, 0, 1, 10, 0, 8, EFMmcs(flat())};
+        Cpu cpu(p3_dft::Radix2Dit<BB>(), flat(), std::move(fri_a));
+        Gpu gpu(p3g::GpuDft<p3_dft::Radix2Dit<BB>>(), p3g::GpuInputMmcs<Flat>(flat()), std::move(fri_b));
+        auto evals = [&](auto& pcs) {
+            std::vector<std::pair<typename std::decay_t<decltype(pcs)>::Domain, RowMajorMatrix<BB>>> ev;
+            for (size_t i = 0; i < shapes.size(); ++i) {
+                typename std::decay_t<decltype(pcs)>::Domain d;
+                d.log_n = shapes[i].first;
+                d.shift = BB::one_val();
+                ev.push_back({d, rand_matrix(size_t(1) << shapes[i].first, shapes[i].second, 100 + uint32_t(i))});
+            }
+            return ev;
+        };
+        auto [c_cpu, pd_cpu] = cpu.commit(evals(cpu));
+        auto [c_gpu, pd_gpu] = gpu.commit(evals(gpu));
+        fails += report("TwoAdicFriPcs::commit with GpuDft + GpuInputMmcs", c_cpu == c_gpu);
+    }
+
+    // 2. mixed-height MMCS commit, then the stock opening and verification
+    {
+        Mixed cpu(Sponge(Wrap{pos}), Trunc(Wrap{pos}), 1);
+        p3g::GpuMerkleTreeMmcs<Mixed> gpu(Sponge(Wrap{pos}), Trunc(Wrap{pos}), 1);
+        auto mats = [&] {
+            std::vector<RowMajorMatrix<BB>> m;
+            for (size_t i = 0; i < shapes.size(); ++i)
+                m.push_back(rand_matrix(size_t(1) << shapes[i].first, shapes[i].second, 200 + uint32_t(i)));
+            return m;
+        };
+        auto [cap_cpu, tree_cpu] = cpu.commit(mats());
+        auto [cap_gpu, tree_gpu] = gpu.commit(mats());
+        fails += report("MerkleTreeMmcs::commit digest layers", tree_cpu.digest_layers == tree_gpu.digest_layers &&
+                                                                    cap_cpu == cap_gpu);
+        bool ok = true;
+        std::vector<p3_matrix::Dimensions> dims;
+        for (const auto& m : tree_gpu.leaves) dims.push_back({m.width(), m.height()});
+        for (size_t index : {size_t(0), size_t(1), size_t(517), size_t(1023)}) {
+            auto opening = gpu.open_batch(index, tree_gpu);
+            ok = ok && cpu.verify_batch(cap_gpu, dims, index, opening);
+        }
+        fails += report("open_batch on the GPU tree verifies", ok);
+    }
+
+    // 3. fold_matrix
+    {
+        std::mt19937 rng(7);
+        auto r = [&] { return BB(uint32_t(rng() % BB::PRIME)); };
+        for (size_t la = 1; la <= 3; ++la) {
+            const size_t log_h = 11;
+            std::vector<BabyBear4> v(size_t(1) << log_h);
+            for (auto& e : v) e = BabyBear4({r(), r(), r(), r()});
+            const BabyBear4 beta({r(), r(), r(), r()});
+            auto want = p3_fri::TwoAdicFriFolding<BB, BabyBear4>::fold_matrix(log_h, la, beta, v);
+            auto got = p3g::gpu_fold_matrix<BB, BabyBear4>(log_h, la, beta, v);
+            fails += report(la == 1 ? "fold_matrix arity 2" : la == 2 ? "fold_matrix arity 4" : "fold_matrix arity 8",
+                            want == got);
+        }
+    }
+    std::printf("%s\n", fails ? "MISMATCH" : "ALL OK");
+    return fails ? 1 : 0;
+}

@@ -1,0 +1,220 @@
+// adapters_standin.cpp -- drives the C++ adapters (p3g_adapters.hpp) with
+// minimal stand-ins for the reference's types, on machines without the
+// reference's headers.  The stand-ins have exactly the members the adapters
+// touch: BabyBear / Goldilocks (value(), as_canonical_u64(), explicit
+// construction from the canonical integer), BabyBear4 (operator[]),
+// RowMajorMatrix (values, width(), height(), (vector, width) constructor),
+// and the MMCS classes' Digest / Commitment / ProverData types.
+//
+//   adapters_standin lde <bb|gl> <in> <out> <log_h> <width> <added_bits> <shift>
+//   adapters_standin commit_matrix <in> <out> <height> <width>
+//   adapters_standin mmcs <bb|gl> <in> <out> <cap_height> <h0> <w0> [<h1> <w1> ...]
+//   adapters_standin fold <in> <out> <log_height> <log_arity>
+//
+// <in> holds canonical little-endian words (u32 BabyBear, u64 Goldilocks;
+// for mmcs the matrices back to back; for fold 4 beta coefficients, then
+// the values); <out> receives the result (for the trees every digest layer
+// from the leaves up).  Poseidon2 is the BabyBear-16 x^7 8+13 permutation
+// with constants from std::mt19937(0xdeadbeef) and the Goldilocks-8 x^7 8+22
+// one from std::mt19937_64(12345), initial and terminal drawn interleaved.
+
+#include "p3g_adapters.hpp"
+
+#include <cstdio>
+#include <cstdlib>
+#include <fstream>
+#include <iterator>
+#include <random>
+#include <string>
+
+namespace standin {
+
+struct BabyBear {
+    static constexpr uint32_t PRIME = 0x78000001u;
+    uint32_t v = 0;
+    BabyBear() = default;
+    explicit BabyBear(uint32_t x) : v(x % PRIME) {}
+    uint32_t value() const { return v; }
+    bool operator==(const BabyBear& o) const { return v == o.v; }
+};
+struct Goldilocks {
+    static constexpr uint64_t PRIME = 0xFFFFFFFF00000001ull;
+    uint64_t v = 0;
+    Goldilocks() = default;
+    explicit Goldilocks(uint64_t x) : v(x) {}
+    uint64_t as_canonical_u64() const { return v >= PRIME ? v - PRIME : v; }
+    bool operator==(const Goldilocks& o) const { return as_canonical_u64() == o.as_canonical_u64(); }
+};
+struct BabyBear4 {
+    std::array<BabyBear, 4> coeffs{};
+    BabyBear& operator[](size_t i) { return coeffs[i]; }
+    const BabyBear& operator[](size_t i) const { return coeffs[i]; }
+};
+
+template <class F>
+struct RowMajorMatrix {
+    std::vector<F> values;
+    size_t width_;
+    RowMajorMatrix(std::vector<F> v, size_t w) : values(std::move(v)), width_(w) {}
+    size_t width() const { return width_; }
+    size_t height() const { return width_ ? values.size() / width_ : 0; }
+};
+
+struct Radix2Dit {  // only the empty-matrix case reaches the base class
+    template <class M, class F>
+    M coset_lde_batch(M m, size_t, const F&) {
+        return m;
+    }
+};
+
+template <class F, size_t N>
+struct FlatMmcs {
+    using Digest = std::array<F, N>;
+    using Commitment = std::vector<Digest>;
+    struct ProverData {
+        std::vector<F> flat_data;
+        size_t height = 0, width = 0;
+        std::vector<std::vector<Digest>> tree;
+    };
+};
+
+template <class F, size_t N>
+struct MixedMmcs {
+    using Digest = std::array<F, N>;
+    struct Commitment {
+        std::vector<Digest> cap;
+        explicit Commitment(std::vector<Digest> c) : cap(std::move(c)) {}
+    };
+    struct ProverData {
+        std::vector<RowMajorMatrix<F>> leaves;
+        std::vector<std::vector<Digest>> digest_layers;
+    };
+    struct Sponge {};
+    struct Trunc {};
+    MixedMmcs(Sponge, Trunc, size_t) {}
+};
+
+}  // namespace standin
+
+using namespace standin;
+
+static std::vector<unsigned char> read_file(const char* path) {
+    std::ifstream f(path, std::ios::binary);
+    return std::vector<unsigned char>(std::istreambuf_iterator<char>(f), {});
+}
+static void write_file(const char* path, const std::vector<unsigned char>& b) {
+    std::ofstream f(path, std::ios::binary);
+    f.write(reinterpret_cast<const char*>(b.data()), std::streamsize(b.size()));
+}
+template <class F, size_t N>
+static void append_layers(std::vector<unsigned char>& out, const std::vector<std::vector<std::array<F, N>>>& l) {
+    for (const auto& layer : l)
+        for (const auto& d : layer) {
+            auto w = p3g::to_words(std::vector<F>(d.begin(), d.end()));
+            out.insert(out.end(), w.begin(), w.end());
+        }
+}
+
+static void set_constants() {
+    std::mt19937 r32(0xdeadbeef);
+    std::vector<std::array<BabyBear, 16>> bi(4), bt(4);
+    for (size_t r = 0; r < 4; ++r)
+        for (size_t i = 0; i < 16; ++i) {
+            bi[r][i] = BabyBear(uint32_t(r32() % BabyBear::PRIME));
+            bt[r][i] = BabyBear(uint32_t(r32() % BabyBear::PRIME));
+        }
+    std::vector<BabyBear> bin;
+    for (size_t r = 0; r < 13; ++r) bin.push_back(BabyBear(uint32_t(r32() % BabyBear::PRIME)));
+    p3g::Context::get().set_poseidon2(bi, bt, bin, 7);
+
+    std::mt19937_64 r64(12345);
+    std::vector<std::array<Goldilocks, 8>> gi(4), gt(4);
+    for (size_t r = 0; r < 4; ++r)
+        for (size_t i = 0; i < 8; ++i) {
+            gi[r][i] = Goldilocks(r64() % Goldilocks::PRIME);
+            gt[r][i] = Goldilocks(r64() % Goldilocks::PRIME);
+        }
+    std::vector<Goldilocks> gin;
+    for (size_t r = 0; r < 22; ++r) gin.push_back(Goldilocks(r64() % Goldilocks::PRIME));
+    p3g::Context::get().set_poseidon2(gi, gt, gin, 7);
+}
+
+template <class F>
+static int run_lde(char** a) {
+    auto in = read_file(a[3]);
+    const size_t log_h = std::strtoul(a[5], nullptr, 0), w = std::strtoul(a[6], nullptr, 0);
+    const size_t bits = std::strtoul(a[7], nullptr, 0);
+    const uint64_t shift = std::strtoull(a[8], nullptr, 0);
+    RowMajorMatrix<F> m(p3g::from_words<F>(in.data(), (size_t(1) << log_h) * w), w);
+    p3g::GpuDft<Radix2Dit> dft;
+    auto out = dft.coset_lde_batch(std::move(m), bits, F(shift));
+    write_file(a[4], p3g::to_words(out.values));
+    return 0;
+}
+
+template <class F, size_t N>
+static int run_mmcs(int argc, char** a) {
+    auto in = read_file(a[3]);
+    const size_t cap = std::strtoul(a[5], nullptr, 0);
+    constexpr size_t E = sizeof(F) == 4 ? 4 : 8;
+    std::vector<RowMajorMatrix<F>> mats;
+    size_t off = 0;
+    for (int i = 6; i + 1 < argc; i += 2) {
+        const size_t h = std::strtoul(a[i], nullptr, 0), w = std::strtoul(a[i + 1], nullptr, 0);
+        mats.emplace_back(p3g::from_words<F>(in.data() + off, h * w), w);
+        off += h * w * E;
+    }
+    using M = MixedMmcs<F, N>;
+    p3g::GpuMerkleTreeMmcs<M> mmcs(typename M::Sponge{}, typename M::Trunc{}, cap);
+    auto [commitment, pd] = mmcs.commit(std::move(mats));
+    std::vector<unsigned char> out;
+    append_layers(out, pd.digest_layers);
+    if (commitment.cap != pd.digest_layers.back()) return 3;
+    write_file(a[4], out);
+    return 0;
+}
+
+int main(int argc, char** argv) {
+    if (argc < 4) return 2;
+    const std::string cmd = argv[1];
+    try {
+        set_constants();
+        if (cmd == "lde") return std::string(argv[2]) == "bb" ? run_lde<BabyBear>(argv) : run_lde<Goldilocks>(argv);
+        if (cmd == "mmcs")
+            return std::string(argv[2]) == "bb" ? run_mmcs<BabyBear, 8>(argc, argv) : run_mmcs<Goldilocks, 4>(argc, argv);
+        if (cmd == "commit_matrix") {
+            auto in = read_file(argv[2]);
+            const size_t h = std::strtoul(argv[4], nullptr, 0), w = std::strtoul(argv[5], nullptr, 0);
+            p3g::GpuInputMmcs<FlatMmcs<BabyBear, 8>> mmcs{FlatMmcs<BabyBear, 8>{}};
+            auto [commitment, pd] = mmcs.commit_matrix(p3g::from_words<BabyBear>(in.data(), h * w), w);
+            if (pd.height != h || pd.width != w || commitment.size() != 1) return 3;
+            std::vector<unsigned char> out;
+            append_layers(out, pd.tree);
+            write_file(argv[3], out);
+            return 0;
+        }
+        if (cmd == "fold") {
+            auto in = read_file(argv[2]);
+            const size_t log_h = std::strtoul(argv[4], nullptr, 0), la = std::strtoul(argv[5], nullptr, 0);
+            auto words = p3g::from_words<BabyBear>(in.data(), 4 + (size_t(4) << log_h));
+            BabyBear4 beta;
+            for (int k = 0; k < 4; ++k) beta[k] = words[k];
+            std::vector<BabyBear4> cur(size_t(1) << log_h);
+            for (size_t i = 0; i < cur.size(); ++i)
+                for (int k = 0; k < 4; ++k) cur[i][k] = words[4 + 4 * i + k];
+            auto res = p3g::gpu_fold_matrix<BabyBear, BabyBear4>(log_h, la, beta, cur);
+            std::vector<BabyBear> flat;
+            for (const auto& e : res)
+                for (int k = 0; k < 4; ++k) flat.push_back(e[k]);
+            write_file(argv[3], p3g::to_words(flat));
+            return 0;
+        }
+    } catch (const std::invalid_argument& e) {
+        std::fprintf(stderr, "invalid_argument: %s\n", e.what());
+        return 4;
+    } catch (const std::exception& e) {
+        std::fprintf(stderr, "error: %s\n", e.what());
+        return 5;
+    }
+    return 2;
+}

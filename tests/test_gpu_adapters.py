@@ -1,0 +1,110 @@
+"""The C++ adapters (include/p3g_adapters.hpp) on the GPU, driven by
+tests/cpp/adapters_standin.cpp with stand-ins of the reference's types, against
+the oracle: GpuDft::coset_lde_batch (natural order), GpuInputMmcs::commit_matrix
+(every layer, odd heights), GpuMerkleTreeMmcs::commit (mixed heights, caps,
+both fields) and gpu_fold_matrix.  Bit-exact."""
+import subprocess
+
+import numpy as np
+import pytest
+
+import oracle as O
+from conftest import compile_cpp
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def prog(tmp_path_factory):
+    out = str(tmp_path_factory.mktemp("adapters") / "standin")
+    rc, log = compile_cpp("adapters_standin.cpp", out)
+    assert rc == 0, log
+    return out
+
+
+def _run(prog, tmp_path, cmd, field, rest, data: np.ndarray):
+    """adapters_standin <cmd> [<field>] <in> <out> <rest...>"""
+    fin, fout = str(tmp_path / "in.bin"), str(tmp_path / "out.bin")
+    data.tofile(fin)
+    argv = [prog, cmd] + ([field] if field else []) + [fin, fout] + [str(x) for x in rest]
+    r = subprocess.run(argv, capture_output=True, text=True, timeout=120)
+    return r.returncode, r.stderr, fout
+
+
+def _layers(raw: np.ndarray, sizes, digest):
+    out, off = [], 0
+    for s in sizes:
+        out.append(raw[off:off + s * digest].reshape(s, digest))
+        off += s * digest
+    assert off == raw.size
+    return out
+
+
+@pytest.mark.parametrize("field,log_h,w,bits,shift", [
+    ("bb", 6, 5, 1, 31), ("bb", 11, 3, 2, 31), ("bb", 14, 9, 1, 31), ("gl", 7, 4, 2, 7), ("gl", 12, 3, 1, 7)])
+def test_gpu_dft_coset_lde_batch(prog, tmp_path, field, log_h, w, bits, shift):
+    rng = np.random.default_rng(log_h * 31 + w)
+    if field == "bb":
+        t = rng.integers(0, O.BB_P, size=(1 << log_h, w), dtype=np.uint32)
+        want = O.bb_coset_lde(t, bits, shift, bitrev=False)
+    else:
+        t = rng.integers(0, O.GL_P, size=(1 << log_h, w), dtype=np.uint64)
+        want = O.gl_coset_lde(t, bits, shift, bitrev=False)
+    rc, err, fout = _run(prog, tmp_path, "lde", field, [log_h, w, bits, shift], t)
+    assert rc == 0, err
+    got = np.fromfile(fout, dtype=t.dtype).reshape(want.shape)
+    assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("h,w", [(1, 8), (37, 8), (256, 16), (1000, 3)])
+def test_gpu_input_mmcs_commit_matrix(prog, tmp_path, h, w):
+    rng = np.random.default_rng(h + w)
+    m = rng.integers(0, O.BB_P, size=(h, w), dtype=np.uint32)
+    rc, err, fout = _run(prog, tmp_path, "commit_matrix", None, [h, w], m)
+    assert rc == 0, err
+    want = O.commit_matrix(O.bb16_params(), m)
+    got = _layers(np.fromfile(fout, dtype=np.uint32), [l.shape[0] for l in want], 8)
+    for g, wl in zip(got, want):
+        assert np.array_equal(g, wl)
+
+
+@pytest.mark.parametrize("field,cap,shapes", [
+    ("bb", 0, [(1024, 7), (256, 3), (1024, 2), (64, 5)]),
+    ("bb", 2, [(512, 16), (512, 1), (8, 4)]),
+    ("gl", 1, [(256, 5), (128, 3), (256, 1)]),
+])
+def test_gpu_merkle_tree_mmcs_commit(prog, tmp_path, field, cap, shapes):
+    rng = np.random.default_rng(len(shapes) * 7 + cap)
+    if field == "bb":
+        mats = [rng.integers(0, O.BB_P, size=s, dtype=np.uint32) for s in shapes]
+        params, digest = O.bb16_params(), 8
+    else:
+        mats = [rng.integers(0, O.GL_P, size=s, dtype=np.uint64) for s in shapes]
+        params, digest = O.gl8_params(), 4
+    flat = np.concatenate([m.reshape(-1) for m in mats])
+    rest = [cap] + [x for s in shapes for x in s]
+    rc, err, fout = _run(prog, tmp_path, "mmcs", field, rest, flat)
+    assert rc == 0, err
+    want = O.mmcs_commit(params, mats, cap)
+    got = _layers(np.fromfile(fout, dtype=flat.dtype), [l.shape[0] for l in want], digest)
+    for g, wl in zip(got, want):
+        assert np.array_equal(g, wl)
+
+
+@pytest.mark.parametrize("log_arity", [1, 2, 3])
+def test_gpu_fold_matrix(prog, tmp_path, log_arity):
+    rng = np.random.default_rng(50 + log_arity)
+    log_h = 11
+    v = rng.integers(0, O.BB_P, size=(1 << log_h, 4), dtype=np.uint32)
+    beta = rng.integers(0, O.BB_P, size=4, dtype=np.uint32)
+    rc, err, fout = _run(prog, tmp_path, "fold", None, [log_h, log_arity],
+                         np.concatenate([beta, v.reshape(-1)]))
+    assert rc == 0, err
+    got = np.fromfile(fout, dtype=np.uint32).reshape(-1, 4)
+    assert np.array_equal(got, O.fold_matrix_bb4(v, log_h, log_arity, beta))
+
+
+def test_adapter_reports_bad_dimensions_as_invalid_argument(prog, tmp_path):
+    rc, err, _ = _run(prog, tmp_path, "commit_matrix", None, [0, 0], np.zeros(0, np.uint32))
+    assert rc == 4, err
+    assert "bad dimensions" in err

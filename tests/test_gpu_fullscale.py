@@ -2,7 +2,8 @@
 Merkle opening the GPU tree produces verifies under the oracle's restatement
 of MerkleTreeMmcs::verify_batch (merkle_tree_mmcs.hpp:168-254) against the
 GPU's root, and the LDEs of the smaller traces match the oracle element by
-element (the large ones are covered by the 2^20 x 256 LDE test)."""
+element (the large ones are covered by the 2^20 x 256 LDE test); the Goldilocks
+2^18 x 128 workload is compared whole."""
 import os
 
 import numpy as np
@@ -68,3 +69,22 @@ def test_config3_batched_plan_openings_verify(gpu_ctx):
     plan.destroy()
     for b in bufs:
         b.free()
+
+
+def test_config2_goldilocks_full_size_matches_oracle(gpu_ctx):
+    """Goldilocks 2^18 x 128, log_blowup 2, shift 7: the full 2^20 x 128 LDE and
+    every digest layer of the Poseidon2-8 tree, element for element."""
+    t = np.random.default_rng(22).integers(0, O.GL_P, size=(1 << 18, 128), dtype=np.uint64)
+    d = gpu_ctx.to_device(t)
+    tree = gpu_ctx.commit_traces_device(P.GOLDILOCKS, [(d.ptr, 18, 128, 2, 7)], 0)
+    lde = O.gl_coset_lde(t, 2, 7, True, nthreads=NT)
+    got = np.empty_like(lde)
+    P.check(P.load().p3g_memcpy_d2h(gpu_ctx.handle, got.ctypes.data, tree.leaf_ptr(0), got.nbytes, None))
+    assert np.array_equal(got, lde)
+    want = O.mmcs_commit(O.gl8_params(), [lde], 0, nthreads=NT)
+    layers = tree.layers()
+    assert len(layers) == len(want)
+    for g, w in zip(layers, want):
+        assert np.array_equal(g, w)
+    tree.free()
+    d.free()
