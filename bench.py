@@ -55,6 +55,22 @@ def dist_info():
     return ws, rank, local
 
 
+def job_throughput(units: float, ms: float, device=None):
+    """Whole-job throughput of independent replicas: the units every rank
+    processed divided by the slowest rank's time.  Returns (units/s, max ms).
+    Collective only over the already-initialised process group (NCCL on the
+    GPU, gloo in the CPU tests); one rank returns its own figures."""
+    import torch
+    import torch.distributed as dist
+    if dist.is_available() and dist.is_initialized() and dist.get_world_size() > 1:
+        t = torch.tensor([ms], dtype=torch.float64, device=device)
+        u = torch.tensor([units], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dist.all_reduce(u, op=dist.ReduceOp.SUM)
+        ms, units = float(t.item()), float(u.item())
+    return units / (ms / 1e3), ms
+
+
 class ClockSampler:
     """Samples nvidia-smi clocks/throttle reasons while the timed region runs."""
 
@@ -408,12 +424,8 @@ def run_ours(args):
     launches = P.kernel_launches() - l0
     step_ms = [evs[i].elapsed_time(evs[i + 1]) for i in range(args.steps)]
     total_ms = evs[0].elapsed_time(evs[-1])
-    if ws > 1:
-        t = torch.tensor([total_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
+    value, total_ms = job_throughput(float(elems) * args.steps, total_ms, dev)
     ms_per_step = total_ms / args.steps
-    value = ws * elems / (ms_per_step / 1e3)
 
     # ---- stage breakdown: the LDE alone (roofline) -- same stream, CUDA events
     d_lde = ctx.alloc(elems * 4, sptr)
@@ -443,11 +455,23 @@ def run_ours(args):
         dt = (time.perf_counter() - t0) * 1e3
         if i >= args.warmup:
             e2e_ms.append(dt)
-    e2e_mean = statistics.mean(e2e_ms)
-    if ws > 1:
-        t = torch.tensor([e2e_mean], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_mean = float(t.item())
+    e2e_value, e2e_mean = job_throughput(float(elems), statistics.mean(e2e_ms), dev)
+
+    # ---- permutation ceiling: the same Poseidon2-16 on 2^22 register-resident
+    # states (p3g_poseidon2_permute), no sponge or tree around it
+    n_states = 1 << 22
+    d_states = ctx.to_device(rng.integers(0, BB_P, size=(n_states, 16), dtype=np.uint32))
+    perm_once = lambda: P.check(P.load().p3g_poseidon2_permute(ctx.handle, P.BABYBEAR, d_states.ptr, n_states, sptr))
+    for _ in range(2):
+        perm_once()
+    torch.cuda.synchronize(dev)
+    e0.record(stream)
+    for _ in range(reps):
+        perm_once()
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    perm_peak = n_states / (e0.elapsed_time(e1) / reps / 1e3)
+    d_states.free()
 
     hbm, src = peaks()
     lde_bytes = 4 * WIDTH * (h + H)
@@ -456,7 +480,7 @@ def run_ours(args):
     tpath = os.path.join(REPO, "profiles", "traffic.json")
     if os.path.exists(tpath):
         with open(tpath) as f:
-            traffic = json.load(f).get("lde_bb_2p20x256_b1_bytes")
+            traffic = json.load(f).get(f"lde_bb_2p{LOG_H}x{WIDTH}_b{LOG_B}_bytes")
     perms = H * ((WIDTH + 7) // 8) + (H - 1)
     hash_ms = ms_per_step - lde_ms
     result = {
@@ -465,12 +489,15 @@ def run_ours(args):
         "p50_ms": float(np.percentile(step_ms, 50)), "p99_ms": float(np.percentile(step_ms, 99)),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32 (BabyBear)",
         "data": "synthetic",
-        "config": {"workload": "plain single-trace BabyBear commit: 2^20 x 256 trace, log_blowup 1, shift 31, "
-                               "bit-reversed LDE 2^21 x 256, Poseidon2-16 (x^7, 8+13) MMCS, cap_height 0",
+        "config": {"workload": f"plain single-trace BabyBear commit: 2^{LOG_H} x {WIDTH} trace, log_blowup {LOG_B}, "
+                               f"shift {SHIFT}, bit-reversed LDE 2^{LOG_H + LOG_B} x {WIDTH}, Poseidon2-16 "
+                               "(x^7, 8+13) MMCS, cap_height 0",
                    "trace_rows": h, "trace_cols": WIDTH, "lde_rows": H, "field": "BabyBear",
-                   "l2": "inputs larger than L2 (1 GiB trace, 2 GiB LDE); no flush",
+                   "l2": (f"inputs larger than L2 ({h * WIDTH * 4 / 2**20:.0f} MiB trace, "
+                          f"{elems * 4 / 2**20:.0f} MiB LDE); no flush") if h * WIDTH * 4 > 129e6
+                         else "inputs smaller than L2 (profiling case)",
                    "parallelism": f"replicas x{ws}"},
-        "e2e": {"value": ws * elems / (e2e_mean / 1e3), "unit": UNIT,
+        "e2e": {"value": e2e_value, "unit": UNIT,
                 "h2d_bytes_per_step": h * WIDTH * 4, "d2h_bytes_per_step": 32,
                 "p50_ms": float(np.percentile(e2e_ms, 50)), "p99_ms": float(np.percentile(e2e_ms, 99))},
         "gpu_launches": int(launches),
@@ -480,6 +507,12 @@ def run_ours(args):
                      "peak_source": src, "algorithmic_bytes": lde_bytes, "ms": lde_ms},
         "stages": {"lde_ms": lde_ms, "merkle_ms": hash_ms, "perms": perms,
                    "perms_per_s": perms / (hash_ms / 1e3) if hash_ms > 0 else None},
+        "hash_roofline": {"kernel": "Merkle stage (k_hash_groups leaf sponge + k_compress_level)",
+                          "bound": "integer multiply pipe (permutation issue)",
+                          "achieved": perms / (hash_ms / 1e3) if hash_ms > 0 else None, "unit": "perms/s",
+                          "peak": perm_peak,
+                          "peak_source": "isolated Poseidon2-16 permutation throughput, same run",
+                          "frac": perms / (hash_ms / 1e3) / perm_peak if hash_ms > 0 else None},
     }
     if not args.no_goldilocks:
         result["config2"] = run_goldilocks(P, torch, ctx, dev, stream, max(3, args.steps // 2), args.warmup)
