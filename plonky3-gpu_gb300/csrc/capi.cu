@@ -133,6 +133,8 @@ int p3g_ctx_create(int device, p3g_ctx** out) {
         P3G_CUDA(cudaMemcpy(ctx->gl_lo, lo.data(), lo.size() * 8, cudaMemcpyHostToDevice));
         P3G_CUDA(cudaMemcpy(ctx->gl_hi, hi.data(), hi.size() * 8, cudaMemcpyHostToDevice));
     }
+    ctx->bb_dft_tw = p3g::make_dft_tw_bb();
+    ctx->gl_dft_tw = p3g::make_dft_tw_gl();
     *out = ctx.release();
     API_END
 }
@@ -147,6 +149,8 @@ int p3g_ctx_destroy(p3g_ctx* ctx) {
         cudaFree(ctx->bb_hi);
         cudaFree(ctx->gl_lo);
         cudaFree(ctx->gl_hi);
+        cudaFree(ctx->bb_dft_tw);
+        cudaFree(ctx->gl_dft_tw);
         if (ctx->pool) cudaMemPoolDestroy(ctx->pool);
     }
     delete ctx;

@@ -201,6 +201,10 @@ struct FBB {
     // product of two const-form values, result in const form
     static P3G_HD T cmul(T a, T b) { return bb::mmul(a, b); }
     static inline T to_const(uint64_t canonical) { return bb::to_mont(uint32_t(canonical)); }
+    // host: canonical value -> prepared twiddle
+    static inline TW h_tw(uint64_t canonical) {
+        return make_uint2(uint32_t(canonical), bb::shoup_companion(uint32_t(canonical)));
+    }
     static inline uint64_t h_mul(uint64_t a, uint64_t b) { return bb::h_mul(uint32_t(a), uint32_t(b)); }
     static inline uint64_t h_pow(uint64_t a, uint64_t e) { return bb::h_pow(uint32_t(a), e); }
     static inline uint64_t h_inv(uint64_t a) { return bb::h_inv(uint32_t(a)); }
@@ -219,6 +223,7 @@ struct FGL {
     static __device__ __forceinline__ T mulc(T a, T c) { return gl::mul(a, c); }
     static __device__ __forceinline__ T cmul(T a, T b) { return gl::mul(a, b); }
     static inline T to_const(uint64_t canonical) { return canonical; }
+    static inline TW h_tw(uint64_t canonical) { return canonical; }
     static inline uint64_t h_mul(uint64_t a, uint64_t b) { return gl::h_mul(a, b); }
     static inline uint64_t h_pow(uint64_t a, uint64_t e) { return gl::h_pow(a, e); }
     static inline uint64_t h_inv(uint64_t a) { return gl::h_inv(a); }

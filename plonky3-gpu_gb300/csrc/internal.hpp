@@ -91,6 +91,9 @@ struct p3g_ctx {
     uint32_t* bb_hi = nullptr;
     uint64_t* gl_lo = nullptr;
     uint64_t* gl_hi = nullptr;
+    // prepared in-tile DFT twiddles (lde.cuh: build_dft_tw), device
+    void* bb_dft_tw = nullptr;
+    void* gl_dft_tw = nullptr;
     // Poseidon2
     bool has_p2bb = false, has_p2gl = false;
     int bb_rf = 0, bb_rp = 0, bb_d = 0;
@@ -128,6 +131,9 @@ namespace p3g {
 // (implemented in lde.cu, merkle.cu, fold.cu; called by capi.cu)
 void lde_bb(p3g_ctx* ctx, const uint32_t* in, int log_h, int w, int log_b, uint32_t shift,
             int bitrev_out, uint32_t* out, cudaStream_t st);
+// device copies of the prepared DFT twiddle tables (cudaMalloc'd; the context frees them)
+void* make_dft_tw_bb();
+void* make_dft_tw_gl();
 void lde_gl(p3g_ctx* ctx, const uint64_t* in, int log_h, int w, int log_b, uint64_t shift,
             int bitrev_out, uint64_t* out, cudaStream_t st);
 

@@ -55,6 +55,33 @@ struct LdeCfg<FGL> {
 constexpr int LDE_SINGLE_MAX = 10;  // single-kernel LDE up to h = 2^10
 constexpr int LDE_PASS_MAX = 21;    // three-pass LDE up to h = 2^21
 
+// Prepared in-tile DFT twiddles (one table per context and field): for every
+// LOGN in 1..DFT_TW_MAXLOG the N = 2^LOGN powers omega_N^e, e < N, as F::TW;
+// the forward tables first, then the inverse ones.  Kernels copy their
+// LOGN's table into shared memory instead of deriving every entry from the
+// two-level root table (two loads, two products and, for BabyBear, a
+// 64-bit Shoup quotient per entry and CTA).
+constexpr int DFT_TW_MAXLOG = 11;
+constexpr size_t DFT_TW_BLOCK = (size_t(2) << DFT_TW_MAXLOG) - 2;  // sum of 2^L, L = 1..11
+constexpr size_t dft_tw_offset(int logn, bool inv) {
+    return (inv ? DFT_TW_BLOCK : 0) + (size_t(1) << logn) - 2;
+}
+template <class F>
+std::vector<typename F::TW> build_dft_tw() {
+    std::vector<typename F::TW> v(2 * DFT_TW_BLOCK);
+    for (int L = 1; L <= DFT_TW_MAXLOG; ++L) {
+        const uint64_t wf = F::root(unsigned(L)), wi = F::h_inv(wf);
+        uint64_t a = 1, b = 1;
+        for (size_t e = 0; e < (size_t(1) << L); ++e) {
+            v[dft_tw_offset(L, false) + e] = F::h_tw(a);
+            v[dft_tw_offset(L, true) + e] = F::h_tw(b);
+            a = F::h_mul(a, wf);
+            b = F::h_mul(b, wi);
+        }
+    }
+    return v;
+}
+
 // out[i] = scale * base^i, all in const form.
 template <class F>
 __global__ void k_pow_table(typename F::T* out, typename F::T base, typename F::T scale, int n) {
@@ -69,6 +96,19 @@ __global__ void k_pow_table(typename F::T* out, typename F::T base, typename F::
         e >>= 1;
     }
     out[i] = F::cmul(r, scale);
+}
+
+// Prepared coset twists of every coset t < 2^log_b, shared by all CTAs:
+// out[t*N + k] = s[k] * omega_H^(bitrev_b(t) * stride * k)   (N = 2^logn).
+template <class F>
+__global__ void k_pre_table(typename F::TW* out, const typename F::T* s, int logn, int log_b, int logH,
+                            uint64_t stride, RootTab<F> roots) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= (int64_t(1) << (logn + log_b))) return;
+    const int tc = int(i >> logn);
+    const uint64_t k = uint64_t(i) & ((uint64_t(1) << logn) - 1);
+    const uint64_t u = bitrev_dev(unsigned(tc), log_b);
+    out[i] = F::tw_from_const(F::cmul(s[k], roots.omega(logH, u * stride * k)));
 }
 
 // h = 1: the LDE of a constant polynomial is constant.
@@ -202,7 +242,9 @@ struct OutStore {
 template <class F, int LOGN>
 __global__ void __launch_bounds__(Tile<F, LOGN, LdeCfg<F>::C13>::THREADS)
 k_lde_single(const typename F::T* __restrict__ in, typename F::T* __restrict__ out, int w,
-             int log_b, int bitrev_out, const typename F::T* __restrict__ sq, RootTab<F> roots) {
+             int log_b, int bitrev_out, const typename F::T* __restrict__ sq, RootTab<F> roots,
+             const typename F::TW* __restrict__ gtwi, const typename F::TW* __restrict__ gtwf,
+             const typename F::TW* __restrict__ gpre) {
     constexpr int C = LdeCfg<F>::C13;
     using SH = Tile<F, LOGN, C>;
     using T = typename F::T;
@@ -220,8 +262,8 @@ k_lde_single(const typename F::T* __restrict__ in, typename F::T* __restrict__ o
     const int logH = LOGN + log_b;
 
     for (int e = tid; e < N; e += NT) {
-        twi[e] = F::tw_from_const(roots.omega_inv(LOGN, e));
-        twf[e] = F::tw_from_const(roots.omega(LOGN, e));
+        twi[e] = gtwi ? gtwi[e] : F::tw_from_const(roots.omega_inv(LOGN, e));
+        twf[e] = gtwf ? gtwf[e] : F::tw_from_const(roots.omega(LOGN, e));
     }
     __syncthreads();
     {
@@ -231,7 +273,8 @@ k_lde_single(const typename F::T* __restrict__ in, typename F::T* __restrict__ o
     }
     for (int tc = 0; tc < (1 << log_b); ++tc) {
         const uint64_t u = bitrev_dev(unsigned(tc), log_b);
-        for (int k = tid; k < N; k += NT) pre[k] = F::tw_from_const(F::cmul(sq[k], roots.omega(logH, u * k)));
+        for (int k = tid; k < N; k += NT)
+            pre[k] = gpre ? gpre[tc * N + k] : F::tw_from_const(F::cmul(sq[k], roots.omega(logH, u * k)));
         __syncthreads();  // pre ready; A complete (first round) or B free (later rounds)
         PermLoad<F, SH, LOGN> ld{A, pre, c};
         OutStore<T> st{out + col, w, int64_t(tc) * N, logH, bitrev_out != 0, ok};
@@ -244,7 +287,7 @@ k_lde_single(const typename F::T* __restrict__ in, typename F::T* __restrict__ o
 template <class F, int LOGN>
 __global__ void __launch_bounds__(Tile<F, LOGN, LdeCfg<F>::C13>::THREADS, 2)
 k_lde_pass1(const typename F::T* __restrict__ in, typename F::T* __restrict__ scratch, int w, int n1,
-            RootTab<F> roots) {
+            RootTab<F> roots, const typename F::TW* __restrict__ gtwi) {
     constexpr int C = LdeCfg<F>::C13;
     using SH = Tile<F, LOGN, C>;
     using T = typename F::T;
@@ -262,12 +305,18 @@ k_lde_pass1(const typename F::T* __restrict__ in, typename F::T* __restrict__ sc
     const int n = n1 + LOGN;
 
     for (int e = tid; e < N; e += NT) {
-        tw[e] = F::tw_from_const(roots.omega_inv(LOGN, e));
+        tw[e] = gtwi ? gtwi[e] : F::tw_from_const(roots.omega_inv(LOGN, e));
         post[e] = F::tw_from_const(roots.omega_inv(n, uint64_t(i1) * bitrev_dev(e, LOGN)));
     }
     __syncthreads();
+    // scratch is tiled by pass 2's column tiles: element (row r, column col)
+    // at ((col / C2) * h + r) * C2 + col % C2, so that each pass-2 CTA reads
+    // one contiguous block
+    constexpr int C2 = LdeCfg<F>::C2;
+    const int64_t h = int64_t(1) << n;
+    T* dst = ok ? scratch + ((int64_t(col / C2) * h + i1) * C2 + col % C2) : scratch;
     GLoad<T> ld{in + i1 * w + col, N1 * w, ok};
-    BitrevStore<F, LOGN> st{scratch + i1 * w + col, N1 * w, post, ok};
+    BitrevStore<F, LOGN> st{dst, N1 * C2, post, ok};
     cta_dif<F, SH, LOGN, C, 1>(A, tw, t, c, ld, st);
 }
 
@@ -276,7 +325,8 @@ template <class F, int LOGN>
 __global__ void __launch_bounds__(Tile<F, LOGN, LdeCfg<F>::C2>::THREADS, 2)
 k_lde_pass2(const typename F::T* __restrict__ scratch, typename F::T* __restrict__ dst, int w, int n2,
             int log_b, const typename F::T* __restrict__ sp, const typename F::T* __restrict__ sq,
-            RootTab<F> roots) {
+            RootTab<F> roots, const typename F::TW* __restrict__ gtwi, const typename F::TW* __restrict__ gtwf,
+            const typename F::TW* __restrict__ gpre) {
     constexpr int C = LdeCfg<F>::C2;
     using SH = Tile<F, LOGN, C>;
     using T = typename F::T;
@@ -299,12 +349,12 @@ k_lde_pass2(const typename F::T* __restrict__ scratch, typename F::T* __restrict
     const int logH = n + log_b;
 
     for (int e = tid; e < N; e += NT) {
-        twi[e] = F::tw_from_const(roots.omega_inv(LOGN, e));
-        twf[e] = F::tw_from_const(roots.omega(LOGN, e));
+        twi[e] = gtwi ? gtwi[e] : F::tw_from_const(roots.omega_inv(LOGN, e));
+        twf[e] = gtwf ? gtwf[e] : F::tw_from_const(roots.omega(LOGN, e));
     }
     __syncthreads();
     {
-        GLoad<T> ld{scratch + int64_t(N) * k2 * w + col, w, ok};
+        GLoad<T> ld{scratch + (int64_t(blockIdx.y) * h + int64_t(N) * k2) * C + c, C, ok};
         TileStore<T, SH> st{A, c};
         cta_dif<F, SH, LOGN, C, 1>(A, twi, t, c, ld, st);
     }
@@ -312,7 +362,8 @@ k_lde_pass2(const typename F::T* __restrict__ scratch, typename F::T* __restrict
     for (int tc = 0; tc < (1 << log_b); ++tc) {
         const uint64_t u = bitrev_dev(unsigned(tc), log_b);
         for (int k = tid; k < N; k += NT) {
-            pre[k] = F::tw_from_const(F::cmul(sp[k], roots.omega(logH, u * uint64_t(N2) * k)));
+            pre[k] = gpre ? gpre[tc * N + k]
+                          : F::tw_from_const(F::cmul(sp[k], roots.omega(logH, u * uint64_t(N2) * k)));
             post[k] = F::tw_from_const(
                 F::cmul(sqk2, roots.omega(logH, uint64_t(k2) * (u + (uint64_t(bitrev_dev(k, LOGN)) << log_b)))));
         }
@@ -328,7 +379,7 @@ k_lde_pass2(const typename F::T* __restrict__ scratch, typename F::T* __restrict
 template <class F, int LOGN>
 __global__ void __launch_bounds__(Tile<F, LOGN, LdeCfg<F>::C13>::THREADS, 2)
 k_lde_pass3(const typename F::T* src, typename F::T* out, int w, int n1, int log_b, int bitrev_out,
-            RootTab<F> roots) {
+            RootTab<F> roots, const typename F::TW* __restrict__ gtwf) {
     constexpr int C = LdeCfg<F>::C13;
     using SH = Tile<F, LOGN, C>;
     using T = typename F::T;
@@ -345,7 +396,7 @@ k_lde_pass3(const typename F::T* src, typename F::T* out, int w, int n1, int log
     const int logH = n + log_b;
     const int64_t base = blk * N;  // = t*h + s1*N2
 
-    for (int e = tid; e < N; e += NT) tw[e] = F::tw_from_const(roots.omega(LOGN, e));
+    for (int e = tid; e < N; e += NT) tw[e] = gtwf ? gtwf[e] : F::tw_from_const(roots.omega(LOGN, e));
     __syncthreads();
     GLoad<T> ld{src + base * w + col, w, ok};
     OutStore<T> st{out + col, w, base, logH, bitrev_out != 0, ok};
@@ -358,51 +409,62 @@ static void set_smem(Kern k, size_t bytes) {
     P3G_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(bytes)));
 }
 
+// The in-tile twiddle table of size 2^logn (nullptr when there is no table:
+// the kernels then derive it from the root table).
+template <class F>
+static const typename F::TW* tw_table(const typename F::TW* dft_tw, int logn, bool inv) {
+    return dft_tw && logn <= DFT_TW_MAXLOG ? dft_tw + dft_tw_offset(logn, inv) : nullptr;
+}
+
 template <class F, int LOGN>
 static void launch_single(const typename F::T* in, typename F::T* out, int w, int log_b, int br,
-                          const typename F::T* sq, RootTab<F> roots, cudaStream_t st) {
+                          const typename F::T* sq, const typename F::TW* pre, RootTab<F> roots,
+                          const typename F::TW* dft_tw, cudaStream_t st) {
     using SH = Tile<F, LOGN, LdeCfg<F>::C13>;
     size_t smem = 2 * SH::TILE * sizeof(typename F::T) + 3 * SH::N * sizeof(typename F::TW);
     auto k = k_lde_single<F, LOGN>;
     set_smem(k, smem);
     dim3 grid(1, ceil_div(w, LdeCfg<F>::C13));
-    k<<<grid, SH::THREADS, smem, st>>>(in, out, w, log_b, br, sq, roots);
+    k<<<grid, SH::THREADS, smem, st>>>(in, out, w, log_b, br, sq, roots, tw_table<F>(dft_tw, LOGN, true),
+                                       tw_table<F>(dft_tw, LOGN, false), pre);
     P3G_LAUNCHED();
     P3G_CUDA(cudaGetLastError());
 }
 template <class F, int LOGN>
 static void launch_pass1(const typename F::T* in, typename F::T* scr, int w, int n1, RootTab<F> roots,
-                         cudaStream_t st) {
+                         const typename F::TW* dft_tw, cudaStream_t st) {
     using SH = Tile<F, LOGN, LdeCfg<F>::C13>;
     size_t smem = SH::TILE * sizeof(typename F::T) + 2 * SH::N * sizeof(typename F::TW);
     auto k = k_lde_pass1<F, LOGN>;
     set_smem(k, smem);
     dim3 grid(1u << n1, ceil_div(w, LdeCfg<F>::C13));
-    k<<<grid, SH::THREADS, smem, st>>>(in, scr, w, n1, roots);
+    k<<<grid, SH::THREADS, smem, st>>>(in, scr, w, n1, roots, tw_table<F>(dft_tw, LOGN, true));
     P3G_LAUNCHED();
     P3G_CUDA(cudaGetLastError());
 }
 template <class F, int LOGN>
 static void launch_pass2(const typename F::T* scr, typename F::T* dst, int w, int n2, int log_b,
-                         const typename F::T* sp, const typename F::T* sq, RootTab<F> roots, cudaStream_t st) {
+                         const typename F::T* sp, const typename F::T* sq, const typename F::TW* pre,
+                         RootTab<F> roots, const typename F::TW* dft_tw, cudaStream_t st) {
     using SH = Tile<F, LOGN, LdeCfg<F>::C2>;
     size_t smem = 2 * SH::TILE * sizeof(typename F::T) + 4 * SH::N * sizeof(typename F::TW);
     auto k = k_lde_pass2<F, LOGN>;
     set_smem(k, smem);
     dim3 grid(1u << n2, ceil_div(w, LdeCfg<F>::C2));
-    k<<<grid, SH::THREADS, smem, st>>>(scr, dst, w, n2, log_b, sp, sq, roots);
+    k<<<grid, SH::THREADS, smem, st>>>(scr, dst, w, n2, log_b, sp, sq, roots, tw_table<F>(dft_tw, LOGN, true),
+                                       tw_table<F>(dft_tw, LOGN, false), pre);
     P3G_LAUNCHED();
     P3G_CUDA(cudaGetLastError());
 }
 template <class F, int LOGN>
 static void launch_pass3(const typename F::T* src, typename F::T* out, int w, int n1, int log_b, int br,
-                         RootTab<F> roots, cudaStream_t st) {
+                         RootTab<F> roots, const typename F::TW* dft_tw, cudaStream_t st) {
     using SH = Tile<F, LOGN, LdeCfg<F>::C13>;
     size_t smem = SH::TILE * sizeof(typename F::T) + SH::N * sizeof(typename F::TW);
     auto k = k_lde_pass3<F, LOGN>;
     set_smem(k, smem);
     dim3 grid(1u << (n1 + log_b), ceil_div(w, LdeCfg<F>::C13));
-    k<<<grid, SH::THREADS, smem, st>>>(src, out, w, n1, log_b, br, roots);
+    k<<<grid, SH::THREADS, smem, st>>>(src, out, w, n1, log_b, br, roots, tw_table<F>(dft_tw, LOGN, false));
     P3G_LAUNCHED();
     P3G_CUDA(cudaGetLastError());
 }
@@ -415,17 +477,58 @@ static void pow_table(typename F::T* out, uint64_t base, uint64_t scale, int n, 
     P3G_LAUNCHED();
     P3G_CUDA(cudaGetLastError());
 }
-
 template <class F>
-static void lde_impl(p3g_ctx* ctx, const typename F::T* in, int log_h, int w, int log_b, uint64_t shift,
-                     int bitrev_out, typename F::T* out, cudaStream_t st, RootTab<F> roots) {
+static void pre_table(typename F::TW* out, const typename F::T* s, int logn, int log_b, int logH, uint64_t stride,
+                      RootTab<F> roots, cudaStream_t st) {
+    const int64_t n = int64_t(1) << (logn + log_b);
+    k_pre_table<F><<<unsigned(ceil_div(n, 256)), 256, 0, st>>>(out, s, logn, log_b, logH, stride, roots);
+    P3G_LAUNCHED();
+    P3G_CUDA(cudaGetLastError());
+}
+
+// Scratch buffers of one LDE call: [0] first power table, [1] second power
+// table, [2] prepared coset twists, [3] pass-1 output (tiled by pass-2
+// column tiles), [4] natural-order staging.  Sizes in bytes (0 = unused).
+struct LdeScratch {
+    size_t bytes[5] = {0, 0, 0, 0, 0};
+    static size_t round(size_t b) { return (b + 255) / 256 * 256; }
+    size_t total() const {
+        size_t t = 0;
+        for (size_t b : bytes) t += round(b);
+        return t;
+    }
+};
+template <class F>
+LdeScratch lde_scratch(int log_h, int w, int log_b, int bitrev_out) {
     using T = typename F::T;
-    P3G_REQUIRE(log_h >= 0 && log_b >= 0, "coset_lde: negative size");
-    P3G_REQUIRE(log_h + log_b <= int(F::TWO_ADICITY), "coset_lde: log_h + log_blowup exceeds two-adicity");
-    if (log_h > LDE_PASS_MAX) throw Error(P3G_EUNSUPPORTED, "coset_lde: log_h > 21 is not supported");
-    P3G_REQUIRE(shift % F::P != 0, "coset_lde: shift must be non-zero");
+    using TW = typename F::TW;
+    LdeScratch s;
+    if (log_h == 0 || w == 0) return s;
+    const size_t h = size_t(1) << log_h;
+    if (log_h <= LDE_SINGLE_MAX) {
+        s.bytes[0] = sizeof(T) * h;
+        s.bytes[2] = sizeof(TW) * (h << log_b);
+        return s;
+    }
+    const int n2 = (log_h + 1) / 2, n1 = log_h - n2;
+    constexpr int C2 = LdeCfg<F>::C2;
+    s.bytes[0] = sizeof(T) << n1;
+    s.bytes[1] = sizeof(T) << n2;
+    s.bytes[2] = sizeof(TW) << (n1 + log_b);
+    s.bytes[3] = sizeof(T) * size_t(ceil_div(w, C2)) * C2 * h;
+    s.bytes[4] = bitrev_out ? 0 : sizeof(T) * (h << log_b) * size_t(w);
+    return s;
+}
+
+// The LDE proper, on validated arguments (log_h <= LDE_PASS_MAX, shift
+// canonical and non-zero) and scratch buffers sized by lde_scratch.
+template <class F>
+void lde_run(const typename F::T* in, int log_h, int w, int log_b, uint64_t shift, int bitrev_out,
+             typename F::T* out, cudaStream_t st, RootTab<F> roots, const typename F::TW* dft_tw,
+             void* const* buf) {
+    using T = typename F::T;
+    using TW = typename F::TW;
     if (w == 0) return;
-    shift %= F::P;
     const int64_t h = int64_t(1) << log_h;
     if (log_h == 0) {
         int64_t total = (int64_t(1) << log_b) * w;
@@ -436,47 +539,73 @@ static void lde_impl(p3g_ctx* ctx, const typename F::T* in, int log_h, int w, in
     }
     const uint64_t inv_h = F::h_inv(uint64_t(h) % F::P);
     if (log_h <= LDE_SINGLE_MAX) {
-        T* sq = static_cast<T*>(ctx->alloc(sizeof(T) * h, st));
+        T* sq = static_cast<T*>(buf[0]);
+        TW* pre = static_cast<TW*>(buf[2]);
         pow_table<F>(sq, shift, inv_h, int(h), st);
+        pre_table<F>(pre, sq, log_h, log_b, log_h + log_b, 1, roots, st);
         switch (log_h) {
-#define C_(L) case L: launch_single<F, L>(in, out, w, log_b, bitrev_out, sq, roots, st); break;
+#define C_(L) case L: launch_single<F, L>(in, out, w, log_b, bitrev_out, sq, pre, roots, dft_tw, st); break;
             C_(1) C_(2) C_(3) C_(4) C_(5) C_(6) C_(7) C_(8) C_(9) C_(10)
 #undef C_
         }
-        ctx->release(sq, st);
         return;
     }
     const int n2 = (log_h + 1) / 2, n1 = log_h - n2;
-    const int64_t N1 = int64_t(1) << n1, N2 = int64_t(1) << n2;
-    const int64_t H = h << log_b;
-    T* sp = static_cast<T*>(ctx->alloc(sizeof(T) * N1, st));
-    T* sq = static_cast<T*>(ctx->alloc(sizeof(T) * N2, st));
-    T* scr = static_cast<T*>(ctx->alloc(sizeof(T) * size_t(h) * w, st));
-    T* mid = bitrev_out ? out : static_cast<T*>(ctx->alloc(sizeof(T) * size_t(H) * w, st));
-    pow_table<F>(sp, F::h_pow(shift, uint64_t(N2)), inv_h, int(N1), st);
+    const int64_t N2 = int64_t(1) << n2;
+    T* sp = static_cast<T*>(buf[0]);
+    T* sq = static_cast<T*>(buf[1]);
+    TW* pre = static_cast<TW*>(buf[2]);
+    T* scr = static_cast<T*>(buf[3]);
+    T* mid = bitrev_out ? out : static_cast<T*>(buf[4]);
+    pow_table<F>(sp, F::h_pow(shift, uint64_t(N2)), inv_h, int(int64_t(1) << n1), st);
     pow_table<F>(sq, shift, 1, int(N2), st);
+    pre_table<F>(pre, sp, n1, log_b, log_h + log_b, uint64_t(N2), roots, st);
     switch (n2) {
-#define C_(L) case L: launch_pass1<F, L>(in, scr, w, n1, roots, st); break;
+#define C_(L) case L: launch_pass1<F, L>(in, scr, w, n1, roots, dft_tw, st); break;
         P3G_CASES_1_11(C_)
 #undef C_
         default: throw Error(P3G_EUNSUPPORTED, "coset_lde: pass-1 size");
     }
     switch (n1) {
-#define C_(L) case L: launch_pass2<F, L>(scr, mid, w, n2, log_b, sp, sq, roots, st); break;
+#define C_(L) case L: launch_pass2<F, L>(scr, mid, w, n2, log_b, sp, sq, pre, roots, dft_tw, st); break;
         P3G_CASES_1_11(C_)
 #undef C_
         default: throw Error(P3G_EUNSUPPORTED, "coset_lde: pass-2 size");
     }
     switch (n2) {
-#define C_(L) case L: launch_pass3<F, L>(mid, out, w, n1, log_b, bitrev_out, roots, st); break;
+#define C_(L) case L: launch_pass3<F, L>(mid, out, w, n1, log_b, bitrev_out, roots, dft_tw, st); break;
         P3G_CASES_1_11(C_)
 #undef C_
         default: throw Error(P3G_EUNSUPPORTED, "coset_lde: pass-3 size");
     }
-    ctx->release(scr, st);
-    ctx->release(sp, st);
-    ctx->release(sq, st);
-    if (!bitrev_out) ctx->release(mid, st);
+}
+
+// Context entry: validates, takes the scratch from the context's pool.
+template <class F>
+static void lde_impl(p3g_ctx* ctx, const typename F::T* in, int log_h, int w, int log_b, uint64_t shift,
+                     int bitrev_out, typename F::T* out, cudaStream_t st, RootTab<F> roots,
+                     const typename F::TW* dft_tw) {
+    P3G_REQUIRE(log_h >= 0 && log_b >= 0, "coset_lde: negative size");
+    P3G_REQUIRE(log_h + log_b <= int(F::TWO_ADICITY), "coset_lde: log_h + log_blowup exceeds two-adicity");
+    if (log_h > LDE_PASS_MAX) throw Error(P3G_EUNSUPPORTED, "coset_lde: log_h > 21 is not supported");
+    P3G_REQUIRE(shift % F::P != 0, "coset_lde: shift must be non-zero");
+    if (w == 0) return;
+    shift %= F::P;
+    const LdeScratch need = lde_scratch<F>(log_h, w, log_b, bitrev_out);
+    void* buf[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    auto release = [&] {
+        for (int i = 0; i < 5; ++i)
+            if (buf[i]) ctx->release(buf[i], st);
+    };
+    try {
+        for (int i = 0; i < 5; ++i)
+            if (need.bytes[i]) buf[i] = ctx->alloc(need.bytes[i], st);
+        lde_run<F>(in, log_h, w, log_b, shift, bitrev_out, out, st, roots, dft_tw, buf);
+    } catch (...) {
+        release();
+        throw;
+    }
+    release();
 }
 
 }  // namespace p3g

@@ -80,8 +80,6 @@ const NoAllocDevice& na_setup() {
     return d;
 }
 
-inline size_t round64(size_t words) { return (words + 63) / 64 * 64; }
-
 void lde_bb_noalloc(const uint32_t* in, int log_h, int w, int log_b, uint32_t shift, int bitrev_out,
                     uint32_t* out, cudaStream_t st) {
     using F = FBB;
@@ -90,66 +88,23 @@ void lde_bb_noalloc(const uint32_t* in, int log_h, int w, int log_b, uint32_t sh
     P3G_REQUIRE(shift % bb::P != 0 && shift < bb::P, "coset_lde_bb_noalloc: shift must be canonical and non-zero");
     if (log_h > LDE_PASS_MAX) throw Error(P3G_EUNSUPPORTED, "coset_lde_bb_noalloc: log_h > 21 is not supported");
     if (w == 0) return;
-    const size_t h = size_t(1) << log_h;
-    const size_t H = h << log_b;
-    // scratch words this call needs (pow tables, pass-1 output, natural-order staging)
-    size_t need = 0;
-    if (log_h == 0) {
-        need = 0;
-    } else if (log_h <= LDE_SINGLE_MAX) {
-        need = round64(h);
-    } else {
-        const int n2 = (log_h + 1) / 2, n1 = log_h - n2;
-        need = round64(size_t(1) << n1) + round64(size_t(1) << n2) + round64(h * size_t(w)) +
-               (bitrev_out ? 0 : round64(H * size_t(w)));
-    }
-    if (need > NOALLOC_SCRATCH_WORDS)
-        throw Error(P3G_EINVAL, "coset_lde_bb_noalloc: needs " + std::to_string(need * 4) +
+    // scratch this call needs (power tables, prepared twists, pass-1 output,
+    // natural-order staging), carved from the fixed array in 256-byte steps
+    const LdeScratch need = lde_scratch<F>(log_h, w, log_b, bitrev_out);
+    if (need.total() > NOALLOC_SCRATCH_WORDS * 4)
+        throw Error(P3G_EINVAL, "coset_lde_bb_noalloc: needs " + std::to_string(need.total()) +
                                     " bytes of scratch, more than its fixed maximum of " +
                                     std::to_string(NOALLOC_SCRATCH_WORDS * 4) + " bytes");
     const NoAllocDevice& d = na_setup();
-    const RootTab<F> roots{d.lo, d.hi};
-    if (log_h == 0) {
-        const int64_t total = int64_t(H) * w;
-        k_broadcast_row<F><<<ceil_div(total, 256), 256, 0, st>>>(in, out, w, int(H));
-        P3G_LAUNCHED();
-        P3G_CUDA(cudaGetLastError());
-        return;
+    void* buf[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    unsigned char* next = reinterpret_cast<unsigned char*>(d.scratch);
+    for (int i = 0; i < 5; ++i) {
+        if (!need.bytes[i]) continue;
+        buf[i] = next;
+        next += LdeScratch::round(need.bytes[i]);
     }
-    const uint64_t inv_h = F::h_inv(uint64_t(h) % F::P);
-    if (log_h <= LDE_SINGLE_MAX) {
-        uint32_t* sq = d.scratch;
-        pow_table<F>(sq, shift, inv_h, int(h), st);
-        switch (log_h) {
-#define C_(L) case L: launch_single<F, L>(in, out, w, log_b, bitrev_out, sq, roots, st); break;
-            C_(1) C_(2) C_(3) C_(4) C_(5) C_(6) C_(7) C_(8) C_(9) C_(10)
-#undef C_
-        }
-        return;
-    }
-    const int n2 = (log_h + 1) / 2, n1 = log_h - n2;
-    const size_t N1 = size_t(1) << n1, N2 = size_t(1) << n2;
-    uint32_t* sp = d.scratch;
-    uint32_t* sq = sp + round64(N1);
-    uint32_t* scr = sq + round64(N2);
-    uint32_t* mid = bitrev_out ? out : scr + round64(h * size_t(w));
-    pow_table<F>(sp, F::h_pow(shift, uint64_t(N2)), inv_h, int(N1), st);
-    pow_table<F>(sq, shift, 1, int(N2), st);
-    switch (n2) {
-#define C_(L) case L: launch_pass1<F, L>(in, scr, w, n1, roots, st); break;
-        P3G_CASES_1_11(C_)
-#undef C_
-    }
-    switch (n1) {
-#define C_(L) case L: launch_pass2<F, L>(scr, mid, w, n2, log_b, sp, sq, roots, st); break;
-        P3G_CASES_1_11(C_)
-#undef C_
-    }
-    switch (n2) {
-#define C_(L) case L: launch_pass3<F, L>(mid, out, w, n1, log_b, bitrev_out, roots, st); break;
-        P3G_CASES_1_11(C_)
-#undef C_
-    }
+    // no prepared twiddle table: the kernels derive their twiddles from the roots
+    lde_run<F>(in, log_h, w, log_b, shift, bitrev_out, out, st, RootTab<F>{d.lo, d.hi}, nullptr, buf);
 }
 
 }  // namespace
