@@ -121,9 +121,46 @@ P3G_HD uint64_t reduce128(uint64_t lo, uint64_t hi) {
     if (t2 >= P) t2 -= P;
     return t2;
 }
+// a*b as four 32-bit limbs r0..r3 (little-endian) by one multiply-add carry
+// chain: the four partial products are formed once, where a 64-bit low
+// product plus a separate __umul64hi recomputes some of them.
+__device__ __forceinline__ void mul_limbs(uint64_t a, uint64_t b, uint32_t& r0, uint32_t& r1, uint32_t& r2,
+                                          uint32_t& r3) {
+    const uint32_t a0 = uint32_t(a), a1 = uint32_t(a >> 32), b0 = uint32_t(b), b1 = uint32_t(b >> 32);
+    asm("{\n\t"
+        "mul.lo.u32 %0, %4, %6;\n\t"
+        "mul.hi.u32 %1, %4, %6;\n\t"
+        "mul.lo.u32 %2, %5, %7;\n\t"
+        "mul.hi.u32 %3, %5, %7;\n\t"
+        "mad.lo.cc.u32 %1, %4, %7, %1;\n\t"
+        "madc.hi.cc.u32 %2, %4, %7, %2;\n\t"
+        "addc.u32 %3, %3, 0;\n\t"
+        "mad.lo.cc.u32 %1, %5, %6, %1;\n\t"
+        "madc.hi.cc.u32 %2, %5, %6, %2;\n\t"
+        "addc.u32 %3, %3, 0;\n\t"
+        "}"
+        : "=&r"(r0), "=&r"(r1), "=&r"(r2), "=&r"(r3)
+        : "r"(a0), "r"(a1), "r"(b0), "r"(b1));
+}
+// a*b mod p as a value below 2^64 but not necessarily below p (any u64
+// inputs): with 2^64 = 2^32 - 1 and 2^96 = -1 (mod p),
+// a*b = (r0 + r1 2^32) + r2 (2^32 - 1) - r3.
+__device__ __forceinline__ uint64_t mul_lazy(uint64_t a, uint64_t b) {
+    uint32_t r0, r1, r2, r3;
+    mul_limbs(a, b, r0, r1, r2, r3);
+    const uint64_t lo = (uint64_t(r1) << 32) | r0;
+    const uint64_t t = (uint64_t(r2) << 32) - r2;
+    uint64_t s = lo + t;
+    if (s < t) s += EPS;  // wrapped: + 2^64 = + EPS; cannot wrap again (s < t)
+    uint64_t d = s - r3;
+    if (s < r3) d -= EPS;  // borrowed: - 2^64 + p = - EPS; d >= 2^64 - 2^32 first
+    return d;
+}
 #ifdef __CUDA_ARCH__
+// canonical product (any u64 inputs)
 __device__ __forceinline__ uint64_t mul(uint64_t a, uint64_t b) {
-    return reduce128(a * b, __umul64hi(a, b));
+    const uint64_t d = mul_lazy(a, b);
+    return d >= P ? d - P : d;
 }
 #else
 inline uint64_t mul(uint64_t a, uint64_t b) {

@@ -124,16 +124,21 @@ __device__ __forceinline__ void reg_dif(typename F::T* x) {
     }
 }
 
-// Super-stage split of LOGN into radices <= 5.
-__host__ __device__ constexpr int ss_count(int logn) { return logn == 0 ? 0 : (logn + 4) / 5; }
-__host__ __device__ constexpr int ss_radix(int logn, int j) {
+// Super-stage split of LOGN into radices of at most 2^mlr.  mlr is 5 for
+// 4-byte elements and 4 for 8-byte ones: a radix-32 group of u64 values
+// takes 64 registers per thread before any temporaries, which held the
+// Goldilocks passes to a few warps per SM.
+template <class T>
+__host__ __device__ constexpr int ss_max_lr() { return sizeof(T) == 8 ? 4 : 5; }
+__host__ __device__ constexpr int ss_count(int logn, int mlr) { return logn == 0 ? 0 : (logn + mlr - 1) / mlr; }
+__host__ __device__ constexpr int ss_radix(int logn, int j, int mlr) {
     // ceil-balanced split: the first (logn % cnt) parts get one more bit
-    return logn / ss_count(logn) + (j < logn % ss_count(logn) ? 1 : 0);
+    return logn / ss_count(logn, mlr) + (j < logn % ss_count(logn, mlr) ? 1 : 0);
 }
-__host__ __device__ constexpr int ss_max_radix(int logn) { return logn == 0 ? 0 : ss_radix(logn, 0); }
-__host__ __device__ constexpr int ss_consumed(int logn, int j) {
+__host__ __device__ constexpr int ss_max_radix(int logn, int mlr) { return logn == 0 ? 0 : ss_radix(logn, 0, mlr); }
+__host__ __device__ constexpr int ss_consumed(int logn, int j, int mlr) {
     int s = 0;
-    for (int i = 0; i < j; ++i) s += ss_radix(logn, i);
+    for (int i = 0; i < j; ++i) s += ss_radix(logn, i, mlr);
     return s;
 }
 __host__ __device__ constexpr int cmax(int a, int b) { return a > b ? a : b; }
@@ -143,14 +148,15 @@ __host__ __device__ constexpr int ilog2(int x) { return x <= 1 ? 0 : 1 + ilog2(x
 template <class T, int LOGN, int C, int MAXT>
 struct DftShape {
     static constexpr int N = 1 << LOGN;
-    static constexpr int TPC0 = N >> ss_max_radix(LOGN);
+    static constexpr int MLR = ss_max_lr<T>();
+    static constexpr int TPC0 = N >> ss_max_radix(LOGN, MLR);
     static constexpr int TPC = TPC0 * C > MAXT ? MAXT / C : TPC0;  // threads per column
     static constexpr int THREADS = TPC * C;
     // swizzled shared-memory layout
     static constexpr int LINE = 128 / int(sizeof(T));   // elements per 128-byte line
     static constexpr int RPL = LINE / C >= 1 ? LINE / C : 1;  // row segments per line
     static constexpr int LG = ilog2(RPL);
-    static constexpr int RL = ss_count(LOGN) ? ss_radix(LOGN, ss_count(LOGN) - 1) : 0;
+    static constexpr int RL = ss_count(LOGN, MLR) ? ss_radix(LOGN, ss_count(LOGN, MLR) - 1, MLR) : 0;
     static constexpr int SH1 = cmax(RL, LG);
     static constexpr int SH2 = cmax(LOGN - LG, LG);
     static constexpr int TILE = N * C;  // elements
@@ -169,9 +175,10 @@ template <class F, class SH, int LOGN, int J, int C, int INV, class Load, class 
 __device__ __forceinline__ void super_stage(typename F::T* tile, const typename F::TW* tw, int t, int c,
                                             Load& load, Store& store) {
     using T = typename F::T;
-    constexpr int CNT = ss_count(LOGN);
-    constexpr int LR = ss_radix(LOGN, J);
-    constexpr int LS = LOGN - ss_consumed(LOGN, J);
+    constexpr int MLR = ss_max_lr<T>();
+    constexpr int CNT = ss_count(LOGN, MLR);
+    constexpr int LR = ss_radix(LOGN, J, MLR);
+    constexpr int LS = LOGN - ss_consumed(LOGN, J, MLR);
     constexpr int R = 1 << LR;
     constexpr int M = (1 << LS) >> LR;
     constexpr int GROUPS = (1 << LOGN) >> LR;
@@ -209,9 +216,10 @@ struct SSChain {
     template <class Load, class Store>
     static __device__ __forceinline__ void run(typename F::T* tile, const typename F::TW* tw, int t, int c,
                                                Load& load, Store& store) {
-        if constexpr (J < ss_count(LOGN)) {
+        constexpr int CNT = ss_count(LOGN, ss_max_lr<typename F::T>());
+        if constexpr (J < CNT) {
             super_stage<F, SH, LOGN, J, C, INV>(tile, tw, t, c, load, store);
-            if constexpr (J + 1 < ss_count(LOGN)) __syncthreads();
+            if constexpr (J + 1 < CNT) __syncthreads();
             SSChain<F, SH, LOGN, C, INV, J + 1>::run(tile, tw, t, c, load, store);
         }
     }

@@ -109,11 +109,13 @@ __device__ __forceinline__ void p2_bb16(uint32_t* s, const P2BB16& p) {
 }
 
 // ------------------------------------------------------------------ Goldilocks 8
+// x^d with the intermediate powers left below 2^64 but unreduced mod p
+// (a product accepts any u64 operands); only the result is canonical.
 __device__ __forceinline__ uint64_t gl_sbox(uint64_t x, int d) {
-    uint64_t x2 = gl::mul(x, x);
+    uint64_t x2 = gl::mul_lazy(x, x);
     if (d == 3) return gl::mul(x2, x);
-    if (d == 5) return gl::mul(gl::mul(x2, x2), x);
-    uint64_t x3 = gl::mul(x2, x), x4 = gl::mul(x2, x2);
+    if (d == 5) return gl::mul(gl::mul_lazy(x2, x2), x);
+    uint64_t x3 = gl::mul_lazy(x2, x), x4 = gl::mul_lazy(x2, x2);
     return gl::mul(x3, x4);
 }
 // x * 2^k for 1 <= k < 64, canonical in/out.
