@@ -78,7 +78,6 @@ __device__ __forceinline__ void mds_light(T* s) {
 }
 
 __device__ __forceinline__ uint32_t bbadd(uint32_t a, uint32_t b) { return bb::add(a, b); }
-__device__ __forceinline__ uint64_t gladd(uint64_t a, uint64_t b) { return gl::add(a, b); }
 
 // State in Montgomery form.
 template <int D, int RF, int RP>
@@ -118,35 +117,93 @@ __device__ __forceinline__ uint64_t gl_sbox(uint64_t x, int d) {
     uint64_t x3 = gl::mul_lazy(x2, x), x4 = gl::mul_lazy(x2, x2);
     return gl::mul(x3, x4);
 }
-// x * 2^k for 1 <= k < 64, canonical in/out.
-__device__ __forceinline__ uint64_t gl_mul_pow2(uint64_t x, int k) {
-    return gl::reduce128(x << k, x >> (64 - k));
+// Goldilocks linear layers on unreduced sums: a G2 is lo + hi * 2^64 with a
+// small hi (a carry count), added with one three-limb carry chain and
+// reduced once per output (2^64 = 2^32 - 1 mod p), instead of a canonical
+// reduction after every addition.
+struct G2 {
+    uint64_t lo;
+    uint32_t hi;
+};
+__device__ __forceinline__ G2 g2(uint64_t x) { return {x, 0u}; }
+__device__ __forceinline__ G2 g2add(G2 a, G2 b) {
+    uint32_t l0, l1, h;
+    asm("{\n\t"
+        "add.cc.u32 %0, %3, %6;\n\t"
+        "addc.cc.u32 %1, %4, %7;\n\t"
+        "addc.u32 %2, %5, %8;\n\t"
+        "}"
+        : "=r"(l0), "=r"(l1), "=r"(h)
+        : "r"(uint32_t(a.lo)), "r"(uint32_t(a.lo >> 32)), "r"(a.hi), "r"(uint32_t(b.lo)),
+          "r"(uint32_t(b.lo >> 32)), "r"(b.hi));
+    return {(uint64_t(l1) << 32) | l0, h};
+}
+// canonical value of a G2 (hi < 2^32)
+__device__ __forceinline__ uint64_t g2red(G2 a) {
+    const uint64_t t = (uint64_t(a.hi) << 32) - a.hi;  // hi * (2^32 - 1) <= (2^32 - 1)^2
+    uint64_t s = a.lo + t;
+    if (s < t) s += gl::EPS;  // wrapped: + 2^64 = + EPS; s < t keeps this below 2^64
+    return s >= gl::P ? s - gl::P : s;
+}
+// x * 2^k as a G2, 1 <= k < 32
+__device__ __forceinline__ G2 g2shl(uint64_t x, int k) { return {x << k, uint32_t(x >> (64 - k))}; }
+
+// MDS-light for width 8 (external.hpp:67-77, 170-201): [2 3 1 1] on each
+// 4-chunk, then the column sums; every output is a sum of at most 21 inputs.
+__device__ __forceinline__ void mds_light_gl8(uint64_t* s) {
+    G2 y[8];
+#pragma unroll
+    for (int c = 0; c < 8; c += 4) {
+        const G2 x0 = g2(s[c]), x1 = g2(s[c + 1]), x2 = g2(s[c + 2]), x3 = g2(s[c + 3]);
+        const G2 t01 = g2add(x0, x1), t23 = g2add(x2, x3);
+        const G2 t0123 = g2add(t01, t23);
+        const G2 t01123 = g2add(t0123, x1), t01233 = g2add(t0123, x3);
+        y[c + 3] = g2add(t01233, g2add(x0, x0));
+        y[c + 1] = g2add(t01123, g2add(x2, x2));
+        y[c + 0] = g2add(t01123, t01);
+        y[c + 2] = g2add(t01233, t23);
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const G2 col = g2add(y[k], y[k + 4]);
+        s[k] = g2red(g2add(y[k], col));
+        s[k + 4] = g2red(g2add(y[k + 4], col));
+    }
+}
+// s + c for canonical c; the result is below 2^64 but possibly >= p (an
+// S-box input: products accept any u64)
+__device__ __forceinline__ uint64_t gl_add_lazy(uint64_t a, uint64_t c) {
+    uint64_t t = a + c;
+    if (t < c) t += gl::EPS;  // a + c - 2^64 < 2^64 - 2^33 leaves room for EPS
+    return t;
 }
 
 template <int D, int RF, int RP>
 __device__ __forceinline__ void p2_gl8(uint64_t* s, const P2GL8& p) {
-    mds_light<uint64_t, 8, gladd>(s);
+    mds_light_gl8(s);
 #pragma unroll
     for (int r = 0; r < RF / 2; ++r) {
 #pragma unroll
-        for (int i = 0; i < 8; ++i) s[i] = gl_sbox(gl::add(s[i], p.initial[r][i]), D);
-        mds_light<uint64_t, 8, gladd>(s);
+        for (int i = 0; i < 8; ++i) s[i] = gl_sbox(gl_add_lazy(s[i], p.initial[r][i]), D);
+        mds_light_gl8(s);
     }
 #pragma unroll
     for (int r = 0; r < RP; ++r) {
-        s[0] = gl_sbox(gl::add(s[0], p.internal[r]), D);
-        uint64_t sum = s[0];
+        // internal layer (generic.hpp:148-175): s_i <- s_i * 2^i + sum(s)
+        s[0] = gl_sbox(gl_add_lazy(s[0], p.internal[r]), D);
+        G2 acc = g2(s[0]);
 #pragma unroll
-        for (int i = 1; i < 8; ++i) sum = gl::add(sum, s[i]);
-        s[0] = gl::add(s[0], sum);
+        for (int i = 1; i < 8; ++i) acc = g2add(acc, g2(s[i]));
+        const G2 sum = g2(g2red(acc));
+        s[0] = g2red(g2add(g2(s[0]), sum));
 #pragma unroll
-        for (int i = 1; i < 8; ++i) s[i] = gl::add(gl_mul_pow2(s[i], i), sum);
+        for (int i = 1; i < 8; ++i) s[i] = g2red(g2add(g2shl(s[i], i), sum));
     }
 #pragma unroll
     for (int r = 0; r < RF / 2; ++r) {
 #pragma unroll
-        for (int i = 0; i < 8; ++i) s[i] = gl_sbox(gl::add(s[i], p.terminal[r][i]), D);
-        mds_light<uint64_t, 8, gladd>(s);
+        for (int i = 0; i < 8; ++i) s[i] = gl_sbox(gl_add_lazy(s[i], p.terminal[r][i]), D);
+        mds_light_gl8(s);
     }
 }
 
