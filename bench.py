@@ -219,6 +219,11 @@ def run_goldilocks(P, torch, ctx, dev, stream, steps: int, warmup: int, log_h: i
     lde_bytes = 8 * width * (h + H)
     hbm, src = peaks()
     perms = H * ((width + 3) // 4) + (H - 1)
+    traffic = None
+    tpath = os.path.join(REPO, "profiles", "traffic.json")
+    if os.path.exists(tpath):
+        with open(tpath) as f:
+            traffic = json.load(f).get(f"lde_gl_2p{log_h}x{width}_b{log_b}_bytes")
     return {
         "workload": f"plain single-trace Goldilocks commit: 2^{log_h} x {width} trace, log_blowup {log_b}, "
                     f"shift {shift}, bit-reversed LDE 2^{log_h + log_b} x {width}, Poseidon2-8 (x^7, 8+22) MMCS, "
@@ -227,7 +232,8 @@ def run_goldilocks(P, torch, ctx, dev, stream, steps: int, warmup: int, log_h: i
         "p50_ms": float(np.percentile(st, 50)), "p99_ms": float(np.percentile(st, 99)),
         "kernels_per_step": int(launches),
         "lde": {"ms": lde_ms, "algorithmic_bytes": lde_bytes, "achieved_gbs": lde_bytes / (lde_ms / 1e3) / 1e9,
-                "peak_gbs": hbm, "frac": lde_bytes / (lde_ms / 1e3) / 1e9 / hbm, "peak_source": src},
+                "peak_gbs": hbm, "frac": lde_bytes / (lde_ms / 1e3) / 1e9 / hbm, "peak_source": src,
+                "traffic": traffic},
         "merkle": {"ms": ms - lde_ms, "perms": perms, "perms_per_s": perms / ((ms - lde_ms) / 1e3)},
     }
 
@@ -522,8 +528,11 @@ def run_ours(args):
         result["config4"] = run_serving(P, torch, ctx, [50, 100, 200, 500, 1000, 2000], args.serving_requests)
     if rank == 0 and not args.no_cpu:
         v, dt, desc = cpu_sample(os.cpu_count() or 1)
+        v1, dt1, desc1 = cpu_sample(1, 12)
         result["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
-                                  "sample": desc, "seconds": dt}
+                                  "sample": desc, "seconds": dt,
+                                  "single_thread": {"value": v1, "cores": 1, "sample": desc1, "seconds": dt1,
+                                                    "note": "the reference's own CPU path is single-threaded"}}
     d_trace.free()
     ctx.close()
     if rank == 0:
