@@ -108,6 +108,24 @@ P3G_API int p3g_poseidon2_permute(p3g_ctx *ctx, int field, void *d_states, size_
 P3G_API int p3g_coset_lde(p3g_ctx *ctx, int field, const void *d_in, uint32_t log_h, uint32_t width,
                   uint32_t log_blowup, uint64_t shift, int bitrev_out, void *d_out, void *stream);
 
+/* The Dft interface's other members on a batch of columns:
+ *   P3G_DFT        Radix2Dit::dft_batch        (radix2_dit.hpp:82-121)
+ *   P3G_IDFT       Radix2Dit::idft_batch       (radix2_dit.hpp:136-160)
+ *   P3G_COSET_DFT  Radix2Dit::coset_dft_batch  (radix2_dit.hpp:173-186), shift used
+ *   P3G_COSET_IDFT Radix2Dit::coset_idft_batch (radix2_dit.hpp:194-210), shift used
+ * and, if bitrev_out, reverse_matrix_index_bits of the result.  Replaces
+ * NttCuda's dft_batch / idft_batch / coset_dft_batch / coset_idft_batch
+ * (ntt_cuda.hpp:310-356).  in, out: (1 << log_h) x width, natural order
+ * unless bitrev_out; in and out must not overlap.  Supports log_h <= 21. */
+enum p3g_dft_kind {
+    P3G_DFT = 0,
+    P3G_IDFT = 1,
+    P3G_COSET_DFT = 2,
+    P3G_COSET_IDFT = 3
+};
+P3G_API int p3g_dft(p3g_ctx *ctx, int field, int kind, const void *d_in, uint32_t log_h, uint32_t width,
+                    uint64_t shift, int bitrev_out, void *d_out, void *stream);
+
 /* BabyBear-only variant of p3g_coset_lde that allocates nothing and needs no
  * context.  It has no counterpart in the reference.  It is for callers that
  * must not enter the CUDA allocator while they prove -- a service that

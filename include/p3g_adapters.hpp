@@ -8,7 +8,9 @@
 // adapters can be passed as template arguments wherever the reference classes
 // are:
 //
-//   GpuDft<p3_dft::Radix2Dit<BabyBear>>            coset_lde_batch      (radix2_dit.hpp:221)
+//   GpuDft<p3_dft::Radix2Dit<BabyBear>>            coset_lde_batch      (radix2_dit.hpp:221),
+//                                                  dft_batch, idft_batch, coset_dft_batch,
+//                                                  coset_idft_batch     (radix2_dit.hpp:82-210)
 //   GpuInputMmcs<p3_merkle::MerkleTreeMmcs<...>>   commit_matrix        (fri_merkle_tree_mmcs.hpp:55)
 //   GpuMerkleTreeMmcs<p3_merkle_tree::MerkleTreeMmcs<...>> commit       (merkle_tree_mmcs.hpp:100)
 //   gpu_fold_matrix<Val, Challenge>(...)          fold_matrix           (fri_folding.hpp:200)
@@ -218,6 +220,40 @@ struct GpuDft : Base {
         std::vector<unsigned char> out(H * w * E);
         dout.download(out.data(), out.size());
         return Mat(from_words<F>(out.data(), H * w), w);
+    }
+
+    // The other Dft members (radix2_dit.hpp:82-210), natural row order.
+    template <class Mat>
+    Mat dft_batch(Mat mat) {
+        return transform(P3G_DFT, std::move(mat), 0);
+    }
+    template <class Mat>
+    Mat idft_batch(Mat mat) {
+        return transform(P3G_IDFT, std::move(mat), 0);
+    }
+    template <class Mat, class F>
+    Mat coset_dft_batch(Mat mat, const F& shift) {
+        return transform(P3G_COSET_DFT, std::move(mat), canonical(shift));
+    }
+    template <class Mat, class F>
+    Mat coset_idft_batch(Mat mat, const F& shift) {
+        return transform(P3G_COSET_IDFT, std::move(mat), canonical(shift));
+    }
+
+   private:
+    template <class Mat>
+    static Mat transform(int kind, Mat mat, uint64_t shift) {
+        using F = std::decay_t<decltype(mat.values[0])>;
+        const size_t h = mat.height(), w = mat.width();
+        if (h <= 1 || w == 0) return mat;  // every kind leaves one row unchanged (radix2_dit.hpp:84)
+        const size_t log_h = log2_strict(h);
+        auto words = to_words(mat.values);
+        DeviceBuffer din(words.size()), dout(words.size());
+        din.upload(words.data(), words.size());
+        check(p3g_dft(Context::get().handle(), field_id<F>(), kind, din.get(), uint32_t(log_h), uint32_t(w), shift, 0,
+                      dout.get(), nullptr));
+        dout.download(words.data(), words.size());
+        return Mat(from_words<F>(words.data(), h * w), w);
     }
 };
 

@@ -286,6 +286,28 @@ int p3g_coset_lde(p3g_ctx* ctx, int field, const void* d_in, uint32_t log_h, uin
     API_END
 }
 
+int p3g_dft(p3g_ctx* ctx, int field, int kind, const void* d_in, uint32_t log_h, uint32_t width, uint64_t shift,
+            int bitrev_out, void* d_out, void* stream) {
+    API_BEGIN
+    P3G_REQUIRE(ctx && (width == 0 || (d_in && d_out)), "dft: null argument");
+    P3G_REQUIRE(width <= (1u << 24), "dft: width too large");
+    P3G_REQUIRE(kind >= P3G_DFT && kind <= P3G_COSET_IDFT, "dft: unknown kind");
+    P3G_REQUIRE(width == 0 || d_in != d_out, "dft: in and out must not overlap");
+    DeviceGuard g(ctx->device);
+    if (field == P3G_BABYBEAR) {
+        P3G_REQUIRE(shift < p3g::bb::P, "dft: shift must be canonical");
+        p3g::dft_bb(ctx, kind, static_cast<const uint32_t*>(d_in), int(log_h), int(width), uint32_t(shift),
+                    bitrev_out, static_cast<uint32_t*>(d_out), S(stream));
+    } else if (field == P3G_GOLDILOCKS) {
+        P3G_REQUIRE(shift < p3g::gl::P, "dft: shift must be canonical");
+        p3g::dft_gl(ctx, kind, static_cast<const uint64_t*>(d_in), int(log_h), int(width), shift, bitrev_out,
+                    static_cast<uint64_t*>(d_out), S(stream));
+    } else {
+        P3G_REQUIRE(false, "dft: unknown field");
+    }
+    API_END
+}
+
 static void copy_cap(const p3g_tree* t, void* h_out, cudaStream_t st) {
     if (!h_out) return;
     const size_t esz = t->field == P3G_BABYBEAR ? 4 : 8;

@@ -23,13 +23,17 @@ GL_P = 0xFFFFFFFF00000001
 EXPORTS = [
     "p3g_version", "p3g_status_string", "p3g_last_error", "p3g_kernel_launches", "p3g_ctx_create", "p3g_ctx_destroy",
     "p3g_stream_synchronize", "p3g_malloc", "p3g_free", "p3g_memcpy_h2d", "p3g_memcpy_d2h",
-    "p3g_set_poseidon2", "p3g_poseidon2_permute", "p3g_coset_lde", "p3g_mmcs_commit",
+    "p3g_set_poseidon2", "p3g_poseidon2_permute", "p3g_coset_lde", "p3g_dft", "p3g_mmcs_commit",
     "p3g_commit_matrix", "p3g_tree_info", "p3g_tree_layer_ptr", "p3g_tree_leaf_ptr",
     "p3g_mmcs_open_batch", "p3g_tree_free", "p3g_commit_traces", "p3g_fold_matrix_bb4",
     "p3g_coset_lde_bb_noalloc", "p3g_plan_commit", "p3g_plan_launch", "p3g_plan_info",
     "p3g_plan_destroy", "p3g_server_create", "p3g_server_submit", "p3g_server_poll",
     "p3g_server_pending", "p3g_server_open", "p3g_server_release", "p3g_server_destroy",
 ]
+
+
+# p3g_dft kinds
+DFT, IDFT, COSET_DFT, COSET_IDFT = 0, 1, 2, 3
 
 
 class P3GError(RuntimeError):
@@ -94,6 +98,7 @@ def load(path: str | None = None):
     L.p3g_set_poseidon2.argtypes = [vp, i32, u32, u32, u32, u32, vp, vp, vp]
     L.p3g_poseidon2_permute.argtypes = [vp, i32, vp, sz, vp]
     L.p3g_coset_lde.argtypes = [vp, i32, vp, u32, u32, u32, u64, i32, vp, vp]
+    L.p3g_dft.argtypes = [vp, i32, i32, vp, u32, u32, u64, i32, vp, vp]
     L.p3g_mmcs_commit.argtypes = [vp, i32, C.POINTER(Matrix), sz, u32, C.POINTER(vp), vp, vp]
     L.p3g_commit_matrix.argtypes = [vp, i32, vp, u64, u32, C.POINTER(vp), vp, vp]
     L.p3g_tree_info.argtypes = [vp, C.POINTER(u32), C.POINTER(u64), C.POINTER(u32)]
@@ -427,6 +432,26 @@ class Context:
         din.free()
         dout.free()
         return out
+
+    # -- dft / idft / coset_dft / coset_idft
+    def dft_device(self, field: int, kind: int, d_in: int, log_h: int, width: int, shift: int, bitrev: bool,
+                   d_out: int, stream=None):
+        check(load().p3g_dft(self.handle, field, kind, d_in, log_h, width, shift, int(bitrev), d_out, stream))
+
+    def dft(self, kind: int, mat: np.ndarray, shift: int = 0, bitrev: bool = False) -> np.ndarray:
+        """kind: DFT, IDFT, COSET_DFT or COSET_IDFT; natural order unless bitrev."""
+        field = BABYBEAR if mat.dtype == np.uint32 else GOLDILOCKS
+        h, w = mat.shape
+        log_h = h.bit_length() - 1
+        assert 1 << log_h == h
+        din = self.to_device(mat)
+        dout = self.alloc(max(h * w * mat.itemsize, 1))
+        try:
+            self.dft_device(field, kind, din.ptr, log_h, w, shift, bitrev, dout.ptr)
+            return dout.download(mat.dtype, (h, w))
+        finally:
+            din.free()
+            dout.free()
 
     # -- MMCS
     def mmcs_commit_device(self, field: int, mats, cap_height: int = 0, stream=None) -> Tree:

@@ -10,7 +10,8 @@
 //      against the stock Pcs (same commitment);
 //   2. GpuMerkleTreeMmcs<mixed-height MMCS>::commit against the stock one (all
 //      digest layers), then the stock open_batch / verify_batch on the GPU tree;
-//   3. gpu_fold_matrix against TwoAdicFriFolding<BB, BB4>::fold_matrix.
+//   3. GpuDft's dft / idft / coset_dft / coset_idft against Radix2Dit's;
+//   4. gpu_fold_matrix against TwoAdicFriFolding<BB, BB4>::fold_matrix.
 
 #include "baby_bear.hpp"
 #include "extension_field.hpp"
@@ -127,7 +128,23 @@ int main() {
         fails += report("open_batch on the GPU tree verifies", ok);
     }
 
-    // 3. fold_matrix
+    // 3. the other Dft members against Radix2Dit
+    {
+        p3_dft::Radix2Dit<BB> cpu;
+        p3g::GpuDft<p3_dft::Radix2Dit<BB>> gpu;
+        const BB shift(uint32_t(7));
+        bool ok = true;
+        for (size_t log_h : {size_t(3), size_t(10), size_t(13)}) {
+            auto m = [&] { return rand_matrix(size_t(1) << log_h, 5, 300 + uint32_t(log_h)); };
+            ok = ok && cpu.dft_batch(m()).values == gpu.dft_batch(m()).values;
+            ok = ok && cpu.idft_batch(m()).values == gpu.idft_batch(m()).values;
+            ok = ok && cpu.coset_dft_batch(m(), shift).values == gpu.coset_dft_batch(m(), shift).values;
+            ok = ok && cpu.coset_idft_batch(m(), shift).values == gpu.coset_idft_batch(m(), shift).values;
+        }
+        fails += report("dft_batch / idft_batch / coset_dft_batch / coset_idft_batch", ok);
+    }
+
+    // 4. fold_matrix
     {
         std::mt19937 rng(7);
         auto r = [&] { return BB(uint32_t(rng() % BB::PRIME)); };

@@ -10,6 +10,7 @@
 //   adapters_standin commit_matrix <in> <out> <height> <width>
 //   adapters_standin mmcs <bb|gl> <in> <out> <cap_height> <h0> <w0> [<h1> <w1> ...]
 //   adapters_standin fold <in> <out> <log_height> <log_arity>
+//   adapters_standin dft <bb|gl> <in> <out> <log_h> <width> <kind 0-3> <shift>
 //
 // <in> holds canonical little-endian words (u32 BabyBear, u64 Goldilocks;
 // for mmcs the matrices back to back; for fold 4 beta coefficients, then
@@ -152,6 +153,22 @@ static int run_lde(char** a) {
     return 0;
 }
 
+template <class F>
+static int run_dft(char** a) {
+    auto in = read_file(a[3]);
+    const size_t log_h = std::strtoul(a[5], nullptr, 0), w = std::strtoul(a[6], nullptr, 0);
+    const int kind = std::atoi(a[7]);
+    const F shift(std::strtoull(a[8], nullptr, 0));
+    RowMajorMatrix<F> m(p3g::from_words<F>(in.data(), (size_t(1) << log_h) * w), w);
+    p3g::GpuDft<Radix2Dit> dft;
+    RowMajorMatrix<F> out = kind == 0   ? dft.dft_batch(std::move(m))
+                            : kind == 1 ? dft.idft_batch(std::move(m))
+                            : kind == 2 ? dft.coset_dft_batch(std::move(m), shift)
+                                        : dft.coset_idft_batch(std::move(m), shift);
+    write_file(a[4], p3g::to_words(out.values));
+    return 0;
+}
+
 template <class F, size_t N>
 static int run_mmcs(int argc, char** a) {
     auto in = read_file(a[3]);
@@ -180,6 +197,10 @@ int main(int argc, char** argv) {
     try {
         set_constants();
         if (cmd == "lde") return std::string(argv[2]) == "bb" ? run_lde<BabyBear>(argv) : run_lde<Goldilocks>(argv);
+        if (cmd == "dft") {
+            if (argc < 9) return 2;
+            return std::string(argv[2]) == "bb" ? run_dft<BabyBear>(argv) : run_dft<Goldilocks>(argv);
+        }
         if (cmd == "mmcs")
             return std::string(argv[2]) == "bb" ? run_mmcs<BabyBear, 8>(argc, argv) : run_mmcs<Goldilocks, 4>(argc, argv);
         if (cmd == "commit_matrix") {

@@ -43,6 +43,7 @@ def test_null_arguments_rejected_without_gpu_work():
     L.p3g_last_error(buf, 256)
     assert b"null" in buf.value
     assert L.p3g_ctx_create(0, None) == 1
+    assert L.p3g_dft(None, 0, P.DFT, None, 4, 4, 0, 0, None, None) == 1
 
 
 def test_seeded_constants_match_oracle():

@@ -56,6 +56,30 @@ def test_gpu_dft_coset_lde_batch(prog, tmp_path, field, log_h, w, bits, shift):
     assert np.array_equal(got, want)
 
 
+@pytest.mark.parametrize("field,log_h,kind", [("bb", 5, 0), ("bb", 12, 1), ("bb", 11, 2), ("bb", 13, 3),
+                                               ("gl", 9, 0), ("gl", 12, 3)])
+def test_gpu_dft_other_members(prog, tmp_path, field, log_h, kind):
+    """GpuDft::dft_batch / idft_batch / coset_dft_batch / coset_idft_batch."""
+    w, shift = 3, 7
+    rng = np.random.default_rng(log_h * 4 + kind)
+    if field == "bb":
+        t = rng.integers(0, O.BB_P, size=(1 << log_h, w), dtype=np.uint32)
+        want = O.bb_dft(["dft", "idft", "coset_dft", "coset_idft"][kind], t, shift)
+    else:
+        t = rng.integers(0, O.GL_P, size=(1 << log_h, w), dtype=np.uint64)
+        want = None  # the oracle restates the BabyBear DFTs; Goldilocks is checked by inversion
+    rc, err, fout = _run(prog, tmp_path, "dft", field, [log_h, w, kind, shift], t)
+    assert rc == 0, err
+    got = np.fromfile(fout, dtype=t.dtype).reshape(t.shape)
+    if want is not None:
+        assert np.array_equal(got, want)
+    else:
+        back = 1 if kind == 0 else 2  # dft -> idft, coset_idft -> coset_dft
+        rc, err, fout2 = _run(prog, tmp_path, "dft", field, [log_h, w, back, shift], got)
+        assert rc == 0, err
+        assert np.array_equal(np.fromfile(fout2, dtype=t.dtype).reshape(t.shape), t)
+
+
 @pytest.mark.parametrize("h,w", [(1, 8), (37, 8), (256, 16), (1000, 3)])
 def test_gpu_input_mmcs_commit_matrix(prog, tmp_path, h, w):
     rng = np.random.default_rng(h + w)
