@@ -205,6 +205,16 @@ typedef struct {
 P3G_API int p3g_commit_traces(p3g_ctx *ctx, int field, const p3g_trace *traces, size_t n_traces,
                       uint32_t cap_height, p3g_tree **tree_out, void *h_cap_out, void *stream);
 
+/* p3g_commit_traces with the traces in HOST memory (d_trace is a host
+ * pointer; pinned memory gives asynchronous copies).  Each trace is copied in
+ * column chunks of 512-byte rows on a second stream, and each chunk's LDE
+ * starts as soon as its copy has landed, so the copies overlap the LDEs.
+ * The commitment is the same as for the unsplit traces (a leaf hashes the
+ * concatenated rows of equal-height matrices in order, merkle_tree.hpp:84-185);
+ * the tree's leaf matrices are the column chunks, in trace order. */
+P3G_API int p3g_commit_traces_host(p3g_ctx *ctx, int field, const p3g_trace *traces, size_t n_traces,
+                                   uint32_t cap_height, p3g_tree **tree_out, void *h_cap_out, void *stream);
+
 /* ------------------------------------------------------------ batched commit as one graph */
 typedef struct p3g_plan p3g_plan;
 

@@ -3,6 +3,7 @@
 // Converts C++ exceptions into P3G_* status codes and a per-thread message,
 // owns contexts (root-of-unity tables, Poseidon2 constants, a stream-ordered
 // memory pool) and trees.  No entry point falls back to the CPU.
+#include <algorithm>
 #include <atomic>
 #include <cstring>
 #include <memory>
@@ -441,6 +442,84 @@ int p3g_commit_traces(p3g_ctx* ctx, int field, const p3g_trace* traces, size_t n
         p3g::tree_release(ctx, t.get(), st);
         throw;
     }
+    *tree_out = t.release();
+    API_END
+}
+
+int p3g_commit_traces_host(p3g_ctx* ctx, int field, const p3g_trace* traces, size_t n_traces, uint32_t cap_height,
+                           p3g_tree** tree_out, void* h_cap_out, void* stream) {
+    API_BEGIN
+    P3G_REQUIRE(ctx && traces && n_traces > 0 && tree_out, "commit_traces_host: null argument");
+    P3G_REQUIRE(field == P3G_BABYBEAR || field == P3G_GOLDILOCKS, "commit_traces_host: unknown field");
+    DeviceGuard g(ctx->device);
+    cudaStream_t st = S(stream);
+    const size_t esz = field == P3G_BABYBEAR ? 4 : 8;
+    // 512-byte chunk rows keep the strided copies at the contiguous copy's
+    // bandwidth (narrower rows lose 15% at 256 bytes, half at 128)
+    const uint32_t cw_max = uint32_t(512 / esz);
+    for (size_t i = 0; i < n_traces; ++i) {
+        const p3g_trace& tr = traces[i];
+        P3G_REQUIRE(tr.width == 0 || tr.d_trace, "commit_traces_host: null trace");
+        P3G_REQUIRE(tr.shift < (field == P3G_BABYBEAR ? uint64_t(p3g::bb::P) : p3g::gl::P),
+                    "commit_traces_host: shift must be canonical");
+        P3G_REQUIRE(tr.log_h <= 21, "commit_traces_host: log_h > 21 is not supported");
+    }
+    auto t = std::make_unique<p3g_tree>();
+    t->field = field;
+    cudaStream_t cs = nullptr;
+    cudaEvent_t start = nullptr;
+    std::vector<cudaEvent_t> evs;
+    void* pending = nullptr;  // chunk buffer not yet handed back to the pool
+    auto cleanup = [&] {
+        for (cudaEvent_t e : evs) cudaEventDestroy(e);
+        if (start) cudaEventDestroy(start);
+        if (cs) cudaStreamDestroy(cs);
+    };
+    try {
+        P3G_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+        P3G_CUDA(cudaEventCreateWithFlags(&start, cudaEventDisableTiming));
+        P3G_CUDA(cudaEventRecord(start, st));
+        P3G_CUDA(cudaStreamWaitEvent(cs, start, 0));
+        for (size_t i = 0; i < n_traces; ++i) {
+            const p3g_trace& tr = traces[i];
+            const uint64_t h = uint64_t(1) << tr.log_h, H = h << tr.log_blowup;
+            for (uint32_t c0 = 0; c0 < tr.width || (tr.width == 0 && c0 == 0); c0 += cw_max) {
+                const uint32_t cw = std::min(cw_max, tr.width - c0);
+                void* lde = ctx->alloc(std::max<size_t>(esz * H * cw, esz), st);
+                t->owned.push_back(lde);
+                t->mats.push_back(p3g_matrix{lde, H, cw, 0});
+                if (cw == 0) break;
+                // copy stream: this chunk's columns into a contiguous h x cw buffer
+                void* dev = ctx->alloc(esz * h * cw, cs);
+                pending = dev;
+                P3G_CUDA(cudaMemcpy2DAsync(dev, esz * cw, static_cast<const char*>(tr.d_trace) + esz * c0,
+                                           esz * tr.width, esz * cw, h, cudaMemcpyHostToDevice, cs));
+                cudaEvent_t ev;
+                P3G_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+                evs.push_back(ev);
+                P3G_CUDA(cudaEventRecord(ev, cs));
+                // compute stream: the chunk's LDE as soon as its copy lands
+                P3G_CUDA(cudaStreamWaitEvent(st, ev, 0));
+                if (field == P3G_BABYBEAR)
+                    p3g::lde_bb(ctx, static_cast<const uint32_t*>(dev), int(tr.log_h), int(cw), int(tr.log_blowup),
+                                uint32_t(tr.shift), 1, static_cast<uint32_t*>(lde), st);
+                else
+                    p3g::lde_gl(ctx, static_cast<const uint64_t*>(dev), int(tr.log_h), int(cw), int(tr.log_blowup),
+                                tr.shift, 1, static_cast<uint64_t*>(lde), st);
+                ctx->release(dev, st);
+                pending = nullptr;
+            }
+        }
+        p3g::mmcs_build(ctx, t.get(), cap_height, st);
+        copy_cap(t.get(), h_cap_out, st);
+    } catch (...) {
+        if (cs) cudaStreamSynchronize(cs);
+        if (pending) ctx->release(pending, st);
+        p3g::tree_release(ctx, t.get(), st);
+        cleanup();
+        throw;
+    }
+    cleanup();
     *tree_out = t.release();
     API_END
 }

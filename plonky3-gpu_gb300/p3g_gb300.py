@@ -25,7 +25,7 @@ EXPORTS = [
     "p3g_stream_synchronize", "p3g_malloc", "p3g_free", "p3g_memcpy_h2d", "p3g_memcpy_d2h",
     "p3g_set_poseidon2", "p3g_poseidon2_permute", "p3g_coset_lde", "p3g_dft", "p3g_mmcs_commit",
     "p3g_commit_matrix", "p3g_tree_info", "p3g_tree_layer_ptr", "p3g_tree_leaf_ptr",
-    "p3g_mmcs_open_batch", "p3g_tree_free", "p3g_commit_traces", "p3g_fold_matrix_bb4",
+    "p3g_mmcs_open_batch", "p3g_tree_free", "p3g_commit_traces", "p3g_commit_traces_host", "p3g_fold_matrix_bb4",
     "p3g_coset_lde_bb_noalloc", "p3g_plan_commit", "p3g_plan_launch", "p3g_plan_info",
     "p3g_plan_destroy", "p3g_server_create", "p3g_server_submit", "p3g_server_poll",
     "p3g_server_pending", "p3g_server_open", "p3g_server_release", "p3g_server_destroy",
@@ -107,6 +107,7 @@ def load(path: str | None = None):
     L.p3g_mmcs_open_batch.argtypes = [vp, vp, vp, sz, vp, vp, vp]
     L.p3g_tree_free.argtypes = [vp, vp, vp]
     L.p3g_commit_traces.argtypes = [vp, i32, C.POINTER(Trace), sz, u32, C.POINTER(vp), vp, vp]
+    L.p3g_commit_traces_host.argtypes = [vp, i32, C.POINTER(Trace), sz, u32, C.POINTER(vp), vp, vp]
     L.p3g_fold_matrix_bb4.argtypes = [vp, vp, u32, u32, vp, vp, vp]
     L.p3g_coset_lde_bb_noalloc.argtypes = [vp, u32, u32, u32, u32, i32, vp, vp]
     L.p3g_plan_commit.argtypes = [vp, i32, C.POINTER(Trace), sz, u32, C.POINTER(FoldJob), u32, C.POINTER(vp)]
@@ -484,6 +485,17 @@ class Context:
         t = C.c_void_p()
         capp = _np_ptr(cap_out) if cap_out is not None else None
         check(load().p3g_commit_traces(self.handle, field, arr, len(traces), cap_height, C.byref(t), capp, stream))
+        return Tree(self, t.value, field)
+
+    def commit_traces_host(self, field: int, traces, cap_height: int = 0, stream=None,
+                           cap_out: np.ndarray | None = None) -> Tree:
+        """traces: list of (host_ptr, log_h, width, log_blowup, shift); host
+        memory should be pinned for the copies to overlap the LDEs."""
+        arr = (Trace * len(traces))(*[Trace(p, lh, w, lb, 0, s) for (p, lh, w, lb, s) in traces])
+        t = C.c_void_p()
+        capp = _np_ptr(cap_out) if cap_out is not None else None
+        check(load().p3g_commit_traces_host(self.handle, field, arr, len(traces), cap_height, C.byref(t), capp,
+                                            stream))
         return Tree(self, t.value, field)
 
     # -- FRI

@@ -1,0 +1,66 @@
+"""p3g_commit_traces_host: traces in host memory, copied in 512-byte column
+chunks on a second stream while earlier chunks' LDEs run.  The commitment and
+every opening must equal p3g_commit_traces on the same traces (and the
+oracle's), whatever the chunking."""
+import numpy as np
+import pytest
+
+import oracle as O
+import p3g_gb300 as P
+
+pytestmark = pytest.mark.gpu
+
+
+def _shapes_bb():
+    return [(12, 300), (12, 128), (10, 7), (12, 129), (9, 256)]
+
+
+def test_host_commit_matches_device_commit_and_oracle(gpu_ctx):
+    rng = np.random.default_rng(61)
+    traces = [rng.integers(0, O.BB_P, size=(1 << lh, w), dtype=np.uint32) for lh, w in _shapes_bb()]
+    bufs = [gpu_ctx.to_device(t) for t in traces]
+    dev = gpu_ctx.commit_traces_device(P.BABYBEAR, [(b.ptr, t.shape[0].bit_length() - 1, t.shape[1], 1, 31)
+                                                    for b, t in zip(bufs, traces)], 1)
+    cap = np.zeros((2, 8), np.uint32)
+    host = gpu_ctx.commit_traces_host(P.BABYBEAR, [(t.ctypes.data, t.shape[0].bit_length() - 1, t.shape[1], 1, 31)
+                                                   for t in traces], 1, cap_out=cap)
+    want = O.mmcs_commit(O.bb16_params(), [O.bb_coset_lde(t, 1, 31, True) for t in traces], 1)
+    got_h, got_d = host.layers(), dev.layers()
+    assert len(got_h) == len(want)
+    for a, b, c in zip(got_h, got_d, want):
+        assert np.array_equal(a, c)
+        assert np.array_equal(b, c)
+    assert np.array_equal(cap, want[-1])
+    # openings: same concatenated rows and the same sibling paths
+    idx = np.array([0, 1, 777, 4095, 8191], dtype=np.uint64)
+    total_w = sum(t.shape[1] for t in traces)
+    rows_h, proof_h = host.open_batch(idx, total_w)
+    rows_d, proof_d = dev.open_batch(idx, total_w)
+    assert np.array_equal(rows_h, rows_d)
+    assert np.array_equal(proof_h, proof_d)
+    host.free()
+    dev.free()
+    for b in bufs:
+        b.free()
+
+
+def test_host_commit_goldilocks_and_zero_width(gpu_ctx):
+    rng = np.random.default_rng(62)
+    shapes = [(10, 100), (10, 0), (8, 64), (10, 3)]
+    traces = [rng.integers(0, O.GL_P, size=(1 << lh, w), dtype=np.uint64) for lh, w in shapes]
+    host = gpu_ctx.commit_traces_host(P.GOLDILOCKS, [(t.ctypes.data if t.size else 0, lh, w, 2, 7)
+                                                     for t, (lh, w) in zip(traces, shapes)], 0)
+    want = O.mmcs_commit(O.gl8_params(), [O.gl_coset_lde(t, 2, 7, True) if t.size else
+                                          np.zeros((1 << (lh + 2), 0), np.uint64)
+                                          for t, (lh, w) in zip(traces, shapes)], 0)
+    for a, c in zip(host.layers(), want):
+        assert np.array_equal(a, c)
+    host.free()
+
+
+def test_host_commit_rejects_bad_arguments(gpu_ctx):
+    with pytest.raises(P.P3GError):
+        gpu_ctx.commit_traces_host(P.BABYBEAR, [(0, 4, 4, 1, 31)], 0)  # null trace
+    t = np.zeros((16, 4), np.uint32)
+    with pytest.raises(P.P3GError):
+        gpu_ctx.commit_traces_host(P.BABYBEAR, [(t.ctypes.data, 4, 4, 1, P.BB_P)], 0)  # shift not canonical
