@@ -305,6 +305,31 @@ P3G_API int p3g_fold_matrix_bb4(p3g_ctx *ctx, const void *d_in, uint32_t log_hei
                         uint32_t log_arity, const uint32_t h_beta[4], void *d_out,
                         void *stream);
 
+/* ------------------------------------------------------------ PCS open
+ * TwoAdicFriPcs::open's two passes over a BabyBear LDE resident on the device
+ * (two_adic_fri_pcs.hpp:271-410).  d_lde: (1 << log_n) x width evaluations on
+ * the coset shift * <omega_n>, rows in natural order or, if bitrev_rows, in
+ * bit-reversed order (as p3g_commit_traces leaves them); 1 to 4 BabyBear^4
+ * points (h_points: n_points x 4 canonical u32).
+ *
+ * Opened values, by barycentric interpolation (compute_diff_invs and
+ * interpolate_coset_with_precomputation, interpolation.hpp:93-180):
+ * h_out[p][c] (n_points x width x 4) = column c's polynomial at point p.
+ * Synchronises the stream. */
+P3G_API int p3g_pcs_open_values(p3g_ctx *ctx, const void *d_lde, uint32_t log_n, uint32_t width, int bitrev_rows,
+                                uint32_t shift, const uint32_t *h_points, uint32_t n_points, uint32_t *h_out,
+                                void *stream);
+/* The reduced opening of one matrix (two_adic_fri_pcs.hpp:350-410), added in
+ * place to d_q ((1 << log_n) x 4 BabyBear^4 on the device):
+ *   q[k] += sum_p sum_c alpha^(alpha_pow + p*width + c)
+ *                       * (opened[p][c] - lde[k][c]) / (z_p - shift * omega_n^k),
+ * k the natural row index; q[k] is stored at k, or at bitrev(k) if q_bitrev
+ * (the order prove_fri takes).  h_opened: n_points x width x 4 from
+ * p3g_pcs_open_values; n_points * width <= 10240. */
+P3G_API int p3g_pcs_reduce(p3g_ctx *ctx, const void *d_lde, uint32_t log_n, uint32_t width, int bitrev_rows,
+                           uint32_t shift, const uint32_t *h_points, uint32_t n_points, const uint32_t *h_opened,
+                           const uint32_t h_alpha[4], uint64_t alpha_pow, int q_bitrev, void *d_q, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

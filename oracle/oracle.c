@@ -701,3 +701,122 @@ int orc_fold_matrix_bb4(const uint32_t *in, unsigned log_height, unsigned log_ar
     orc_parallel(n, nthreads, orc_fold_range, &x);
     return 0;
 }
+
+/* ======================================================================== */
+/* PCS open: opened values and the reduced-opening vector (test oracle)     */
+/* ======================================================================== */
+static void bb4_add(const uint32_t a[4], const uint32_t b[4], uint32_t out[4]) {
+    for (int i = 0; i < 4; ++i) out[i] = orc_bb_add(a[i], b[i]);
+}
+static void bb4_scale(const uint32_t a[4], uint32_t s, uint32_t out[4]) {
+    for (int i = 0; i < 4; ++i) out[i] = orc_bb_mul(a[i], s);
+}
+static void bb4_pow(const uint32_t a[4], uint64_t e, uint32_t out[4]) {
+    uint32_t r[4] = {1, 0, 0, 0}, b[4] = {a[0], a[1], a[2], a[3]};
+    while (e) {
+        if (e & 1) orc_bb4_mul(r, b, r);
+        orc_bb4_mul(b, b, b);
+        e >>= 1;
+    }
+    memcpy(out, r, sizeof r);
+}
+
+typedef struct {
+    const uint32_t *lde;
+    unsigned log_n;
+    size_t w;
+    uint32_t shift;
+    const uint32_t *z;
+    uint32_t *partial; /* per row block: w x 4 partial sums */
+    size_t block;
+} orc_open_ctx;
+
+/* rows [b*block, (b+1)*block) of sum_i d_i f_i / (z - g h_i) */
+static void orc_open_range(void *vx, size_t b0, size_t b1) {
+    orc_open_ctx *x = (orc_open_ctx *)vx;
+    const size_t n = (size_t)1 << x->log_n;
+    const uint32_t om = orc_bb_two_adic_generator(x->log_n);
+    /* common_inv = 1 / (n g^(n-1)) (interpolation.hpp compute_diff_invs) */
+    const uint32_t common_inv = orc_bb_inv(orc_bb_mul((uint32_t)(n % ORC_BB_P), orc_bb_pow(x->shift, n - 1)));
+    for (size_t b = b0; b < b1; ++b) {
+        uint32_t *acc = x->partial + b * x->w * 4;
+        memset(acc, 0, x->w * 4 * sizeof(uint32_t));
+        const size_t r0 = b * x->block, r1 = r0 + x->block < n ? r0 + x->block : n;
+        uint32_t h = orc_bb_pow(om, r0);
+        for (size_t i = r0; i < r1; ++i) {
+            const uint32_t d = orc_bb_mul(h, common_inv);
+            uint32_t diff[4] = {orc_bb_sub(x->z[0], orc_bb_mul(x->shift, h)), x->z[1], x->z[2], x->z[3]}, inv[4];
+            orc_bb4_inv(diff, inv);
+            for (size_t c = 0; c < x->w; ++c) {
+                uint32_t t[4];
+                bb4_scale(inv, orc_bb_mul(x->lde[i * x->w + c], d), t);
+                bb4_add(acc + 4 * c, t, acc + 4 * c);
+            }
+            h = orc_bb_mul(h, om);
+        }
+    }
+}
+
+void orc_pcs_open_values(const uint32_t *lde, unsigned log_n, size_t w, uint32_t shift,
+                         const uint32_t z[4], uint32_t *out, int nthreads) {
+    const size_t n = (size_t)1 << log_n, block = 256;
+    const size_t nb = (n + block - 1) / block;
+    uint32_t *partial = (uint32_t *)malloc(nb * w * 4 * sizeof(uint32_t));
+    orc_open_ctx x = {lde, log_n, w, shift, z, partial, block};
+    orc_parallel(nb, nthreads, orc_open_range, &x);
+    /* vanishing factor z^n - g^n */
+    uint32_t van[4];
+    bb4_pow(z, n, van);
+    van[0] = orc_bb_sub(van[0], orc_bb_pow(shift, n));
+    for (size_t c = 0; c < w; ++c) {
+        uint32_t s[4] = {0, 0, 0, 0};
+        for (size_t b = 0; b < nb; ++b) bb4_add(s, partial + (b * w + c) * 4, s);
+        orc_bb4_mul(van, s, out + 4 * c);
+    }
+    free(partial);
+}
+
+typedef struct {
+    const uint32_t *lde;
+    unsigned log_n;
+    size_t w;
+    uint32_t shift;
+    const uint32_t *z;
+    size_t m;
+    const uint32_t *opened;
+    const uint32_t *apow; /* m*w alpha powers */
+    uint32_t *q;
+} orc_reduce_ctx;
+
+static void orc_reduce_range(void *vx, size_t k0, size_t k1) {
+    orc_reduce_ctx *x = (orc_reduce_ctx *)vx;
+    const uint32_t om = orc_bb_two_adic_generator(x->log_n);
+    uint32_t xk = orc_bb_mul(x->shift, orc_bb_pow(om, k0));
+    for (size_t k = k0; k < k1; ++k) {
+        for (size_t p = 0; p < x->m; ++p) {
+            const uint32_t *zp = x->z + 4 * p;
+            uint32_t diff[4] = {orc_bb_sub(zp[0], xk), zp[1], zp[2], zp[3]}, dinv[4];
+            orc_bb4_inv(diff, dinv);
+            for (size_t c = 0; c < x->w; ++c) {
+                const uint32_t *fz = x->opened + 4 * (p * x->w + c);
+                uint32_t numer[4] = {orc_bb_sub(fz[0], x->lde[k * x->w + c]), fz[1], fz[2], fz[3]}, t[4];
+                orc_bb4_mul(x->apow + 4 * (p * x->w + c), numer, t);
+                orc_bb4_mul(t, dinv, t);
+                bb4_add(x->q + 4 * k, t, x->q + 4 * k);
+            }
+        }
+        xk = orc_bb_mul(xk, om);
+    }
+}
+
+void orc_pcs_reduce(const uint32_t *lde, unsigned log_n, size_t w, uint32_t shift,
+                    const uint32_t *z, size_t m, const uint32_t *opened, const uint32_t alpha[4],
+                    uint64_t ap0, uint32_t *q, int nthreads) {
+    const size_t n = (size_t)1 << log_n;
+    uint32_t *apow = (uint32_t *)malloc((m * w + 1) * 4 * sizeof(uint32_t));
+    bb4_pow(alpha, ap0, apow);
+    for (size_t i = 1; i < m * w; ++i) orc_bb4_mul(apow + 4 * (i - 1), alpha, apow + 4 * i);
+    orc_reduce_ctx x = {lde, log_n, w, shift, z, m, opened, apow, q};
+    orc_parallel(n, nthreads, orc_reduce_range, &x);
+    free(apow);
+}

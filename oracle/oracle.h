@@ -113,6 +113,21 @@ int orc_commit_matrix(const orc_p2 *p, const void *flat, size_t height, size_t w
 int orc_fold_matrix_bb4(const uint32_t *in, unsigned log_height, unsigned log_arity,
                         const uint32_t beta[4], uint32_t *out, int nthreads);
 
+/* ---------------- PCS open ---------------- */
+/* Opened values of one LDE matrix at point z, as TwoAdicFriPcs::open computes
+ * them (two_adic_fri_pcs.hpp:296-335) with compute_diff_invs and
+ * interpolate_coset_with_precomputation (interpolation.hpp:93-180):
+ *   f(z) = (z^n - g^n) * sum_i d_i * f_i / (z - g h_i),  d_i = h_i / (n g^(n-1)),
+ * h_i = omega_n^i; lde: n x w canonical, natural row order; out: w BB4. */
+void orc_pcs_open_values(const uint32_t *lde, unsigned log_n, size_t w, uint32_t shift,
+                         const uint32_t z[4], uint32_t *out, int nthreads);
+/* The reduced-opening accumulation of one matrix (two_adic_fri_pcs.hpp:350-410):
+ *   q[k] += sum_p sum_c alpha^(ap0 + p*w + c) * (opened[p][c] - lde[k][c]) / (z_p - g omega_n^k)
+ * for k < n (natural order), m points z (m x 4), opened m x w BB4. */
+void orc_pcs_reduce(const uint32_t *lde, unsigned log_n, size_t w, uint32_t shift,
+                    const uint32_t *z, size_t m, const uint32_t *opened, const uint32_t alpha[4],
+                    uint64_t ap0, uint32_t *q, int nthreads);
+
 #ifdef __cplusplus
 }
 #endif

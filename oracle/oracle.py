@@ -67,6 +67,10 @@ def lib():
         L.orc_bb_inv.argtypes = [u32]
         L.orc_bb_two_adic_generator.restype = u32
         L.orc_bb_two_adic_generator.argtypes = [C.c_uint]
+        L.orc_pcs_open_values.restype = None
+        L.orc_pcs_open_values.argtypes = [vp, C.c_uint, sz, u32, vp, vp, i32]
+        L.orc_pcs_reduce.restype = None
+        L.orc_pcs_reduce.argtypes = [vp, C.c_uint, sz, u32, vp, sz, vp, vp, u64, vp, i32]
         for n in ("orc_gl_add", "orc_gl_sub", "orc_gl_mul"):
             getattr(L, n).restype = u64
             getattr(L, n).argtypes = [u64, u64]
@@ -395,3 +399,28 @@ def bb4_inv(a):
     o = np.zeros(4, np.uint32)
     lib().orc_bb4_inv(_ptr(x), _ptr(o))
     return o
+
+
+# ------------------------------------------------------------------ PCS open
+def pcs_open_values(lde: np.ndarray, shift: int, z, nthreads: int = 1) -> np.ndarray:
+    """Opened values of an n x w natural-order LDE at BB4 point z (w x 4)."""
+    m = np.ascontiguousarray(lde, dtype=np.uint32)
+    n, w = m.shape
+    zz = np.asarray(z, dtype=np.uint32).reshape(4)
+    out = np.zeros((w, 4), dtype=np.uint32)
+    lib().orc_pcs_open_values(_ptr(m), n.bit_length() - 1, w, shift, _ptr(zz), _ptr(out), nthreads)
+    return out
+
+
+def pcs_reduce(lde: np.ndarray, shift: int, zs, opened, alpha, ap0: int, q: np.ndarray,
+               nthreads: int = 1) -> np.ndarray:
+    """Adds one matrix's reduced-opening terms into q (n x 4, natural order)."""
+    m = np.ascontiguousarray(lde, dtype=np.uint32)
+    n, w = m.shape
+    z = np.ascontiguousarray(zs, dtype=np.uint32).reshape(-1, 4)
+    ov = np.ascontiguousarray(opened, dtype=np.uint32).reshape(z.shape[0], w, 4)
+    a = np.asarray(alpha, dtype=np.uint32).reshape(4)
+    assert q.dtype == np.uint32 and q.shape == (n, 4) and q.flags.c_contiguous
+    lib().orc_pcs_reduce(_ptr(m), n.bit_length() - 1, w, shift, _ptr(z), z.shape[0], _ptr(ov), _ptr(a), ap0,
+                         _ptr(q), nthreads)
+    return q

@@ -4,9 +4,11 @@
 // reference's unmodified headers (dloghin/plonky3-gpu, src/include) into
 // oracle/_ref/ref_driver; tests/golden/make_golden.py runs it and commits the
 // resulting fixtures.  The only code of this file's own is argument parsing,
-// seeded input generation in the reference tests' convention, and one traits
-// specialisation: the reference's Goldilocks has no two-adic generator, so
-// the harness supplies omega_{2^k} = 7^((p-1)/2^k) (7 generates F_p^*).
+// seeded input generation in the reference tests' convention, a transcript
+// adapter over the reference's DuplexChallenger (the member functions that
+// TwoAdicFriPcs::open and prove_fri call), and one traits specialisation: the
+// reference's Goldilocks has no two-adic generator, so the harness supplies
+// omega_{2^k} = 7^((p-1)/2^k) (7 generates F_p^*).
 //
 // Output: raw little-endian canonical field elements written to <out>.
 
@@ -28,6 +30,7 @@
 #include "fri_folding.hpp"
 #include "fri_params.hpp"
 #include "two_adic_fri_pcs.hpp"
+#include "duplex_challenger.hpp"
 
 #include <cstdio>
 #include <cstdlib>
@@ -110,6 +113,24 @@ using SpongeGL = p3_symmetric::PaddingFreeSponge<WrapGL, GL, 8, 4, 4>;
 using TruncGL = p3_symmetric::TruncatedPermutation<WrapGL, GL, 2, 4, 8>;
 using MmcsGL = p3_merkle_tree::MerkleTreeMmcs<GL, GL, SpongeGL, TruncGL, 4>;
 using FlatBB = p3_merkle::MerkleTreeMmcs<BB, BB, SpongeBB, TruncBB, 2, 8>;
+
+// The transcript TwoAdicFriPcs::open and prove_fri drive (fri_prover.hpp,
+// two_adic_fri_pcs.hpp:271-510), over the reference's DuplexChallenger with
+// the seeded BB16 permutation.
+struct OpenTranscript {
+    p3_challenger::DuplexChallenger<BB, WrapBB, 16, 8> d;
+    explicit OpenTranscript(WrapBB w) : d(std::move(w)) {}
+    template <typename C>
+    void observe_commitment(const C& c) { d.observe_merkle_cap(c); }
+    template <typename EF = BabyBear4>
+    EF sample_challenge() { return d.template sample_algebra_element<EF>(); }
+    template <typename EF>
+    void observe_challenge(const EF& v) { d.template observe_algebra_element<EF>(v); }
+    void observe_arity(size_t la) { d.observe(BB(static_cast<uint32_t>(la))); }
+    uint64_t grind(size_t bits) { return d.grind(bits); }
+    bool check_witness(size_t bits, uint64_t w) { return d.check_witness(bits, w); }
+    size_t sample_bits(size_t n) { return d.sample_bits(n); }
+};
 
 // ---------------------------------------------------------------------------
 // output helpers
@@ -348,6 +369,47 @@ int main(int argc, char** argv) {
         MmcsBB mmcs(SpongeBB(WrapBB{make_pos_bb()}), TruncBB(WrapBB{make_pos_bb()}), cap);
         auto [c, tree] = mmcs.commit(std::move(mats));
         put_layers(tree);
+    } else if (cmd == "pcs_open") {
+        // pcs_open <seed> <log_h>x<w> ... : TwoAdicFriPcs::commit as in pcs_commit, then
+        // open every matrix at one point zeta sampled from the transcript.  Writes zeta,
+        // alpha (the first challenge open samples), every opened value, the number of
+        // FRI commit-phase rounds, the log arity of round 0 and its commitment (the
+        // Merkle root of the bit-reversed reduced-opening vector of the tallest height).
+        uint64_t seed = strtoull(argv[3], 0, 0);
+        auto shapes = parse_shapes(argc, argv, 4);
+        using EFMmcs = p3_merkle::ExtensionMmcs<BB, BabyBear4, FlatBB>;
+        using Pcs = p3_fri::TwoAdicFriPcs<BB, BabyBear4, p3_dft::Radix2Dit<BB>, FlatBB, EFMmcs>;
+        auto mk = [] { return FlatBB(SpongeBB(WrapBB{make_pos_bb()}), TruncBB(WrapBB{make_pos_bb()})); };
+        p3_fri::FriParameters<EFMmcs> fri{1, 0, 1, 10, 0, 8, EFMmcs(mk())};
+        Pcs pcs(p3_dft::Radix2Dit<BB>(), mk(), std::move(fri));
+        std::vector<std::pair<typename Pcs::Domain, RowMajorMatrix<BB>>> ev;
+        size_t max_log = 0;
+        for (size_t i = 0; i < shapes.size(); ++i) {
+            typename Pcs::Domain d;
+            d.log_n = shapes[i].first;
+            d.shift = BB::one_val();
+            ev.push_back({d, rand_matrix<BB>(size_t(1) << shapes[i].first, shapes[i].second, seed + i)});
+            max_log = std::max(max_log, shapes[i].first + 1);
+        }
+        auto [commit, pd] = pcs.commit(std::move(ev));
+        OpenTranscript tr(WrapBB{make_pos_bb()});
+        tr.observe_commitment(commit);
+        const BabyBear4 zeta = tr.sample_challenge<BabyBear4>();
+        OpenTranscript peek = tr;
+        const BabyBear4 alpha = peek.sample_challenge<BabyBear4>();
+        std::vector<std::vector<BabyBear4>> points(shapes.size(), std::vector<BabyBear4>{zeta});
+        std::vector<std::pair<const typename Pcs::PcsProverData*, std::vector<std::vector<BabyBear4>>>> od;
+        od.push_back({&pd, points});
+        auto [opened, proof] = pcs.open(od, tr);
+        for (size_t k = 0; k < 4; ++k) put(zeta[k]);
+        for (size_t k = 0; k < 4; ++k) put(alpha[k]);
+        for (const auto& mat : opened[0])
+            for (const auto& pt : mat)
+                for (const auto& v : pt)
+                    for (size_t k = 0; k < 4; ++k) put(v[k]);
+        put32(uint32_t(proof.commit_phase_commits.size()));
+        put32(uint32_t(p3_fri::compute_log_arity_for_round(max_log, false, 0, 1, 1)));
+        for (const auto& e : proof.commit_phase_commits.at(0)[0]) put(e);
     } else if (cmd == "pcs_commit") {
         // pcs_commit <seed> <log_h>x<w> ... : TwoAdicFriPcs::commit (log_blowup 1,
         // domain shift 1 as in fri_test.cpp) with the seeded BB16 Poseidon2.

@@ -524,6 +524,27 @@ int p3g_commit_traces_host(p3g_ctx* ctx, int field, const p3g_trace* traces, siz
     API_END
 }
 
+int p3g_pcs_open_values(p3g_ctx* ctx, const void* d_lde, uint32_t log_n, uint32_t width, int bitrev_rows,
+                        uint32_t shift, const uint32_t* h_points, uint32_t n_points, uint32_t* h_out, void* stream) {
+    API_BEGIN
+    P3G_REQUIRE(ctx && d_lde && h_points && h_out, "pcs_open_values: null argument");
+    DeviceGuard g(ctx->device);
+    p3g::pcs_open_values(ctx, static_cast<const uint32_t*>(d_lde), int(log_n), int(width), bitrev_rows, shift,
+                         h_points, int(n_points), h_out, S(stream));
+    API_END
+}
+
+int p3g_pcs_reduce(p3g_ctx* ctx, const void* d_lde, uint32_t log_n, uint32_t width, int bitrev_rows, uint32_t shift,
+                   const uint32_t* h_points, uint32_t n_points, const uint32_t* h_opened, const uint32_t h_alpha[4],
+                   uint64_t alpha_pow, int q_bitrev, void* d_q, void* stream) {
+    API_BEGIN
+    P3G_REQUIRE(ctx && d_lde && h_points && h_opened && h_alpha && d_q, "pcs_reduce: null argument");
+    DeviceGuard g(ctx->device);
+    p3g::pcs_reduce(ctx, static_cast<const uint32_t*>(d_lde), int(log_n), int(width), bitrev_rows, shift, h_points,
+                    int(n_points), h_opened, h_alpha, alpha_pow, q_bitrev, static_cast<uint32_t*>(d_q), S(stream));
+    API_END
+}
+
 int p3g_fold_matrix_bb4(p3g_ctx* ctx, const void* d_in, uint32_t log_height, uint32_t log_arity,
                         const uint32_t h_beta[4], void* d_out, void* stream) {
     API_BEGIN

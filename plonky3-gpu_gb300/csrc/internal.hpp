@@ -131,6 +131,12 @@ namespace p3g {
 // (implemented in lde.cu, merkle.cu, fold.cu; called by capi.cu)
 void lde_bb(p3g_ctx* ctx, const uint32_t* in, int log_h, int w, int log_b, uint32_t shift,
             int bitrev_out, uint32_t* out, cudaStream_t st);
+// TwoAdicFriPcs::open's opened values and reduced opening over a resident LDE (open.cu)
+void pcs_open_values(p3g_ctx* ctx, const uint32_t* lde, int log_n, int w, int bitrev_rows, uint32_t shift,
+                     const uint32_t* h_points, int m, uint32_t* h_out, cudaStream_t st);
+void pcs_reduce(p3g_ctx* ctx, const uint32_t* lde, int log_n, int w, int bitrev_rows, uint32_t shift,
+                const uint32_t* h_points, int m, const uint32_t* h_opened, const uint32_t* h_alpha, uint64_t alpha_pow,
+                int q_bitrev, uint32_t* q, cudaStream_t st);
 // device copies of the prepared DFT twiddle tables (cudaMalloc'd; the context frees them)
 void* make_dft_tw_bb();
 void* make_dft_tw_gl();

@@ -29,6 +29,7 @@ EXPORTS = [
     "p3g_coset_lde_bb_noalloc", "p3g_plan_commit", "p3g_plan_launch", "p3g_plan_info",
     "p3g_plan_destroy", "p3g_server_create", "p3g_server_submit", "p3g_server_poll",
     "p3g_server_pending", "p3g_server_open", "p3g_server_release", "p3g_server_destroy",
+    "p3g_pcs_open_values", "p3g_pcs_reduce",
 ]
 
 
@@ -121,6 +122,8 @@ def load(path: str | None = None):
     L.p3g_server_open.argtypes = [vp, u64, vp, sz, vp, vp]
     L.p3g_server_release.argtypes = [vp, u64]
     L.p3g_server_destroy.argtypes = [vp]
+    L.p3g_pcs_open_values.argtypes = [vp, vp, u32, u32, i32, u32, vp, u32, vp, vp]
+    L.p3g_pcs_reduce.argtypes = [vp, vp, u32, u32, i32, u32, vp, u32, vp, vp, u64, i32, vp, vp]
     for name in EXPORTS:
         if name not in ("p3g_version", "p3g_status_string", "p3g_kernel_launches"):
             getattr(L, name).restype = i32
@@ -478,6 +481,12 @@ class Context:
                                        None, None))
         return Tree(self, t.value, field), buf
 
+    def commit_matrix_device(self, field: int, d_flat: int, height: int, width: int, stream=None) -> Tree:
+        """Flat MMCS commit_matrix of a device matrix (height x width)."""
+        t = C.c_void_p()
+        check(load().p3g_commit_matrix(self.handle, field, d_flat, height, width, C.byref(t), None, stream))
+        return Tree(self, t.value, field)
+
     def commit_traces_device(self, field: int, traces, cap_height: int = 0, stream=None,
                              cap_out: np.ndarray | None = None) -> Tree:
         """traces: list of (device_ptr, log_h, width, log_blowup, shift)."""
@@ -497,6 +506,25 @@ class Context:
         check(load().p3g_commit_traces_host(self.handle, field, arr, len(traces), cap_height, C.byref(t), capp,
                                             stream))
         return Tree(self, t.value, field)
+
+    # -- PCS open
+    def pcs_open_values_device(self, d_lde: int, log_n: int, width: int, bitrev_rows: bool, shift: int, points,
+                               stream=None) -> np.ndarray:
+        """Opened values (n_points x width x 4) of a resident BabyBear LDE."""
+        pts = np.ascontiguousarray(points, dtype=np.uint32).reshape(-1, 4)
+        out = np.zeros((pts.shape[0], width, 4), dtype=np.uint32)
+        check(load().p3g_pcs_open_values(self.handle, d_lde, log_n, width, int(bitrev_rows), shift, _np_ptr(pts),
+                                         pts.shape[0], _np_ptr(out), stream))
+        return out
+
+    def pcs_reduce_device(self, d_lde: int, log_n: int, width: int, bitrev_rows: bool, shift: int, points, opened,
+                          alpha, alpha_pow: int, q_bitrev: bool, d_q: int, stream=None):
+        """Adds one matrix's reduced opening into the device vector d_q (2^log_n x 4)."""
+        pts = np.ascontiguousarray(points, dtype=np.uint32).reshape(-1, 4)
+        ov = np.ascontiguousarray(opened, dtype=np.uint32).reshape(pts.shape[0], width, 4)
+        a = np.ascontiguousarray(alpha, dtype=np.uint32).reshape(4)
+        check(load().p3g_pcs_reduce(self.handle, d_lde, log_n, width, int(bitrev_rows), shift, _np_ptr(pts),
+                                    pts.shape[0], _np_ptr(ov), _np_ptr(a), alpha_pow, int(q_bitrev), d_q, stream))
 
     # -- FRI
     def fold_matrix_bb4_device(self, d_in: int, log_height: int, log_arity: int, beta, d_out: int,

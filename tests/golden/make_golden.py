@@ -3,8 +3,9 @@
 
 oracle/_ref/ref_driver is compiled (``make -C oracle ref``) from the
 reference's unmodified headers (dloghin/plonky3-gpu, src/include) plus
-oracle/ref_driver.cpp, which only parses arguments and draws seeded inputs in
-the reference tests' convention (std::mt19937(seed), ``rng() % p``).  This
+oracle/ref_driver.cpp, which parses arguments, draws seeded inputs in the
+reference tests' convention (std::mt19937(seed), ``rng() % p``) and adapts the
+reference's DuplexChallenger for TwoAdicFriPcs::open.  This
 script runs it over a fixed list of cases and stores the outputs: small
 arrays in full, large ones as a SHA-256 of their little-endian bytes plus the
 leading values.  Needs the reference sources, so it runs only where they are
@@ -171,6 +172,16 @@ def main() -> int:
         raw = np.frombuffer(run("pcs_commit", seed, *shapes), np.uint32)
         pcs.append({"seed": seed, "shapes": shapes, "log_blowup": 1, "shift": 1, "root": raw.tolist()})
     g["pcs_commit"] = pcs
+
+    opens = []
+    for seed, shapes in ((3, ["5x16", "8x16", "7x16"]), (11, ["6x5", "6x3"]), (12, ["9x2", "4x7"])):
+        raw = np.frombuffer(run("pcs_open", seed, *shapes), np.uint32)
+        n_open = sum(int(s.split("x")[1]) for s in shapes) * 4
+        opens.append({"seed": seed, "shapes": shapes, "log_blowup": 1, "shift": 1,
+                      "zeta": raw[0:4].tolist(), "alpha": raw[4:8].tolist(),
+                      "opened": raw[8:8 + n_open].tolist(), "fri_rounds": int(raw[8 + n_open]),
+                      "log_arity0": int(raw[9 + n_open]), "commit0": raw[10 + n_open:18 + n_open].tolist()})
+    g["pcs_open"] = opens
 
     folds = []
     for (lh, la, seed, mode) in ((4, 1, 0xDEADBEEF, 0), (6, 1, 71, 0), (10, 1, 72, 0), (5, 2, 73, 0),

@@ -293,3 +293,41 @@ def test_mmcs_verify_batch_against_reference_trees(golden):
                 bad = [r.copy() for r in rows]
                 bad[0][0] ^= 1
                 assert not O.mmcs_verify_batch(p, layers[-1], heights, [m.shape[1] for m in mats], index, bad, proof)
+
+
+# ---------------------------------------------------------------- PCS open
+def _bitrev_rows(a):
+    n = a.shape[0]
+    bits = n.bit_length() - 1
+    idx = [int(format(i, f"0{bits}b")[::-1], 2) if bits else 0 for i in range(n)]
+    return a[idx]
+
+
+def pcs_open_case(case, open_values=None, reduce=None):
+    """Opened values and the first FRI commitment of TwoAdicFriPcs::open for one
+    golden case, from the restated formulas (or the functions passed in)."""
+    open_values = open_values or (lambda lde, z: O.pcs_open_values(lde, case["shift"], z))
+    reduce = reduce or (lambda lde, z, ov, ap, q: O.pcs_reduce(lde, case["shift"], [z], ov[None], case["alpha"],
+                                                               ap, q))
+    shapes = [tuple(int(v) for v in s.split("x")) for s in case["shapes"]]
+    traces = [O.bb_random_matrix(1 << lh, w, case["seed"] + i) for i, (lh, w) in enumerate(shapes)]
+    ldes = [O.bb_coset_lde(t, case["log_blowup"], case["shift"], bitrev=False) for t in traces]
+    z = case["zeta"]
+    opened = [open_values(l, z) for l in ldes]
+    qs, ap = {}, 0
+    for lde, ov in zip(ldes, opened):
+        q = qs.setdefault(lde.shape[0], np.zeros((lde.shape[0], 4), np.uint32))
+        reduce(lde, z, ov, ap, q)
+        ap += lde.shape[1]
+    tallest = max(qs)
+    arity = 1 << case["log_arity0"]
+    flat = _bitrev_rows(qs[tallest]).reshape(tallest // arity, arity * 4)
+    root = O.commit_matrix(O.bb16_params(), flat)[-1][0]
+    return np.concatenate([o.reshape(-1) for o in opened]), root, ldes, qs
+
+
+def test_pcs_open_vs_reference(golden):
+    for case in golden["pcs_open"]:
+        opened, root, _, _ = pcs_open_case(case)
+        assert opened.tolist() == case["opened"]
+        assert root.tolist() == case["commit0"]
