@@ -467,6 +467,33 @@ def run_ours(args):
     torch.cuda.synchronize(dev)
     e2e_value, e2e_mean = job_throughput(float(elems), statistics.mean(e2e_ms), dev)
 
+    # ---- PCS open on the commit's resident bit-reversed LDE (2^21 x 256):
+    # opened values at 2 points and the reduced opening into a q vector
+    tree = ctx.commit_traces_device(P.BABYBEAR, [(d_trace.ptr, LOG_H, WIDTH, LOG_B, SHIFT)], 0, stream=sptr)
+    log_n = LOG_H + LOG_B
+    pts = rng.integers(0, BB_P, size=(2, 4), dtype=np.uint32)
+    alpha = rng.integers(0, BB_P, size=4, dtype=np.uint32)
+    d_q = ctx.alloc(H * 16, sptr)
+    ov = ctx.pcs_open_values_device(tree.leaf_ptr(0), log_n, WIDTH, True, SHIFT, pts, stream=sptr)
+    ctx.pcs_reduce_device(tree.leaf_ptr(0), log_n, WIDTH, True, SHIFT, pts, ov, alpha, 0, True, d_q.ptr, sptr)
+    torch.cuda.synchronize(dev)
+    open_reps = 5
+    e0.record(stream)
+    for _ in range(open_reps):
+        ctx.pcs_open_values_device(tree.leaf_ptr(0), log_n, WIDTH, True, SHIFT, pts, stream=sptr)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    open_ms = e0.elapsed_time(e1) / open_reps
+    e0.record(stream)
+    for _ in range(open_reps):
+        ctx.pcs_reduce_device(tree.leaf_ptr(0), log_n, WIDTH, True, SHIFT, pts, ov, alpha, 0, True, d_q.ptr, sptr)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    reduce_ms = e0.elapsed_time(e1) / open_reps
+    d_q.free(sptr)
+    tree.free(sptr)
+    torch.cuda.synchronize(dev)
+
     # ---- permutation ceiling: the same Poseidon2-16 on 2^22 register-resident
     # states (p3g_poseidon2_permute), no sponge or tree around it
     n_states = 1 << 22
@@ -519,6 +546,12 @@ def run_ours(args):
                      "peak_source": src, "algorithmic_bytes": lde_bytes, "ms": lde_ms},
         "stages": {"lde_ms": lde_ms, "merkle_ms": hash_ms, "perms": perms,
                    "perms_per_s": perms / (hash_ms / 1e3) if hash_ms > 0 else None},
+        "pcs_open": {"workload": f"TwoAdicFriPcs::open passes on the resident bit-reversed LDE 2^{LOG_H + LOG_B} x "
+                                 f"{WIDTH}, 2 BabyBear^4 points",
+                     "open_values_ms": open_ms, "reduce_ms": reduce_ms,
+                     "lde_bytes": elems * 4,
+                     "open_values_gbs": elems * 4 / (open_ms / 1e3) / 1e9,
+                     "reduce_gbs": elems * 4 / (reduce_ms / 1e3) / 1e9},
         "hash_roofline": {"kernel": "Merkle stage (k_hash_groups leaf sponge + k_compress_level)",
                           "bound": "integer multiply pipe (permutation issue)",
                           "achieved": perms / (hash_ms / 1e3) if hash_ms > 0 else None, "unit": "perms/s",
