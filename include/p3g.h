@@ -305,6 +305,14 @@ P3G_API int p3g_fold_matrix_bb4(p3g_ctx *ctx, const void *d_in, uint32_t log_hei
                         uint32_t log_arity, const uint32_t h_beta[4], void *d_out,
                         void *stream);
 
+/* y[i] += a * x[i] for n BabyBear^4 values on the device: prove_fri's mix-in of
+ * the next reduced opening, current += beta^arity * next (fri_prover.hpp:127-138).
+ * With p3g_commit_matrix (the round's commitment of current viewed as
+ * (n / arity) x (4 arity) BabyBear, fri_extension_mmcs.hpp:49-75) and
+ * p3g_fold_matrix_bb4 this is every device step of the FRI commit phase. */
+P3G_API int p3g_bb4_axpy(p3g_ctx *ctx, void *d_y, const void *d_x, uint64_t n, const uint32_t h_a[4],
+                         void *stream);
+
 /* ------------------------------------------------------------ PCS open
  * TwoAdicFriPcs::open's two passes over a BabyBear LDE resident on the device
  * (two_adic_fri_pcs.hpp:271-410).  d_lde: (1 << log_n) x width evaluations on

@@ -424,3 +424,108 @@ def pcs_reduce(lde: np.ndarray, shift: int, zs, opened, alpha, ap0: int, q: np.n
     lib().orc_pcs_reduce(_ptr(m), n.bit_length() - 1, w, shift, _ptr(z), z.shape[0], _ptr(ov), _ptr(a), ap0,
                          _ptr(q), nthreads)
     return q
+
+
+# ------------------------------------------------------------------ transcript
+class Transcript:
+    """The reference's DuplexChallenger<BabyBear, Perm, 16, 8>
+    (duplex_challenger.hpp:43-260) restated over the oracle's Poseidon2-16:
+    observations fill an input buffer that overwrites the first RATE state
+    words when full (or before a sample), then the state is permuted and its
+    first RATE words become the output buffer, sampled from the back.
+    TEST INFRASTRUCTURE: it drives the FRI commit phase in the tests."""
+    RATE = 8
+
+    def __init__(self, params: P2Params):
+        self.p = params
+        self.state = np.zeros(16, dtype=np.uint32)
+        self.inp: list[int] = []
+        self.out: list[int] = []
+
+    def copy(self) -> "Transcript":
+        t = Transcript(self.p)
+        t.state, t.inp, t.out = self.state.copy(), list(self.inp), list(self.out)
+        return t
+
+    def _absorb(self, v: int):
+        self.inp.append(int(v) % BB_P)
+        if len(self.inp) == self.RATE:
+            self._duplex()
+
+    def _duplex(self):
+        for i, v in enumerate(self.inp):
+            self.state[i] = v
+        self.inp = []
+        self.state = permute(self.p, self.state)
+        self.out = [int(x) for x in self.state[:self.RATE]]
+
+    def observe(self, v: int):
+        self.out = []
+        self._absorb(v)
+
+    def observe_ext(self, v):
+        self.out = []
+        for c in v:
+            self._absorb(int(c))
+
+    def observe_cap(self, digests):
+        if len(digests) == 0:
+            return
+        self.out = []
+        for d in digests:
+            for e in d:
+                self._absorb(int(e))
+
+    def sample(self) -> int:
+        if self.inp or not self.out:
+            self._duplex()
+        return self.out.pop()
+
+    def sample_ext(self) -> list[int]:
+        return [self.sample() for _ in range(4)]
+
+    def _observe_witness(self, w: int):
+        self.out = []
+        self._absorb(w & 0xFFFFFFFF)
+        self._absorb(w >> 32)
+
+    def grind(self, bits: int) -> int:
+        mask = (1 << bits) - 1
+        w = 0
+        while True:
+            a = self.copy()
+            a._observe_witness(w)
+            if a.sample() & mask == 0:
+                self._observe_witness(w)
+                self.sample()
+                return w
+            w += 1
+
+
+def fri_log_arity(log_height: int, has_next: bool, next_log_height: int, log_final_height: int,
+                  max_log_arity: int) -> int:
+    """compute_log_arity_for_round (fri_params.hpp:36-57)."""
+    target = next_log_height if has_next else log_final_height
+    if log_height <= target:
+        return 0
+    return min(log_height - target, max_log_arity)
+
+
+def bb4_axpy(y: np.ndarray, a, x: np.ndarray) -> np.ndarray:
+    """y + a * x elementwise over BabyBear^4 (n x 4 arrays)."""
+    out = np.empty_like(y)
+    aa = np.asarray(a, dtype=np.uint32)
+    for i in range(y.shape[0]):
+        t = bb4_mul(aa, x[i])
+        out[i] = [(int(y[i][k]) + int(t[k])) % BB_P for k in range(4)]
+    return out
+
+
+def bb4_pow(a, e: int):
+    r, b = np.array([1, 0, 0, 0], np.uint32), np.asarray(a, dtype=np.uint32)
+    while e:
+        if e & 1:
+            r = bb4_mul(r, b)
+        b = bb4_mul(b, b)
+        e >>= 1
+    return r

@@ -410,6 +410,13 @@ int main(int argc, char** argv) {
         put32(uint32_t(proof.commit_phase_commits.size()));
         put32(uint32_t(p3_fri::compute_log_arity_for_round(max_log, false, 0, 1, 1)));
         for (const auto& e : proof.commit_phase_commits.at(0)[0]) put(e);
+        // then: the PCS commitment, every commit-phase root and the final polynomial
+        for (const auto& e : commit[0]) put(e);
+        for (const auto& c : proof.commit_phase_commits)
+            for (const auto& e : c[0]) put(e);
+        put32(uint32_t(proof.final_poly.size()));
+        for (const auto& v : proof.final_poly)
+            for (size_t k = 0; k < 4; ++k) put(v[k]);
     } else if (cmd == "pcs_commit") {
         // pcs_commit <seed> <log_h>x<w> ... : TwoAdicFriPcs::commit (log_blowup 1,
         // domain shift 1 as in fri_test.cpp) with the seeded BB16 Poseidon2.

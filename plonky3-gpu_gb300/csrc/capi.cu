@@ -524,6 +524,14 @@ int p3g_commit_traces_host(p3g_ctx* ctx, int field, const p3g_trace* traces, siz
     API_END
 }
 
+int p3g_bb4_axpy(p3g_ctx* ctx, void* d_y, const void* d_x, uint64_t n, const uint32_t h_a[4], void* stream) {
+    API_BEGIN
+    P3G_REQUIRE(ctx && (n == 0 || (d_y && d_x)) && h_a, "bb4_axpy: null argument");
+    DeviceGuard g(ctx->device);
+    p3g::bb4_axpy(ctx, static_cast<uint32_t*>(d_y), static_cast<const uint32_t*>(d_x), n, h_a, S(stream));
+    API_END
+}
+
 int p3g_pcs_open_values(p3g_ctx* ctx, const void* d_lde, uint32_t log_n, uint32_t width, int bitrev_rows,
                         uint32_t shift, const uint32_t* h_points, uint32_t n_points, uint32_t* h_out, void* stream) {
     API_BEGIN

@@ -119,4 +119,23 @@ void fold_bb4(p3g_ctx* ctx, const uint32_t* in, int log_height, int log_arity, c
     P3G_CUDA(cudaGetLastError());
 }
 
+// y[i] += a * x[i] over BabyBear^4 (a in Montgomery form): prove_fri's mix-in of
+// the next reduced opening, current[k] += beta^arity * next[k] (fri_prover.hpp:127-138).
+__global__ void k_bb4_axpy(bb4* __restrict__ y, const bb4* __restrict__ x, uint64_t n, bb4 am) {
+    const uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    y[i] = bb4_add(y[i], bb4_mul_cm(x[i], am));
+}
+
+void bb4_axpy(p3g_ctx*, uint32_t* y, const uint32_t* x, uint64_t n, const uint32_t* a, cudaStream_t st) {
+    P3G_REQUIRE(y && x && a, "bb4_axpy: null argument");
+    for (int k = 0; k < 4; ++k) P3G_REQUIRE(a[k] < bb::P, "bb4_axpy: a must be canonical");
+    if (n == 0) return;
+    const bb4 am = {{bb::to_mont(a[0]), bb::to_mont(a[1]), bb::to_mont(a[2]), bb::to_mont(a[3])}};
+    k_bb4_axpy<<<unsigned((n + 255) / 256), 256, 0, st>>>(reinterpret_cast<bb4*>(y), reinterpret_cast<const bb4*>(x),
+                                                         n, am);
+    P3G_LAUNCHED();
+    P3G_CUDA(cudaGetLastError());
+}
+
 }  // namespace p3g

@@ -137,6 +137,8 @@ void pcs_open_values(p3g_ctx* ctx, const uint32_t* lde, int log_n, int w, int bi
 void pcs_reduce(p3g_ctx* ctx, const uint32_t* lde, int log_n, int w, int bitrev_rows, uint32_t shift,
                 const uint32_t* h_points, int m, const uint32_t* h_opened, const uint32_t* h_alpha, uint64_t alpha_pow,
                 int q_bitrev, uint32_t* q, cudaStream_t st);
+// y += a * x over BabyBear^4 (fold.cu)
+void bb4_axpy(p3g_ctx* ctx, uint32_t* y, const uint32_t* x, uint64_t n, const uint32_t* a, cudaStream_t st);
 // device copies of the prepared DFT twiddle tables (cudaMalloc'd; the context frees them)
 void* make_dft_tw_bb();
 void* make_dft_tw_gl();

@@ -177,10 +177,18 @@ def main() -> int:
     for seed, shapes in ((3, ["5x16", "8x16", "7x16"]), (11, ["6x5", "6x3"]), (12, ["9x2", "4x7"])):
         raw = np.frombuffer(run("pcs_open", seed, *shapes), np.uint32)
         n_open = sum(int(s.split("x")[1]) for s in shapes) * 4
+        o = 8 + n_open
+        rounds = int(raw[o])
+        tail = o + 10
+        commits = raw[tail + 8:tail + 8 + 8 * rounds].reshape(rounds, 8).tolist()
+        nf = int(raw[tail + 8 + 8 * rounds])
+        final = raw[tail + 9 + 8 * rounds:tail + 9 + 8 * rounds + 4 * nf].reshape(nf, 4).tolist()
         opens.append({"seed": seed, "shapes": shapes, "log_blowup": 1, "shift": 1,
+                      "fri": {"log_final_poly_len": 0, "max_log_arity": 1, "commit_pow_bits": 0},
                       "zeta": raw[0:4].tolist(), "alpha": raw[4:8].tolist(),
-                      "opened": raw[8:8 + n_open].tolist(), "fri_rounds": int(raw[8 + n_open]),
-                      "log_arity0": int(raw[9 + n_open]), "commit0": raw[10 + n_open:18 + n_open].tolist()})
+                      "opened": raw[8:o].tolist(), "fri_rounds": rounds,
+                      "log_arity0": int(raw[o + 1]), "commit0": raw[o + 2:o + 10].tolist(),
+                      "pcs_root": raw[tail:tail + 8].tolist(), "commits": commits, "final_poly": final})
     g["pcs_open"] = opens
 
     folds = []

@@ -44,6 +44,8 @@ def test_null_arguments_rejected_without_gpu_work():
     assert b"null" in buf.value
     assert L.p3g_ctx_create(0, None) == 1
     assert L.p3g_dft(None, 0, P.DFT, None, 4, 4, 0, 0, None, None) == 1
+    assert L.p3g_bb4_axpy(None, None, None, 4, None, None) == 1
+    assert L.p3g_pcs_open_values(None, None, 4, 4, 0, 31, None, 1, None, None) == 1
 
 
 def test_seeded_constants_match_oracle():

@@ -331,3 +331,77 @@ def test_pcs_open_vs_reference(golden):
         opened, root, _, _ = pcs_open_case(case)
         assert opened.tolist() == case["opened"]
         assert root.tolist() == case["commit0"]
+
+
+def fri_final_poly(current: np.ndarray, log_final_poly_len: int) -> np.ndarray:
+    """prove_fri's final polynomial (fri_prover.hpp:141-179): truncate, bit-reverse,
+    naive inverse DFT."""
+    n = 1 << log_final_poly_len
+    cur = _bitrev_rows(current[:n])
+    L = O.lib()
+    om_inv = L.orc_bb_pow(L.orc_bb_two_adic_generator(log_final_poly_len), n - 1)
+    n_inv = L.orc_bb_inv(n % O.BB_P)
+    out = np.zeros((n, 4), np.uint32)
+    for k in range(n):
+        s = np.zeros(4, np.uint32)
+        for j in range(n):
+            wkj = L.orc_bb_pow(om_inv, k * j)
+            s = np.array([(int(s[e]) + int(cur[j][e]) * wkj) % O.BB_P for e in range(4)], np.uint32)
+        out[k] = [int(v) * n_inv % O.BB_P for v in s]
+    return out
+
+
+def fri_commit_phase(case, inputs, tr, commit, fold, axpy, length, download):
+    """prove_fri's commit phase (fri_prover.hpp:73-139) over the given inputs
+    (bit-reversed reduced openings, tallest first) with the operations passed
+    in; returns the per-round roots and the final polynomial."""
+    fri = case["fri"]
+    log_final = case["log_blowup"] + fri["log_final_poly_len"]
+    current, idx, roots = inputs[0], 1, []
+    while length(current) > (1 << log_final):
+        log_h = length(current).bit_length() - 1
+        has_next = idx < len(inputs)
+        nxt = length(inputs[idx]).bit_length() - 1 if has_next else 0
+        la = O.fri_log_arity(log_h, has_next, nxt, log_final, fri["max_log_arity"])
+        if la == 0:
+            break
+        root = commit(current, 1 << la)
+        tr.observe_cap([root])
+        roots.append(root)
+        tr.grind(fri["commit_pow_bits"])
+        beta = tr.sample_ext()
+        current = fold(current, log_h, la, beta)
+        if idx < len(inputs) and length(inputs[idx]) == length(current):
+            current = axpy(current, O.bb4_pow(beta, 1 << la), inputs[idx])
+            idx += 1
+    return roots, fri_final_poly(download(current), fri["log_final_poly_len"])
+
+
+def open_transcript(case):
+    """The transcript up to prove_fri: observe the PCS commitment, sample zeta
+    (the caller's opening point) and alpha (TwoAdicFriPcs::open's first sample)."""
+    tr = O.Transcript(O.bb16_params())
+    tr.observe_cap([case["pcs_root"]])
+    zeta = tr.sample_ext()
+    alpha = tr.sample_ext()
+    return tr, zeta, alpha
+
+
+def test_transcript_and_fri_commit_phase_vs_reference(golden):
+    for case in golden["pcs_open"]:
+        tr, zeta, alpha = open_transcript(case)
+        assert zeta == case["zeta"] and alpha == case["alpha"]
+        opened, _, ldes, qs = pcs_open_case(case)
+        for v in opened.reshape(-1, 4):  # two_adic_fri_pcs.hpp:338-346
+            tr.observe_ext(v)
+        inputs = [_bitrev_rows(qs[h]) for h in sorted(qs, reverse=True)]
+        roots, final = fri_commit_phase(
+            case, inputs, tr,
+            commit=lambda cur, arity: O.commit_matrix(O.bb16_params(), cur.reshape(-1, 4 * arity))[-1][0],
+            fold=lambda cur, lh, la, beta: O.fold_matrix_bb4(cur, lh, la, beta),
+            axpy=O.bb4_axpy, length=len, download=lambda c: c)
+        assert [r.tolist() for r in roots] == case["commits"]
+        assert final.tolist() == case["final_poly"]
+        for pc in golden["pcs_commit"]:  # the same commitment where the commit cases overlap
+            if pc["seed"] == case["seed"] and pc["shapes"] == case["shapes"]:
+                assert pc["root"] == case["pcs_root"]
