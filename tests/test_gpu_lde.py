@@ -87,3 +87,26 @@ def test_lde_full_size_config1(gpu_ctx):
     got = gpu_ctx.coset_lde(t, 1)
     want = O.bb_coset_lde(t, 1, nthreads=os.cpu_count() or 1)
     assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("log_h,w,lb,field", [(21, 3, 1, "bb"), (21, 1, 2, "bb"), (17, 20, 3, "bb"),
+                                              (21, 2, 1, "gl"), (19, 3, 2, "gl")])
+def test_lde_largest_supported_heights(gpu_ctx, log_h, w, lb, field):
+    """The three-pass limit (h = 2^21) and deep blowups, odd widths, both orders."""
+    rng = np.random.default_rng(log_h * 7 + w)
+    if field == "bb":
+        t = rng.integers(0, O.BB_P, size=(1 << log_h, w), dtype=np.uint32)
+        ref = lambda br: O.bb_coset_lde(t, lb, 31, br, nthreads=os.cpu_count() or 1)
+        shift = 31
+    else:
+        t = rng.integers(0, O.GL_P, size=(1 << log_h, w), dtype=np.uint64)
+        ref = lambda br: O.gl_coset_lde(t, lb, 7, br, nthreads=os.cpu_count() or 1)
+        shift = 7
+    for br in (True, False):
+        assert np.array_equal(gpu_ctx.coset_lde(t, lb, shift, br), ref(br)), (log_h, w, lb, br)
+
+
+def test_lde_beyond_supported_height_is_reported(gpu_ctx):
+    d = gpu_ctx.alloc(64)
+    assert P.load().p3g_coset_lde(gpu_ctx.handle, 0, d.ptr, 22, 1, 1, 31, 1, d.ptr, None) == 5  # unsupported
+    d.free()
