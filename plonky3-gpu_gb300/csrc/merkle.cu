@@ -10,10 +10,15 @@
 // compress(node i, hash(row i of those matrices)); the tree stops at
 // 2^cap_height nodes.
 //
-// The leaf kernel reads every row straight from HBM (one thread per row, no
-// host-side concatenation) with the Poseidon2 state in registers; one kernel
-// per level computes the compressions and the injection together.  All digest
-// layers stay resident on the device for openings.
+// One persistent kernel (k_hash_groups) hashes the rows of every height group
+// -- the leaves and the rows injected at higher levels -- taking 256-row work
+// units from an atomic queue, each row read straight from HBM by one thread
+// with the Poseidon2 state in registers (no host-side concatenation); one
+// kernel per level then compresses pairs and folds in that level's injected
+// digests.  tree_prepare lays out the digest layers and uploads the work
+// descriptors once, tree_enqueue only launches, so a plan can capture the
+// launches in a graph and replay them.  All digest layers stay resident on the
+// device for openings.
 #include <algorithm>
 #include <cstring>
 #include <numeric>
