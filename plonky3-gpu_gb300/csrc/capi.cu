@@ -88,6 +88,21 @@ int p3g_last_error(char* buf, size_t len) {
     return P3G_OK;
 }
 
+// Frees the context's device tables and pool (null members are skipped).
+static void free_ctx_resources(p3g_ctx* ctx) {
+    cudaFree(ctx->bb_lo);
+    cudaFree(ctx->bb_hi);
+    cudaFree(ctx->gl_lo);
+    cudaFree(ctx->gl_hi);
+    cudaFree(ctx->bb_dft_tw);
+    cudaFree(ctx->gl_dft_tw);
+    ctx->bb_lo = ctx->bb_hi = nullptr;
+    ctx->gl_lo = ctx->gl_hi = nullptr;
+    ctx->bb_dft_tw = ctx->gl_dft_tw = nullptr;
+    if (ctx->pool) cudaMemPoolDestroy(ctx->pool);
+    ctx->pool = nullptr;
+}
+
 int p3g_ctx_create(int device, p3g_ctx** out) {
     API_BEGIN
     P3G_REQUIRE(out != nullptr, "ctx_create: null output");
@@ -97,45 +112,50 @@ int p3g_ctx_create(int device, p3g_ctx** out) {
     DeviceGuard g(device);
     auto ctx = std::make_unique<p3g_ctx>();
     ctx->device = device;
-    P3G_CUDA(cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device));
-    cudaMemPoolProps props = {};
-    props.allocType = cudaMemAllocationTypePinned;
-    props.location.type = cudaMemLocationTypeDevice;
-    props.location.id = device;
-    P3G_CUDA(cudaMemPoolCreate(&ctx->pool, &props));
-    uint64_t keep = ~uint64_t(0);
-    P3G_CUDA(cudaMemPoolSetAttribute(ctx->pool, cudaMemPoolAttrReleaseThreshold, &keep));
-    // two-level root tables g^E = lo[E mod 2^LB] * hi[E >> LB] (const form)
-    {
-        using RB = p3g::RootTab<p3g::FBB>;
-        const uint32_t g27 = p3g::bb::two_adic_generator(27);
-        std::vector<uint32_t> lo(size_t(1) << RB::LB), hi(size_t(1) << (27 - RB::LB));
-        uint32_t v = 1;
-        for (auto& x : lo) { x = p3g::bb::to_mont(v); v = p3g::bb::h_mul(v, g27); }
-        const uint32_t step = v;  // g^(2^LB)
-        v = 1;
-        for (auto& x : hi) { x = p3g::bb::to_mont(v); v = p3g::bb::h_mul(v, step); }
-        P3G_CUDA(cudaMalloc(&ctx->bb_lo, lo.size() * 4));
-        P3G_CUDA(cudaMalloc(&ctx->bb_hi, hi.size() * 4));
-        P3G_CUDA(cudaMemcpy(ctx->bb_lo, lo.data(), lo.size() * 4, cudaMemcpyHostToDevice));
-        P3G_CUDA(cudaMemcpy(ctx->bb_hi, hi.data(), hi.size() * 4, cudaMemcpyHostToDevice));
+    try {
+        P3G_CUDA(cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device));
+        cudaMemPoolProps props = {};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = device;
+        P3G_CUDA(cudaMemPoolCreate(&ctx->pool, &props));
+        uint64_t keep = ~uint64_t(0);
+        P3G_CUDA(cudaMemPoolSetAttribute(ctx->pool, cudaMemPoolAttrReleaseThreshold, &keep));
+        // two-level root tables g^E = lo[E mod 2^LB] * hi[E >> LB] (const form)
+        {
+            using RB = p3g::RootTab<p3g::FBB>;
+            const uint32_t g27 = p3g::bb::two_adic_generator(27);
+            std::vector<uint32_t> lo(size_t(1) << RB::LB), hi(size_t(1) << (27 - RB::LB));
+            uint32_t v = 1;
+            for (auto& x : lo) { x = p3g::bb::to_mont(v); v = p3g::bb::h_mul(v, g27); }
+            const uint32_t step = v;  // g^(2^LB)
+            v = 1;
+            for (auto& x : hi) { x = p3g::bb::to_mont(v); v = p3g::bb::h_mul(v, step); }
+            P3G_CUDA(cudaMalloc(&ctx->bb_lo, lo.size() * 4));
+            P3G_CUDA(cudaMalloc(&ctx->bb_hi, hi.size() * 4));
+            P3G_CUDA(cudaMemcpy(ctx->bb_lo, lo.data(), lo.size() * 4, cudaMemcpyHostToDevice));
+            P3G_CUDA(cudaMemcpy(ctx->bb_hi, hi.data(), hi.size() * 4, cudaMemcpyHostToDevice));
+        }
+        {
+            using RG = p3g::RootTab<p3g::FGL>;
+            const uint64_t g32 = p3g::gl::two_adic_generator(32);
+            std::vector<uint64_t> lo(size_t(1) << RG::LB), hi(size_t(1) << (32 - RG::LB));
+            uint64_t v = 1;
+            for (auto& x : lo) { x = v; v = p3g::gl::h_mul(v, g32); }
+            const uint64_t step = v;
+            v = 1;
+            for (auto& x : hi) { x = v; v = p3g::gl::h_mul(v, step); }
+            P3G_CUDA(cudaMalloc(&ctx->gl_lo, lo.size() * 8));
+            P3G_CUDA(cudaMalloc(&ctx->gl_hi, hi.size() * 8));
+            P3G_CUDA(cudaMemcpy(ctx->gl_lo, lo.data(), lo.size() * 8, cudaMemcpyHostToDevice));
+            P3G_CUDA(cudaMemcpy(ctx->gl_hi, hi.data(), hi.size() * 8, cudaMemcpyHostToDevice));
+        }
+        ctx->bb_dft_tw = p3g::make_dft_tw_bb();
+        ctx->gl_dft_tw = p3g::make_dft_tw_gl();
+    } catch (...) {
+        free_ctx_resources(ctx.get());  // whatever was created before the failure
+        throw;
     }
-    {
-        using RG = p3g::RootTab<p3g::FGL>;
-        const uint64_t g32 = p3g::gl::two_adic_generator(32);
-        std::vector<uint64_t> lo(size_t(1) << RG::LB), hi(size_t(1) << (32 - RG::LB));
-        uint64_t v = 1;
-        for (auto& x : lo) { x = v; v = p3g::gl::h_mul(v, g32); }
-        const uint64_t step = v;
-        v = 1;
-        for (auto& x : hi) { x = v; v = p3g::gl::h_mul(v, step); }
-        P3G_CUDA(cudaMalloc(&ctx->gl_lo, lo.size() * 8));
-        P3G_CUDA(cudaMalloc(&ctx->gl_hi, hi.size() * 8));
-        P3G_CUDA(cudaMemcpy(ctx->gl_lo, lo.data(), lo.size() * 8, cudaMemcpyHostToDevice));
-        P3G_CUDA(cudaMemcpy(ctx->gl_hi, hi.data(), hi.size() * 8, cudaMemcpyHostToDevice));
-    }
-    ctx->bb_dft_tw = p3g::make_dft_tw_bb();
-    ctx->gl_dft_tw = p3g::make_dft_tw_gl();
     *out = ctx.release();
     API_END
 }
@@ -146,13 +166,7 @@ int p3g_ctx_destroy(p3g_ctx* ctx) {
     {
         DeviceGuard g(ctx->device);
         cudaDeviceSynchronize();
-        cudaFree(ctx->bb_lo);
-        cudaFree(ctx->bb_hi);
-        cudaFree(ctx->gl_lo);
-        cudaFree(ctx->gl_hi);
-        cudaFree(ctx->bb_dft_tw);
-        cudaFree(ctx->gl_dft_tw);
-        if (ctx->pool) cudaMemPoolDestroy(ctx->pool);
+        free_ctx_resources(ctx);
     }
     delete ctx;
     API_END
