@@ -510,6 +510,18 @@ def run_ours(args):
     perm_peak = n_states / (e0.elapsed_time(e1) / reps / 1e3)
     d_states.free()
 
+    # ---- proof-of-work search (DuplexChallenger::grind, p3g_grind) at 26 bits
+    # from 4 random challenger states: candidates searched per second, host
+    # clock around each call (the call synchronises)
+    grind_bits, grind_cand, grind_s = 26, 0, 0.0
+    ctx.grind(P.BABYBEAR, np.zeros(16, np.uint32), [], 8, stream=sptr)
+    for k in range(4):
+        st = rng.integers(0, BB_P, size=16, dtype=np.uint32)
+        t0 = time.perf_counter()
+        w = ctx.grind(P.BABYBEAR, st, [int(x) for x in st[:k]], grind_bits, stream=sptr)
+        grind_s += time.perf_counter() - t0
+        grind_cand += w + 1
+
     hbm, src = peaks()
     lde_bytes = 4 * WIDTH * (h + H)
     lde_gbs = lde_bytes / (lde_ms / 1e3) / 1e9
@@ -552,6 +564,11 @@ def run_ours(args):
                      "lde_bytes": elems * 4,
                      "open_values_gbs": elems * 4 / (open_ms / 1e3) / 1e9,
                      "reduce_gbs": elems * 4 / (reduce_ms / 1e3) / 1e9},
+        "pow_grind": {"workload": f"DuplexChallenger::grind, {grind_bits} bits, 4 challenger states "
+                                  "(0-3 pending inputs), Poseidon2-16",
+                      "candidates": grind_cand, "ms": grind_s * 1e3,
+                      "perms_per_s": grind_cand / grind_s,
+                      "frac_of_perm_peak": grind_cand / grind_s / perm_peak},
         "hash_roofline": {"kernel": "Merkle stage (k_hash_groups leaf sponge + k_compress_level)",
                           "bound": "integer multiply pipe (permutation issue)",
                           "achieved": perms / (hash_ms / 1e3) if hash_ms > 0 else None, "unit": "perms/s",

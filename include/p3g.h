@@ -45,7 +45,8 @@ enum p3g_status {
     P3G_ECUDA = 3,       /* CUDA runtime error (reference: P3_CUDA_CHECK runtime_error) */
     P3G_ETIMEOUT = 4,    /* a bounded device or host wait ran out */
     P3G_EUNSUPPORTED = 5,/* shape or parameter outside what this build supports */
-    P3G_ESTATE = 6       /* missing set-up (e.g. no Poseidon2 constants) */
+    P3G_ESTATE = 6,      /* missing set-up (e.g. no Poseidon2 constants) */
+    P3G_ENOTFOUND = 7    /* a bounded search ended without a result (p3g_grind) */
 };
 
 enum p3g_field {
@@ -312,6 +313,29 @@ P3G_API int p3g_fold_matrix_bb4(p3g_ctx *ctx, const void *d_in, uint32_t log_hei
  * p3g_fold_matrix_bb4 this is every device step of the FRI commit phase. */
 P3G_API int p3g_bb4_axpy(p3g_ctx *ctx, void *d_y, const void *d_x, uint64_t n, const uint32_t h_a[4],
                          void *stream);
+
+/* ------------------------------------------------------------ proof of work
+ * DuplexChallenger::grind (duplex_challenger.hpp:234-251) for the challenger
+ * DuplexChallenger<F, Perm, WIDTH, RATE> over the context's Poseidon2
+ * permutation: BabyBear WIDTH 16, RATE 8; Goldilocks WIDTH 8, RATE 4.
+ * Called by prove_fri for the commit- and query-phase witnesses
+ * (fri_prover.hpp:116, 195).
+ *
+ * The challenger's state: h_sponge_state (WIDTH elements) and its pending
+ * inputs h_input (n_input < RATE elements, in observation order); values are
+ * u32 (BabyBear, canonical) or u64 (Goldilocks).  The pending outputs do not
+ * matter: observing the witness discards them.  Writes the smallest witness w
+ * for which observe_witness(w) (elements F(w mod 2^32), F(w >> 32)) followed
+ * by sample() gives an element whose canonical value has its low `bits` bits
+ * zero -- the witness the reference's sequential search returns.  The caller
+ * then applies check_witness(bits, w) to its own challenger, which performs
+ * the same observe-and-sample that grind leaves behind.
+ * bits must be below FIELD_BITS (31 BabyBear, 64 Goldilocks); max_witness
+ * bounds the search (0 = unbounded, as in the reference); P3G_ENOTFOUND if no
+ * witness below it passes.  Synchronises the stream. */
+P3G_API int p3g_grind(p3g_ctx *ctx, int field, const void *h_sponge_state, const void *h_input,
+                      uint32_t n_input, uint32_t bits, uint64_t max_witness, uint64_t *witness_out,
+                      void *stream);
 
 /* ------------------------------------------------------------ PCS open
  * TwoAdicFriPcs::open's two passes over a BabyBear LDE resident on the device

@@ -14,6 +14,8 @@
 //   GpuInputMmcs<p3_merkle::MerkleTreeMmcs<...>>   commit_matrix        (fri_merkle_tree_mmcs.hpp:55)
 //   GpuMerkleTreeMmcs<p3_merkle_tree::MerkleTreeMmcs<...>> commit       (merkle_tree_mmcs.hpp:100)
 //   gpu_fold_matrix<Val, Challenge>(...)          fold_matrix           (fri_folding.hpp:200)
+//   GpuDuplexChallenger<F, Perm, WIDTH, RATE>     DuplexChallenger with grind on the GPU
+//                                                  (duplex_challenger.hpp:42-285)
 //
 // e.g. TwoAdicFriPcs<BB, BB4, GpuDft<Radix2Dit<BB>>, GpuInputMmcs<FlatMmcs>, EFMmcs>.
 // The element types must be the reference's 4-byte BabyBear (value(),
@@ -372,5 +374,125 @@ std::vector<Challenge> gpu_fold_matrix(size_t log_height, size_t log_arity, cons
     }
     return res;
 }
+
+// ----------------------------------------------------------------- challenger
+// DuplexChallenger<F, Perm, WIDTH, RATE> (duplex_challenger.hpp:42-285) whose
+// proof-of-work search, grind (:234-251), runs on the GPU (p3g_grind).  The
+// reference keeps its sponge state private, so this class carries its own:
+// the same transcript steps -- observations fill an input buffer that is
+// written over the first RATE state words when full or before a sample, the
+// state is permuted by Perm on the host and its first RATE words become the
+// output buffer, sampled from the back.  It has the reference's public
+// members and stands in for it wherever a challenger is a template argument,
+// e.g. as the inner challenger of a prove_fri transcript.  BabyBear WIDTH 16
+// RATE 8 or Goldilocks WIDTH 8 RATE 4; the context's Poseidon2 constants for
+// the field (Context::set_poseidon2) must describe the same permutation as Perm.
+template <class F, class Perm, size_t WIDTH, size_t RATE>
+class GpuDuplexChallenger {
+    static_assert((sizeof(F) == 4 && WIDTH == 16 && RATE == 8) || (sizeof(F) == 8 && WIDTH == 8 && RATE == 4),
+                  "BabyBear width 16 rate 8, or Goldilocks width 8 rate 4");
+    using Word = std::conditional_t<sizeof(F) == 4, uint32_t, uint64_t>;
+
+public:
+    static constexpr size_t FIELD_BITS = sizeof(F) == 4 ? 31 : 64;
+
+    explicit GpuDuplexChallenger(Perm perm) : perm_(std::move(perm)), state_{} { in_.reserve(RATE); }
+
+    void observe(F v) {
+        out_.clear();
+        absorb(v);
+    }
+    void observe_slice(const std::vector<F>& vs) {
+        if (vs.empty()) return;
+        out_.clear();
+        for (const F& v : vs) absorb(v);
+    }
+    F sample() {
+        if (!in_.empty() || out_.empty()) duplexing();
+        F v = out_.back();
+        out_.pop_back();
+        return v;
+    }
+    size_t sample_bits(size_t bits) {
+        size_t result = 0, left = bits;
+        while (left > 0) {
+            const uint64_t v = canonical(sample());
+            const size_t chunk = left < FIELD_BITS ? left : FIELD_BITS;
+            const uint64_t mask = chunk == 64 ? ~uint64_t(0) : (uint64_t(1) << chunk) - 1;
+            result |= size_t(v & mask) << (bits - left);
+            left -= chunk;
+        }
+        return result;
+    }
+    template <class EF>
+    EF sample_algebra_element() {
+        EF r{};
+        for (size_t i = 0; i < EF::DEGREE; ++i) r.coeffs[i] = sample();
+        return r;
+    }
+    template <class EF>
+    void observe_algebra_element(const EF& v) {
+        out_.clear();
+        for (size_t i = 0; i < EF::DEGREE; ++i) absorb(v.coeffs[i]);
+    }
+    template <class EF>
+    void observe_algebra_slice(const std::vector<EF>& vs) {
+        if (vs.empty()) return;
+        out_.clear();
+        for (const EF& v : vs)
+            for (size_t i = 0; i < EF::DEGREE; ++i) absorb(v.coeffs[i]);
+    }
+    template <class Hash>
+    void observe_merkle_cap(const std::vector<Hash>& cap) {
+        if (cap.empty()) return;
+        out_.clear();
+        for (const Hash& h : cap)
+            for (const F& e : h) absorb(e);
+    }
+
+    // The smallest witness whose observation and one sample give an element
+    // with `bits` low zero bits; leaves the transcript as the reference's does
+    // (witness observed, that sample consumed).
+    uint64_t grind(size_t bits) {
+        if (bits >= FIELD_BITS) throw std::invalid_argument("grind: PoW bits must be less than FIELD_BITS");
+        std::array<Word, WIDTH> st;
+        std::array<Word, RATE> in{};
+        for (size_t i = 0; i < WIDTH; ++i) st[i] = Word(canonical(state_[i]));
+        for (size_t i = 0; i < in_.size(); ++i) in[i] = Word(canonical(in_[i]));
+        uint64_t w = 0;
+        check(p3g_grind(Context::get().handle(), field_id<F>(), st.data(), in.data(), uint32_t(in_.size()),
+                        uint32_t(bits), 0, &w, nullptr));
+        observe_witness(w);
+        sample();
+        return w;
+    }
+    bool check_witness(size_t bits, uint64_t w) {
+        observe_witness(w);
+        const uint64_t v = canonical(sample());
+        const uint64_t mask = bits >= 64 ? ~uint64_t(0) : (uint64_t(1) << bits) - 1;
+        return (v & mask) == 0;
+    }
+
+private:
+    void absorb(F v) {
+        in_.push_back(v);
+        if (in_.size() == RATE) duplexing();
+    }
+    void observe_witness(uint64_t w) {
+        out_.clear();
+        absorb(F(uint32_t(w & 0xFFFFFFFFu)));
+        absorb(F(uint32_t(w >> 32)));
+    }
+    void duplexing() {
+        std::copy(in_.begin(), in_.end(), state_.begin());
+        in_.clear();
+        perm_.permute_mut(state_);
+        out_.assign(state_.begin(), state_.begin() + RATE);
+    }
+
+    Perm perm_;
+    std::array<F, WIDTH> state_;
+    std::vector<F> in_, out_;
+};
 
 }  // namespace p3g

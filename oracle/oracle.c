@@ -412,6 +412,63 @@ DEFINE_P2(p2gl, uint64_t, orc_gl_add, orc_gl_mul)
 void orc_p2_permute_bb(const orc_p2 *p, uint32_t *state) { p2bb_permute(p, state); }
 void orc_p2_permute_gl(const orc_p2 *p, uint64_t *state) { p2gl_permute(p, state); }
 
+/* DuplexChallenger::grind (duplex_challenger.hpp:234-251), searched in order
+ * exactly as the reference does: each candidate replays the challenger's
+ * absorb / duplexing / sample steps (:51-73, 115-124) on a copy of the state.
+ * The state is held as u64 for both fields. */
+typedef struct {
+    uint64_t st[ORC_P2_MAX_W];
+    uint64_t in[ORC_P2_MAX_W];
+    int n_in, n_out;
+} orc_chal;
+
+static void chal_duplex(const orc_p2 *p, orc_chal *c) {
+    for (int i = 0; i < c->n_in; ++i) c->st[i] = c->in[i];
+    c->n_in = 0;
+    if (p->field == 0) {
+        uint32_t s[ORC_P2_MAX_W];
+        for (int i = 0; i < p->width; ++i) s[i] = (uint32_t)c->st[i];
+        p2bb_permute(p, s);
+        for (int i = 0; i < p->width; ++i) c->st[i] = s[i];
+    } else {
+        p2gl_permute(p, c->st);
+    }
+    c->n_out = p->rate;  /* output buffer = st[0..rate), popped from the back */
+}
+
+static void chal_absorb(const orc_p2 *p, orc_chal *c, uint64_t v) {
+    c->in[c->n_in++] = v;
+    if (c->n_in == p->rate) chal_duplex(p, c);
+}
+
+int orc_grind(const orc_p2 *p, const void *state, const void *input, unsigned n_input, unsigned bits,
+              uint64_t limit, uint64_t *witness_out) {
+    if ((int)n_input >= p->rate) return -1;
+    const uint64_t mask = bits >= 64 ? ~(uint64_t)0 : (((uint64_t)1 << bits) - 1);
+    orc_chal saved;
+    memset(&saved, 0, sizeof saved);
+    for (int i = 0; i < p->width; ++i)
+        saved.st[i] = p->field == 0 ? ((const uint32_t *)state)[i] : ((const uint64_t *)state)[i];
+    for (unsigned i = 0; i < n_input; ++i)
+        saved.in[i] = p->field == 0 ? ((const uint32_t *)input)[i] : ((const uint64_t *)input)[i];
+    saved.n_in = (int)n_input;
+    for (uint64_t w = 0; w < limit; ++w) {
+        orc_chal a = saved;
+        a.n_out = 0;  /* observe_witness clears the output buffer */
+        const uint32_t lo = (uint32_t)w, hi = (uint32_t)(w >> 32);
+        chal_absorb(p, &a, p->field == 0 ? lo % ORC_BB_P : lo);
+        chal_absorb(p, &a, p->field == 0 ? hi % ORC_BB_P : hi);
+        if (a.n_in > 0 || a.n_out == 0) chal_duplex(p, &a);
+        uint64_t v = a.st[a.n_out - 1];
+        if (p->field != 0) v %= ORC_GL_P;
+        if ((v & mask) == 0) {
+            *witness_out = w;
+            return 0;
+        }
+    }
+    return -1;
+}
+
 /* A sponge that absorbs from a list of row slices without building a flat
  * copy; identical to hash_iter over the concatenation
  * (padding_free_sponge.hpp:63-113). */

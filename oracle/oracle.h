@@ -85,6 +85,11 @@ typedef struct {
 
 void orc_p2_permute_bb(const orc_p2 *p, uint32_t *state);
 void orc_p2_permute_gl(const orc_p2 *p, uint64_t *state);
+/* DuplexChallenger<F, Perm, width, rate>::grind from the challenger's sponge
+ * state (width elements) and n_input < rate pending inputs (u32 BabyBear, u64
+ * Goldilocks): the smallest witness below limit, or -1 if none. */
+int orc_grind(const orc_p2 *p, const void *state, const void *input, unsigned n_input, unsigned bits,
+              uint64_t limit, uint64_t *witness_out);
 /* PaddingFreeSponge::hash_iter: elements are u32 (BB) or u64 (GL). */
 void orc_p2_hash(const orc_p2 *p, const void *data, size_t len, void *digest_out);
 /* TruncatedPermutation<.., 2, digest, width>::compress */

@@ -97,6 +97,8 @@ def lib():
         L.orc_gl_coset_lde.argtypes = [vp, C.c_uint, sz, C.c_uint, u64, i32, vp, i32]
         L.orc_p2_permute_bb.argtypes = [vp, vp]
         L.orc_p2_permute_gl.argtypes = [vp, vp]
+        L.orc_grind.restype = i32
+        L.orc_grind.argtypes = [vp, vp, vp, C.c_uint, C.c_uint, u64, vp]
         L.orc_p2_hash.argtypes = [vp, vp, sz, vp]
         L.orc_p2_compress.argtypes = [vp, vp, vp, vp]
         L.orc_mmcs_commit.restype = i32
@@ -489,7 +491,8 @@ class Transcript:
         self._absorb(w & 0xFFFFFFFF)
         self._absorb(w >> 32)
 
-    def grind(self, bits: int) -> int:
+    def grind_py(self, bits: int) -> int:
+        """grind, searched by replaying this class's own steps per candidate."""
         mask = (1 << bits) - 1
         w = 0
         while True:
@@ -500,6 +503,29 @@ class Transcript:
                 self.sample()
                 return w
             w += 1
+
+    def grind(self, bits: int) -> int:
+        """grind through the C restatement (orc_grind), then the observe and
+        sample that the reference's grind leaves behind."""
+        w = grind(self.p, self.state, self.inp, bits)
+        self._observe_witness(w)
+        self.sample()
+        return w
+
+    def check_witness(self, bits: int, w: int) -> bool:
+        self._observe_witness(w)
+        return self.sample() & ((1 << bits) - 1) == 0
+
+
+def grind(p: P2Params, state, pending, bits: int, limit: int = 1 << 40) -> int:
+    """DuplexChallenger::grind from a sponge state and pending inputs (orc_grind)."""
+    dt = _dt(p)
+    st = np.ascontiguousarray(state, dtype=dt)
+    inp = np.ascontiguousarray(list(pending) if len(pending) else [0], dtype=dt)
+    w = C.c_uint64()
+    if lib().orc_grind(C.byref(p), _ptr(st), _ptr(inp), len(pending), bits, limit, C.byref(w)) != 0:
+        raise ValueError("no witness below the limit")
+    return w.value
 
 
 def fri_log_arity(log_height: int, has_next: bool, next_log_height: int, log_final_height: int,

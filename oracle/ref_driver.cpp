@@ -417,6 +417,22 @@ int main(int argc, char** argv) {
         put32(uint32_t(proof.final_poly.size()));
         for (const auto& v : proof.final_poly)
             for (size_t k = 0; k < 4; ++k) put(v[k]);
+        // then: the query-phase proof-of-work witness (query_proof_of_work_bits = 8)
+        put64(proof.query_pow_witness);
+    } else if (cmd == "grind") {
+        // grind <seed> <n_obs> <bits>... : the reference's DuplexChallenger (BB16,
+        // rate 8, seeded permutation) observes n_obs seeded values, then for each
+        // bits: grind(bits) and one more sample().  (Its grind does not compile
+        // for the reference's Goldilocks, which has no FIELD_BITS.)
+        uint64_t seed = strtoull(argv[3], 0, 0);
+        size_t n_obs = atoi(argv[4]);
+        p3_challenger::DuplexChallenger<BB, WrapBB, 16, 8> ch(WrapBB{make_pos_bb()});
+        std::mt19937 rng(static_cast<uint32_t>(seed));
+        for (size_t i = 0; i < n_obs; ++i) ch.observe(BB(static_cast<uint32_t>(rng() % BB::PRIME)));
+        for (int a = 5; a < argc; ++a) {
+            put64(ch.grind(atoi(argv[a])));
+            put(ch.sample());
+        }
     } else if (cmd == "pcs_commit") {
         // pcs_commit <seed> <log_h>x<w> ... : TwoAdicFriPcs::commit (log_blowup 1,
         // domain shift 1 as in fri_test.cpp) with the seeded BB16 Poseidon2.

@@ -74,6 +74,7 @@ const char* p3g_status_string(int s) {
         case P3G_ETIMEOUT: return "timed out";
         case P3G_EUNSUPPORTED: return "unsupported";
         case P3G_ESTATE: return "missing set-up";
+        case P3G_ENOTFOUND: return "not found";
         default: return "unknown status";
     }
 }
@@ -543,6 +544,27 @@ int p3g_bb4_axpy(p3g_ctx* ctx, void* d_y, const void* d_x, uint64_t n, const uin
     P3G_REQUIRE(ctx && (n == 0 || (d_y && d_x)) && h_a, "bb4_axpy: null argument");
     DeviceGuard g(ctx->device);
     p3g::bb4_axpy(ctx, static_cast<uint32_t*>(d_y), static_cast<const uint32_t*>(d_x), n, h_a, S(stream));
+    API_END
+}
+
+int p3g_grind(p3g_ctx* ctx, int field, const void* h_sponge_state, const void* h_input, uint32_t n_input,
+              uint32_t bits, uint64_t max_witness, uint64_t* witness_out, void* stream) {
+    API_BEGIN
+    P3G_REQUIRE(ctx && h_sponge_state && witness_out && (n_input == 0 || h_input), "grind: null argument");
+    P3G_REQUIRE(field == P3G_BABYBEAR || field == P3G_GOLDILOCKS, "grind: unknown field");
+    const uint32_t width = field == P3G_BABYBEAR ? 16 : 8, rate = width / 2;
+    P3G_REQUIRE(n_input < rate, "grind: more pending inputs than the challenger holds (n_input < RATE)");
+    P3G_REQUIRE(bits < (field == P3G_BABYBEAR ? 31u : 64u), "grind: bits must be below the field's FIELD_BITS");
+    if (field == P3G_BABYBEAR) {
+        const auto* st = static_cast<const uint32_t*>(h_sponge_state);
+        const auto* in = static_cast<const uint32_t*>(h_input);
+        for (uint32_t i = 0; i < width; ++i) P3G_REQUIRE(st[i] < p3g::bb::P, "grind: sponge state not canonical");
+        for (uint32_t i = 0; i < n_input; ++i) P3G_REQUIRE(in[i] < p3g::bb::P, "grind: input not canonical");
+    }
+    DeviceGuard g(ctx->device);
+    const uint64_t limit = max_witness ? max_witness : ~uint64_t(0);
+    if (!p3g::grind(ctx, field, h_sponge_state, h_input, n_input, bits, limit, witness_out, S(stream)))
+        throw p3g::Error(P3G_ENOTFOUND, "grind: no witness below max_witness");
     API_END
 }
 

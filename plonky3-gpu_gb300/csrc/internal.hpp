@@ -159,6 +159,9 @@ void tree_prepare(p3g_ctx* ctx, p3g_tree* tree, unsigned cap_height, bool flat, 
 void tree_enqueue(p3g_ctx* ctx, p3g_tree* tree, cudaStream_t st);
 void tree_release(p3g_ctx* ctx, p3g_tree* tree, cudaStream_t st);
 void permute_states(p3g_ctx* ctx, int field, void* d_states, size_t n, cudaStream_t st);
+// DuplexChallenger::grind: smallest witness below `limit` (false if none)
+bool grind(p3g_ctx* ctx, int field, const void* h_state, const void* h_input, uint32_t n_input, uint32_t bits,
+           uint64_t limit, uint64_t* witness, cudaStream_t st);
 void open_batch(p3g_ctx* ctx, const p3g_tree* tree, const uint64_t* h_idx, size_t nq,
                 void* h_rows, void* h_proof, cudaStream_t st);
 

@@ -281,6 +281,69 @@ void permute_states(p3g_ctx* ctx, int field, void* d_states, size_t n, cudaStrea
         dispatch_gl(ctx, PermFn<HGL>{&ctx->p2gl, static_cast<uint64_t*>(d_states), n, st});
 }
 
+template <class H>
+struct GrindFn {
+    const typename H::Params* p;
+    const GrindArgs<typename H::T, H::W>* a;
+    uint64_t base, count;
+    unsigned long long* found;
+    int sm_count;
+    cudaStream_t st;
+    template <int D, int RF, int RP>
+    void operator()() const { Launch<H, D, RF, RP>::grind(*p, *a, base, count, found, sm_count, st); }
+};
+
+template <class H>
+static bool grind_impl(p3g_ctx* ctx, const typename H::Params* params, const typename H::T* h_state,
+                       const typename H::T* h_input, uint32_t n_input, uint32_t bits, uint64_t limit,
+                       uint64_t* witness, cudaStream_t st) {
+    using T = typename H::T;
+    GrindArgs<T, H::W> a{};
+    for (int i = 0; i < H::W; ++i) a.state[i] = H::absorb(i < int(n_input) ? h_input[i] : h_state[i]);
+    a.n_input = n_input;
+    a.mask = bits == 64 ? ~uint64_t(0) : (uint64_t(1) << bits) - 1;
+    auto* found = static_cast<unsigned long long*>(ctx->alloc(sizeof(unsigned long long), st));
+    struct Release {
+        p3g_ctx* c;
+        void* p;
+        cudaStream_t s;
+        ~Release() { c->release(p, s); }
+    } rel{ctx, found, st};
+    P3G_CUDA(cudaMemsetAsync(found, 0xFF, sizeof(unsigned long long), st));
+    // Launches of at most 2^30 candidates (well under a second each); the
+    // first is sized so that it holds a hit with probability 1 - e^-16.
+    uint64_t chunk = uint64_t(1) << std::min(30u, std::max(20u, bits + 4));
+    unsigned long long hit = ~0ull;
+    for (uint64_t base = 0; base < limit; ) {
+        const uint64_t count = std::min(chunk, limit - base);
+        GrindFn<H> fn{params, &a, base, count, found, ctx->sm_count, st};
+        if constexpr (std::is_same<H, HBB>::value) dispatch_bb(ctx, fn);
+        else dispatch_gl(ctx, fn);
+        P3G_CUDA(cudaMemcpyAsync(&hit, found, sizeof hit, cudaMemcpyDeviceToHost, st));
+        P3G_CUDA(cudaStreamSynchronize(st));
+        if (hit != ~0ull) {
+            *witness = hit;
+            return true;
+        }
+        base += count;
+        chunk = std::min(chunk * 2, uint64_t(1) << 30);
+    }
+    return false;
+}
+
+bool grind(p3g_ctx* ctx, int field, const void* h_state, const void* h_input, uint32_t n_input, uint32_t bits,
+           uint64_t limit, uint64_t* witness, cudaStream_t st) {
+    if (bits == 0) {  // every sample passes a zero-bit mask: the first candidate
+        *witness = 0;
+        return limit > 0;
+    }
+    if (field == P3G_BABYBEAR)
+        return grind_impl<HBB>(ctx, &ctx->p2bb, static_cast<const uint32_t*>(h_state),
+                               static_cast<const uint32_t*>(h_input), n_input, bits, limit, witness, st);
+    return grind_impl<HGL>(ctx, &ctx->p2gl, static_cast<const uint64_t*>(h_state),
+                           static_cast<const uint64_t*>(h_input), n_input, bits, limit, witness, st);
+}
+
 void open_batch(p3g_ctx* ctx, const p3g_tree* tree, const uint64_t* h_idx, size_t nq, void* h_rows,
                 void* h_proof, cudaStream_t st) {
     if (nq == 0) return;

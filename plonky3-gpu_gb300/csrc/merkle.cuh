@@ -200,6 +200,51 @@ __global__ void __launch_bounds__(128) k_permute(typename H::Params p, typename 
     for (int i = 0; i < H::W; ++i) states[j * H::W + i] = H::squeeze(s[i]);
 }
 
+// Proof-of-work search, DuplexChallenger::grind (duplex_challenger.hpp:234-251).
+// The challenger's sponge state and pending inputs are fixed; a candidate
+// witness c is observed as the two elements F(c mod 2^32) and F(c >> 32)
+// (observe_witness, :57-61) and one element is sampled: state word RATE - 1
+// after the next duplexing.  With RATE - 1 inputs pending, the low half fills
+// the buffer and duplexes first, so such a candidate costs two permutations
+// (one call site, run twice).  Thread t tries base + t, base + t + T, ... in
+// increasing order and stops once the smallest hit so far is at or below its
+// next candidate, so *found ends as the smallest hit in [base, base + count).
+template <class T, int W>
+struct GrindArgs {
+    T state[W];  // sponge state with the pending inputs written over its first words, internal form
+    uint32_t n_input;
+    uint64_t mask;
+};
+
+template <class H, int D, int RF, int RP>
+__global__ void __launch_bounds__(128) k_grind(typename H::Params p, GrindArgs<typename H::T, H::W> a,
+                                               uint64_t base, uint64_t count, unsigned long long* found) {
+    using T = typename H::T;
+    const int k = int(a.n_input);
+    const int passes = k + 1 == H::RATE ? 2 : 1;
+    const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+    for (uint64_t off = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; off < count; off += stride) {
+        const uint64_t c = base + off;
+        if (*reinterpret_cast<volatile unsigned long long*>(found) <= c) break;
+        const T lo = H::absorb(H::from_u32(uint32_t(c)));
+        const T hi = H::absorb(H::from_u32(uint32_t(c >> 32)));
+        T s[H::W];
+#pragma unroll
+        for (int i = 0; i < H::W; ++i) s[i] = a.state[i];  // from the parameter bank
+#pragma unroll
+        for (int i = 0; i < H::RATE; ++i) {
+            if (i == k) s[i] = lo;
+            if (i == k + 1) s[i] = hi;
+        }
+#pragma unroll 1
+        for (int pass = 0; pass < passes; ++pass) {
+            if (pass == 1) s[0] = hi;
+            H::template perm<D, RF, RP>(s, p);
+        }
+        if ((uint64_t(H::squeeze(s[H::RATE - 1])) & a.mask) == 0) atomicMin(found, c);
+    }
+}
+
 // Host launchers, explicitly instantiated once per schedule.
 template <class H, int D, int RF, int RP>
 struct Launch {
@@ -210,6 +255,8 @@ struct Launch {
     static void level(const typename H::Params& p, const T* child, uint64_t nchild, T* parent, uint64_t nparent,
                       const T* inj, cudaStream_t st);
     static void permute(const typename H::Params& p, T* states, uint64_t n, cudaStream_t st);
+    static void grind(const typename H::Params& p, const GrindArgs<T, H::W>& a, uint64_t base, uint64_t count,
+                      unsigned long long* found, int sm_count, cudaStream_t st);
 };
 
 #ifdef P3G_MERKLE_INSTANTIATE
@@ -239,6 +286,21 @@ void Launch<H, D, RF, RP>::level(const typename H::Params& p, const T* child, ui
                                  uint64_t nparent, const T* inj, cudaStream_t st) {
     k_compress_level<H, D, RF, RP><<<unsigned((nparent + 127) / 128), 128, 0, st>>>(p, child, nchild, parent,
                                                                                      nparent, inj);
+    P3G_LAUNCHED();
+    P3G_CUDA(cudaGetLastError());
+}
+template <class H, int D, int RF, int RP>
+void Launch<H, D, RF, RP>::grind(const typename H::Params& p, const GrindArgs<T, H::W>& a, uint64_t base,
+                                 uint64_t count, unsigned long long* found, int sm_count, cudaStream_t st) {
+    if (count == 0) return;
+    static int occ = 0;
+    if (occ == 0) {
+        int o = 0;
+        P3G_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_grind<H, D, RF, RP>, 128, 0));
+        occ = o > 0 ? o : 1;
+    }
+    const uint64_t blocks = std::min<uint64_t>(uint64_t(occ) * sm_count, (count + 127) / 128);
+    k_grind<H, D, RF, RP><<<unsigned(blocks), 128, 0, st>>>(p, a, base, count, found);
     P3G_LAUNCHED();
     P3G_CUDA(cudaGetLastError());
 }

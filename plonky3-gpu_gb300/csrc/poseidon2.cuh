@@ -212,8 +212,10 @@ struct HBB {
     using T = uint32_t;
     using Params = P2BB16;
     static constexpr int W = 16, RATE = 8, DIG = 8;
-    static __device__ __forceinline__ T absorb(T canonical) { return bb::mmul(canonical, bb::R2); }
+    static __host__ __device__ __forceinline__ T absorb(T canonical) { return bb::mmul(canonical, bb::R2); }
     static __device__ __forceinline__ T squeeze(T m) { return bb::canon(bb::smul(int32_t(m), 1)); }
+    // BabyBear(uint32_t) reduces its argument (baby_bear.hpp:51)
+    static __device__ __forceinline__ T from_u32(uint32_t x) { return x % bb::P; }
     template <int D, int RF, int RP>
     static __device__ __forceinline__ void perm(T* s, const Params& p) { p2_bb16<D, RF, RP>(s, p); }
 };
@@ -221,8 +223,9 @@ struct HGL {
     using T = uint64_t;
     using Params = P2GL8;
     static constexpr int W = 8, RATE = 4, DIG = 4;
-    static __device__ __forceinline__ T absorb(T canonical) { return canonical; }
+    static __host__ __device__ __forceinline__ T absorb(T canonical) { return canonical; }
     static __device__ __forceinline__ T squeeze(T v) { return v; }
+    static __device__ __forceinline__ T from_u32(uint32_t x) { return x; }  // goldilocks.hpp:34
     template <int D, int RF, int RP>
     static __device__ __forceinline__ void perm(T* s, const Params& p) { p2_gl8<D, RF, RP>(s, p); }
 };

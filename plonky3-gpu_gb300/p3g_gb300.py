@@ -29,7 +29,7 @@ EXPORTS = [
     "p3g_coset_lde_bb_noalloc", "p3g_plan_commit", "p3g_plan_launch", "p3g_plan_info",
     "p3g_plan_destroy", "p3g_server_create", "p3g_server_submit", "p3g_server_poll",
     "p3g_server_pending", "p3g_server_open", "p3g_server_release", "p3g_server_destroy",
-    "p3g_pcs_open_values", "p3g_pcs_reduce", "p3g_bb4_axpy",
+    "p3g_pcs_open_values", "p3g_pcs_reduce", "p3g_bb4_axpy", "p3g_grind",
 ]
 
 
@@ -124,6 +124,7 @@ def load(path: str | None = None):
     L.p3g_server_destroy.argtypes = [vp]
     L.p3g_pcs_open_values.argtypes = [vp, vp, u32, u32, i32, u32, vp, u32, vp, vp]
     L.p3g_bb4_axpy.argtypes = [vp, vp, vp, u64, vp, vp]
+    L.p3g_grind.argtypes = [vp, C.c_int, vp, vp, u32, u32, u64, vp, vp]
     L.p3g_pcs_reduce.argtypes = [vp, vp, u32, u32, i32, u32, vp, u32, vp, vp, u64, i32, vp, vp]
     for name in EXPORTS:
         if name not in ("p3g_version", "p3g_status_string", "p3g_kernel_launches"):
@@ -512,6 +513,18 @@ class Context:
         """y += a * x for n BabyBear^4 values on the device."""
         aa = np.ascontiguousarray(a, dtype=np.uint32).reshape(4)
         check(load().p3g_bb4_axpy(self.handle, d_y, d_x, n, _np_ptr(aa), stream))
+
+    # -- proof of work
+    def grind(self, field: int, sponge_state, pending, bits: int, max_witness: int = 0, stream=None) -> int:
+        """DuplexChallenger::grind from the challenger's sponge state and
+        pending inputs: the smallest passing witness."""
+        dt = np.uint32 if field == BABYBEAR else np.uint64
+        st = np.ascontiguousarray(sponge_state, dtype=dt)
+        inp = np.ascontiguousarray(pending, dtype=dt).reshape(-1)
+        w = C.c_uint64()
+        check(load().p3g_grind(self.handle, field, _np_ptr(st), _np_ptr(inp) if inp.size else None, inp.size,
+                               bits, max_witness, C.byref(w), stream))
+        return w.value
 
     # -- PCS open
     def pcs_open_values_device(self, d_lde: int, log_n: int, width: int, bitrev_rows: bool, shift: int, points,

@@ -11,7 +11,9 @@
 //   2. GpuMerkleTreeMmcs<mixed-height MMCS>::commit against the stock one (all
 //      digest layers), then the stock open_batch / verify_batch on the GPU tree;
 //   3. GpuDft's dft / idft / coset_dft / coset_idft against Radix2Dit's;
-//   4. gpu_fold_matrix against TwoAdicFriFolding<BB, BB4>::fold_matrix.
+//   4. gpu_fold_matrix against TwoAdicFriFolding<BB, BB4>::fold_matrix;
+//   5. GpuDuplexChallenger against DuplexChallenger: the same observations,
+//      samples, sample_bits and grind witnesses.
 
 #include "baby_bear.hpp"
 #include "extension_field.hpp"
@@ -27,6 +29,7 @@
 #include "fri_folding.hpp"
 #include "fri_params.hpp"
 #include "two_adic_fri_pcs.hpp"
+#include "duplex_challenger.hpp"
 
 #include "p3g_adapters.hpp"
 
@@ -158,6 +161,28 @@ int main() {
             fails += report(la == 1 ? "fold_matrix arity 2" : la == 2 ? "fold_matrix arity 4" : "fold_matrix arity 8",
                             want == got);
         }
+    }
+    // 5. the challenger
+    {
+        p3_challenger::DuplexChallenger<BB, Wrap, 16, 8> cpu(Wrap{pos});
+        p3g::GpuDuplexChallenger<BB, Wrap, 16, 8> gpu(Wrap{pos});
+        std::mt19937 rng(11);
+        bool ok = true;
+        for (size_t n_obs : {size_t(3), size_t(7), size_t(6), size_t(1)}) {
+            for (size_t i = 0; i < n_obs; ++i) {
+                const BB v(uint32_t(rng() % BB::PRIME));
+                cpu.observe(v);
+                gpu.observe(v);
+            }
+            for (size_t bits : {size_t(0), size_t(9), size_t(14)}) ok = ok && cpu.grind(bits) == gpu.grind(bits);
+            ok = ok && cpu.sample() == gpu.sample() && cpu.sample_bits(20) == gpu.sample_bits(20);
+            const auto a = cpu.sample_algebra_element<BabyBear4>();
+            const auto b = gpu.sample_algebra_element<BabyBear4>();
+            ok = ok && a == b;
+            cpu.observe_algebra_element(a);
+            gpu.observe_algebra_element(b);
+        }
+        fails += report("DuplexChallenger with grind on the GPU", ok);
     }
     std::printf("%s\n", fails ? "MISMATCH" : "ALL OK");
     return fails ? 1 : 0;

@@ -11,6 +11,7 @@
 //   adapters_standin mmcs <bb|gl> <in> <out> <cap_height> <h0> <w0> [<h1> <w1> ...]
 //   adapters_standin fold <in> <out> <log_height> <log_arity>
 //   adapters_standin dft <bb|gl> <in> <out> <log_h> <width> <kind 0-3> <shift>
+//   adapters_standin challenger <out> <seed> <n_obs> <bits>...
 //
 // <in> holds canonical little-endian words (u32 BabyBear, u64 Goldilocks;
 // for mmcs the matrices back to back; for fold 4 beta coefficients, then
@@ -18,6 +19,10 @@
 // from the leaves up).  Poseidon2 is the BabyBear-16 x^7 8+13 permutation
 // with constants from std::mt19937(0xdeadbeef) and the Goldilocks-8 x^7 8+22
 // one from std::mt19937_64(12345), initial and terminal drawn interleaved.
+// The challenger command observes n_obs values std::mt19937(seed)() % p in a
+// GpuDuplexChallenger<BabyBear, ..., 16, 8> (host steps permuted through
+// p3g_poseidon2_permute), then for each bits grinds and samples once more,
+// writing the witness (u64) and the sample (u32).
 
 #include "p3g_adapters.hpp"
 
@@ -47,6 +52,7 @@ struct Goldilocks {
     bool operator==(const Goldilocks& o) const { return as_canonical_u64() == o.as_canonical_u64(); }
 };
 struct BabyBear4 {
+    static constexpr size_t DEGREE = 4;
     std::array<BabyBear, 4> coeffs{};
     BabyBear& operator[](size_t i) { return coeffs[i]; }
     const BabyBear& operator[](size_t i) const { return coeffs[i]; }
@@ -140,6 +146,35 @@ static void set_constants() {
     p3g::Context::get().set_poseidon2(gi, gt, gin, 7);
 }
 
+struct DevicePermBB {  // Perm for the challenger's host steps: one state through the GPU permutation
+    void permute_mut(std::array<BabyBear, 16>& s) const {
+        uint32_t w[16];
+        for (size_t i = 0; i < 16; ++i) w[i] = s[i].value();
+        p3g::DeviceBuffer d(sizeof w);
+        d.upload(w, sizeof w);
+        p3g::check(p3g_poseidon2_permute(p3g::Context::get().handle(), P3G_BABYBEAR, d.get(), 1, nullptr));
+        d.download(w, sizeof w);
+        for (size_t i = 0; i < 16; ++i) s[i] = BabyBear(w[i]);
+    }
+};
+
+static int run_challenger(int argc, char** a) {
+    const uint32_t seed = uint32_t(std::strtoul(a[3], nullptr, 0));
+    const size_t n_obs = std::strtoul(a[4], nullptr, 0);
+    p3g::GpuDuplexChallenger<BabyBear, DevicePermBB, 16, 8> ch{DevicePermBB{}};
+    std::mt19937 rng(seed);
+    for (size_t i = 0; i < n_obs; ++i) ch.observe(BabyBear(uint32_t(rng() % BabyBear::PRIME)));
+    std::vector<unsigned char> out;
+    for (int i = 5; i < argc; ++i) {
+        const uint64_t w = ch.grind(std::strtoul(a[i], nullptr, 0));
+        const uint32_t v = ch.sample().value();
+        out.insert(out.end(), reinterpret_cast<const unsigned char*>(&w), reinterpret_cast<const unsigned char*>(&w) + 8);
+        out.insert(out.end(), reinterpret_cast<const unsigned char*>(&v), reinterpret_cast<const unsigned char*>(&v) + 4);
+    }
+    write_file(a[2], out);
+    return 0;
+}
+
 template <class F>
 static int run_lde(char** a) {
     auto in = read_file(a[3]);
@@ -196,6 +231,7 @@ int main(int argc, char** argv) {
     const std::string cmd = argv[1];
     try {
         set_constants();
+        if (cmd == "challenger") return run_challenger(argc, argv);
         if (cmd == "lde") return std::string(argv[2]) == "bb" ? run_lde<BabyBear>(argv) : run_lde<Goldilocks>(argv);
         if (cmd == "dft") {
             if (argc < 9) return 2;

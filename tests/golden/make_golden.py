@@ -182,14 +182,33 @@ def main() -> int:
         tail = o + 10
         commits = raw[tail + 8:tail + 8 + 8 * rounds].reshape(rounds, 8).tolist()
         nf = int(raw[tail + 8 + 8 * rounds])
-        final = raw[tail + 9 + 8 * rounds:tail + 9 + 8 * rounds + 4 * nf].reshape(nf, 4).tolist()
+        end = tail + 9 + 8 * rounds + 4 * nf
+        final = raw[tail + 9 + 8 * rounds:end].reshape(nf, 4).tolist()
+        pow_witness = int(raw[end]) | (int(raw[end + 1]) << 32)
         opens.append({"seed": seed, "shapes": shapes, "log_blowup": 1, "shift": 1,
-                      "fri": {"log_final_poly_len": 0, "max_log_arity": 1, "commit_pow_bits": 0},
+                      "fri": {"log_final_poly_len": 0, "max_log_arity": 1, "commit_pow_bits": 0,
+                              "query_pow_bits": 8, "query_pow_witness": pow_witness},
                       "zeta": raw[0:4].tolist(), "alpha": raw[4:8].tolist(),
                       "opened": raw[8:o].tolist(), "fri_rounds": rounds,
                       "log_arity0": int(raw[o + 1]), "commit0": raw[o + 2:o + 10].tolist(),
                       "pcs_root": raw[tail:tail + 8].tolist(), "commits": commits, "final_poly": final})
     g["pcs_open"] = opens
+
+    grinds = []
+    bits_list = [1, 8, 12, 0, 16]
+    for seed, n_obs in ((1, 0), (2, 1), (3, 5), (4, 6), (5, 7), (6, 8), (7, 13), (8, 15)):
+        raw = run("grind", seed, n_obs, *bits_list)
+        ws, samples = [], []
+        for i in range(len(bits_list)):
+            chunk = raw[i * 12:(i + 1) * 12]
+            ws.append(int(np.frombuffer(chunk[:8], np.uint64)[0]))
+            samples.append(int(np.frombuffer(chunk[8:], np.uint32)[0]))
+        grinds.append({"seed": seed, "n_obs": n_obs, "bits": bits_list, "witness": ws, "sample_after": samples})
+    raw = run("grind", 9, 3, 20)
+    grinds.append({"seed": 9, "n_obs": 3, "bits": [20],
+                   "witness": [int(np.frombuffer(raw[:8], np.uint64)[0])],
+                   "sample_after": [int(np.frombuffer(raw[8:12], np.uint32)[0])]})
+    g["grind"] = grinds
 
     folds = []
     for (lh, la, seed, mode) in ((4, 1, 0xDEADBEEF, 0), (6, 1, 71, 0), (10, 1, 72, 0), (5, 2, 73, 0),

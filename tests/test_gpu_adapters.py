@@ -2,7 +2,8 @@
 tests/cpp/adapters_standin.cpp with stand-ins of the reference's types, against
 the oracle: GpuDft::coset_lde_batch (natural order), GpuInputMmcs::commit_matrix
 (every layer, odd heights), GpuMerkleTreeMmcs::commit (mixed heights, caps,
-both fields) and gpu_fold_matrix.  Bit-exact."""
+both fields) and gpu_fold_matrix; GpuDuplexChallenger against the reference's
+own grind witnesses.  Bit-exact."""
 import subprocess
 
 import numpy as np
@@ -126,6 +127,20 @@ def test_gpu_fold_matrix(prog, tmp_path, log_arity):
     assert rc == 0, err
     got = np.fromfile(fout, dtype=np.uint32).reshape(-1, 4)
     assert np.array_equal(got, O.fold_matrix_bb4(v, log_h, log_arity, beta))
+
+
+def test_gpu_duplex_challenger_grind(prog, tmp_path, golden):
+    """GpuDuplexChallenger's observe / grind / sample sequence gives the
+    witnesses and samples of the reference's DuplexChallenger."""
+    for c in golden["grind"]:
+        fout = str(tmp_path / "ch.bin")
+        r = subprocess.run([prog, "challenger", fout, str(c["seed"]), str(c["n_obs"])] + [str(b) for b in c["bits"]],
+                           capture_output=True, text=True, timeout=120)
+        assert r.returncode == 0, r.stderr
+        raw = open(fout, "rb").read()
+        for i, (w, after) in enumerate(zip(c["witness"], c["sample_after"])):
+            assert int.from_bytes(raw[12 * i:12 * i + 8], "little") == w, (c, i)
+            assert int.from_bytes(raw[12 * i + 8:12 * i + 12], "little") == after, (c, i)
 
 
 def test_adapter_reports_bad_dimensions_as_invalid_argument(prog, tmp_path):

@@ -1,16 +1,17 @@
-"""The FRI commit phase of prove_fri (fri_prover.hpp:73-185) with every data
+"""The FRI commit phase of prove_fri (fri_prover.hpp:73-195) with every data
 step on the GPU -- each round's commitment (p3g_commit_matrix of the current
 vector as (n / arity) x (4 arity) BabyBear), fold (p3g_fold_matrix_bb4) and
 mix-in of the next reduced opening (p3g_bb4_axpy) -- and the reduced openings
 themselves from the GPU's PCS-open passes, driven by the oracle's restated
-transcript.  Every round's root and the final polynomial must equal the
-reference's proof for each golden case."""
+transcript, and the query-phase proof-of-work witness from p3g_grind.  Every
+round's root, the final polynomial and the witness must equal the reference's
+proof for each golden case."""
 import numpy as np
 import pytest
 
 import oracle as O
 import p3g_gb300 as P
-from test_oracle import fri_commit_phase, open_transcript
+from test_oracle import fri_commit_phase, fri_query_pow, open_transcript
 
 pytestmark = pytest.mark.gpu
 
@@ -60,10 +61,17 @@ def test_fri_commit_phase_on_gpu_vs_reference(gpu_ctx, golden):
             gpu_ctx.bb4_axpy_device(cur.buf.ptr, nxt.buf.ptr, cur.n, a)
             return cur
 
-        roots, final = fri_commit_phase(case, inputs, tr, commit, fold, axpy, length=lambda c: c.n,
-                                        download=lambda c: c.buf.download(np.uint32, (c.n, 4)))
+        roots, final, arities = fri_commit_phase(case, inputs, tr, commit, fold, axpy, length=lambda c: c.n,
+                                                 download=lambda c: c.buf.download(np.uint32, (c.n, 4)))
         assert [r.tolist() for r in roots] == case["commits"]
         assert final.tolist() == case["final_poly"]
+
+        def gpu_grind(t, bits):  # the query-phase witness from the GPU search
+            w = gpu_ctx.grind(P.BABYBEAR, t.state, t.inp, bits)
+            assert t.check_witness(bits, w)
+            return w
+
+        assert fri_query_pow(case, tr, final, arities, gpu_grind) == case["fri"]["query_pow_witness"]
         for b in keep + list(qs.values()):
             b.free()
 

@@ -354,10 +354,11 @@ def fri_final_poly(current: np.ndarray, log_final_poly_len: int) -> np.ndarray:
 def fri_commit_phase(case, inputs, tr, commit, fold, axpy, length, download):
     """prove_fri's commit phase (fri_prover.hpp:73-139) over the given inputs
     (bit-reversed reduced openings, tallest first) with the operations passed
-    in; returns the per-round roots and the final polynomial."""
+    in; returns the per-round roots, the final polynomial and the per-round
+    log arities."""
     fri = case["fri"]
     log_final = case["log_blowup"] + fri["log_final_poly_len"]
-    current, idx, roots = inputs[0], 1, []
+    current, idx, roots, arities = inputs[0], 1, [], []
     while length(current) > (1 << log_final):
         log_h = length(current).bit_length() - 1
         has_next = idx < len(inputs)
@@ -368,13 +369,25 @@ def fri_commit_phase(case, inputs, tr, commit, fold, axpy, length, download):
         root = commit(current, 1 << la)
         tr.observe_cap([root])
         roots.append(root)
+        arities.append(la)
         tr.grind(fri["commit_pow_bits"])
         beta = tr.sample_ext()
         current = fold(current, log_h, la, beta)
         if idx < len(inputs) and length(inputs[idx]) == length(current):
             current = axpy(current, O.bb4_pow(beta, 1 << la), inputs[idx])
             idx += 1
-    return roots, fri_final_poly(download(current), fri["log_final_poly_len"])
+    return roots, fri_final_poly(download(current), fri["log_final_poly_len"]), arities
+
+
+def fri_query_pow(case, tr, final, arities, grind):
+    """prove_fri after the commit phase up to the query-phase witness
+    (fri_prover.hpp:179-195): observe the final polynomial and every round's
+    arity, then grind query_pow_bits with `grind(transcript, bits)`."""
+    for c in final:
+        tr.observe_ext(c)
+    for la in arities:
+        tr.observe(la)
+    return grind(tr, case["fri"]["query_pow_bits"])
 
 
 def open_transcript(case):
@@ -395,13 +408,59 @@ def test_transcript_and_fri_commit_phase_vs_reference(golden):
         for v in opened.reshape(-1, 4):  # two_adic_fri_pcs.hpp:338-346
             tr.observe_ext(v)
         inputs = [_bitrev_rows(qs[h]) for h in sorted(qs, reverse=True)]
-        roots, final = fri_commit_phase(
+        roots, final, arities = fri_commit_phase(
             case, inputs, tr,
             commit=lambda cur, arity: O.commit_matrix(O.bb16_params(), cur.reshape(-1, 4 * arity))[-1][0],
             fold=lambda cur, lh, la, beta: O.fold_matrix_bb4(cur, lh, la, beta),
             axpy=O.bb4_axpy, length=len, download=lambda c: c)
         assert [r.tolist() for r in roots] == case["commits"]
         assert final.tolist() == case["final_poly"]
+        w = fri_query_pow(case, tr, final, arities, lambda t, bits: t.grind_py(bits))
+        assert w == case["fri"]["query_pow_witness"]
         for pc in golden["pcs_commit"]:  # the same commitment where the commit cases overlap
             if pc["seed"] == case["seed"] and pc["shapes"] == case["shapes"]:
                 assert pc["root"] == case["pcs_root"]
+
+
+def test_grind_vs_reference(golden):
+    """DuplexChallenger::grind (duplex_challenger.hpp:234-251) after 0..15
+    observations (every pending-input count, including RATE - 1 where the
+    witness's low half fills the buffer), bits 0..20, and the sample that
+    follows: the C restatement, and the Python one for the small cases."""
+    p = O.bb16_params()
+    for c in golden["grind"]:
+        tr, tr_py = O.Transcript(p), O.Transcript(p)
+        for v in O.mt19937(c["seed"], c["n_obs"]):
+            tr.observe(int(v) % O.BB_P)
+            tr_py.observe(int(v) % O.BB_P)
+        for bits, w, after in zip(c["bits"], c["witness"], c["sample_after"]):
+            assert tr.grind(bits) == w, (c, bits)
+            assert tr.sample() == after
+            if bits <= 12:
+                assert tr_py.grind_py(bits) == w
+                assert tr_py.sample() == after
+            else:
+                assert tr_py.check_witness(bits, w) and tr_py.sample() == after
+
+
+def test_grind_oracle_goldilocks_and_limits():
+    """The restatement over Goldilocks (width 8, rate 4; the reference's grind
+    does not compile for its Goldilocks, so this is unpinned) agrees with a
+    direct replay; a limit below the first hit reports no witness."""
+    p = O.gl8_params()
+    rng = np.random.default_rng(5)
+    for k in range(4):
+        st = rng.integers(0, O.GL_P, size=8, dtype=np.uint64)
+        pend = [int(x) for x in rng.integers(0, O.GL_P, size=k, dtype=np.uint64)]
+        w = O.grind(p, st, pend, 6)
+        for cand in range(w + 1):  # replay: candidate w passes, every smaller one fails
+            s = st.copy()
+            inp = pend + [cand & 0xFFFFFFFF, cand >> 32]
+            s[:min(len(inp), 4)] = inp[:4]
+            s = O.permute(p, s)
+            if len(inp) > 4:
+                s[0] = inp[4]
+                s = O.permute(p, s)
+            assert (int(s[3]) & 63 == 0) == (cand == w), (k, cand, w)
+        with pytest.raises(ValueError):
+            O.grind(p, st, pend, 6, limit=w)
