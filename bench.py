@@ -451,7 +451,8 @@ def run_ours(args):
 
     # ---- end to end through the C ABI with the trace in pinned host memory:
     # p3g_commit_traces_host copies column chunks on a second stream while the
-    # earlier chunks' LDEs run; the root read-back synchronises the stream
+    # earlier chunks' LDEs and row hashes run; the root read-back synchronises
+    # the stream
     pinned = torch.empty(h * WIDTH, dtype=torch.int32, pin_memory=True)
     pinned.numpy().view(np.uint32)[:] = trace.reshape(-1)
     cap = np.zeros((1, 8), np.uint32)

@@ -208,11 +208,15 @@ P3G_API int p3g_commit_traces(p3g_ctx *ctx, int field, const p3g_trace *traces, 
 
 /* p3g_commit_traces with the traces in HOST memory (d_trace is a host
  * pointer; pinned memory gives asynchronous copies).  Each trace is copied in
- * column chunks of 512-byte rows on a second stream, and each chunk's LDE
- * starts as soon as its copy has landed, so the copies overlap the LDEs.
- * The commitment is the same as for the unsplit traces (a leaf hashes the
- * concatenated rows of equal-height matrices in order, merkle_tree.hpp:84-185);
- * the tree's leaf matrices are the column chunks, in trace order. */
+ * column chunks of 512-byte rows (a trace of 2^14 rows or more given first
+ * starts with chunks of 1/4, 1/4 and 1/2 of that) on a second stream; each
+ * chunk's LDE starts as soon as its copy has landed, and its row hashes as
+ * soon as its LDE is written, resuming the sponge of the chunks before it
+ * wherever the row so far is a multiple of the sponge rate long.  So the
+ * copies overlap the LDEs and the hashing.  The commitment is the same as for
+ * the unsplit traces (a leaf hashes the concatenated rows of equal-height
+ * matrices in order, merkle_tree.hpp:84-185); the tree's leaf matrices are
+ * the column chunks, in trace order. */
 P3G_API int p3g_commit_traces_host(p3g_ctx *ctx, int field, const p3g_trace *traces, size_t n_traces,
                                    uint32_t cap_height, p3g_tree **tree_out, void *h_cap_out, void *stream);
 

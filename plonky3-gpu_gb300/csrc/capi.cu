@@ -469,9 +469,6 @@ int p3g_commit_traces_host(p3g_ctx* ctx, int field, const p3g_trace* traces, siz
     DeviceGuard g(ctx->device);
     cudaStream_t st = S(stream);
     const size_t esz = field == P3G_BABYBEAR ? 4 : 8;
-    // 512-byte chunk rows keep the strided copies at the contiguous copy's
-    // bandwidth (narrower rows lose 15% at 256 bytes, half at 128)
-    const uint32_t cw_max = uint32_t(512 / esz);
     for (size_t i = 0; i < n_traces; ++i) {
         const p3g_trace& tr = traces[i];
         P3G_REQUIRE(tr.width == 0 || tr.d_trace, "commit_traces_host: null trace");
@@ -479,57 +476,92 @@ int p3g_commit_traces_host(p3g_ctx* ctx, int field, const p3g_trace* traces, siz
                     "commit_traces_host: shift must be canonical");
         P3G_REQUIRE(tr.log_h <= 21, "commit_traces_host: log_h > 21 is not supported");
     }
+    // Column chunks.  512-byte chunk rows keep the strided copies at the
+    // contiguous copy's bandwidth (narrower rows lose 15% at 256 bytes, half
+    // at 128).  A large first trace starts with chunks of 1/4, 1/4 and 1/2 of
+    // that, so that hashing starts after a short copy; every chunk width is a
+    // multiple of the sponge rate, so each chunk's row hashes run as soon as
+    // its LDE is written, resuming the sponge of the chunks before it.
+    const uint32_t cw_max = uint32_t(512 / esz);
+    struct Chunk {
+        size_t trace;
+        uint32_t c0, cw;
+    };
+    std::vector<Chunk> chunks;
+    for (size_t i = 0; i < n_traces; ++i) {
+        const p3g_trace& tr = traces[i];
+        uint32_t c0 = 0;
+        if (tr.width == 0) chunks.push_back({i, 0, 0});
+        if (i == 0 && tr.log_h >= 14)
+            for (uint32_t w : {cw_max / 4, cw_max / 4, cw_max / 2})
+                if (c0 < tr.width) {
+                    chunks.push_back({i, c0, std::min(w, tr.width - c0)});
+                    c0 += chunks.back().cw;
+                }
+        for (; c0 < tr.width; c0 += cw_max) chunks.push_back({i, c0, std::min(cw_max, tr.width - c0)});
+    }
     auto t = std::make_unique<p3g_tree>();
     t->field = field;
     cudaStream_t cs = nullptr;
     cudaEvent_t start = nullptr;
     std::vector<cudaEvent_t> evs;
-    void* pending = nullptr;  // chunk buffer not yet handed back to the pool
+    // Device copies of the chunks, allocated on `st` before anything else is
+    // queued (the pool then reuses them call after call on the same stream),
+    // filled on the copy stream, handed back on `st` after each chunk's LDE.
+    std::vector<void*> staged_in(chunks.size(), nullptr);
     auto cleanup = [&] {
         for (cudaEvent_t e : evs) cudaEventDestroy(e);
         if (start) cudaEventDestroy(start);
         if (cs) cudaStreamDestroy(cs);
     };
     try {
+        for (const Chunk& c : chunks) {  // the tree's leaf matrices: every chunk's LDE, in order
+            const uint64_t H = uint64_t(1) << (traces[c.trace].log_h + traces[c.trace].log_blowup);
+            void* lde = ctx->alloc(std::max<size_t>(esz * H * c.cw, esz), st);
+            t->owned.push_back(lde);
+            t->mats.push_back(p3g_matrix{lde, H, c.cw, 0});
+        }
+        p3g::tree_prepare(ctx, t.get(), cap_height, false, st, false, /*staged=*/true);
+        for (size_t k = 0; k < chunks.size(); ++k)
+            if (chunks[k].cw > 0)
+                staged_in[k] = ctx->alloc(esz * (uint64_t(1) << traces[chunks[k].trace].log_h) * chunks[k].cw, st);
         P3G_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
         P3G_CUDA(cudaEventCreateWithFlags(&start, cudaEventDisableTiming));
         P3G_CUDA(cudaEventRecord(start, st));
         P3G_CUDA(cudaStreamWaitEvent(cs, start, 0));
-        for (size_t i = 0; i < n_traces; ++i) {
-            const p3g_trace& tr = traces[i];
-            const uint64_t h = uint64_t(1) << tr.log_h, H = h << tr.log_blowup;
-            for (uint32_t c0 = 0; c0 < tr.width || (tr.width == 0 && c0 == 0); c0 += cw_max) {
-                const uint32_t cw = std::min(cw_max, tr.width - c0);
-                void* lde = ctx->alloc(std::max<size_t>(esz * H * cw, esz), st);
-                t->owned.push_back(lde);
-                t->mats.push_back(p3g_matrix{lde, H, cw, 0});
-                if (cw == 0) break;
+        for (size_t k = 0; k < chunks.size(); ++k) {
+            const Chunk& c = chunks[k];
+            const p3g_trace& tr = traces[c.trace];
+            if (c.cw > 0) {
+                const uint64_t h = uint64_t(1) << tr.log_h;
                 // copy stream: this chunk's columns into a contiguous h x cw buffer
-                void* dev = ctx->alloc(esz * h * cw, cs);
-                pending = dev;
-                P3G_CUDA(cudaMemcpy2DAsync(dev, esz * cw, static_cast<const char*>(tr.d_trace) + esz * c0,
-                                           esz * tr.width, esz * cw, h, cudaMemcpyHostToDevice, cs));
+                void* dev = staged_in[k];
+                P3G_CUDA(cudaMemcpy2DAsync(dev, esz * c.cw, static_cast<const char*>(tr.d_trace) + esz * c.c0,
+                                           esz * tr.width, esz * c.cw, h, cudaMemcpyHostToDevice, cs));
                 cudaEvent_t ev;
                 P3G_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
                 evs.push_back(ev);
                 P3G_CUDA(cudaEventRecord(ev, cs));
                 // compute stream: the chunk's LDE as soon as its copy lands
                 P3G_CUDA(cudaStreamWaitEvent(st, ev, 0));
+                void* lde = t->owned[k];
                 if (field == P3G_BABYBEAR)
-                    p3g::lde_bb(ctx, static_cast<const uint32_t*>(dev), int(tr.log_h), int(cw), int(tr.log_blowup),
+                    p3g::lde_bb(ctx, static_cast<const uint32_t*>(dev), int(tr.log_h), int(c.cw), int(tr.log_blowup),
                                 uint32_t(tr.shift), 1, static_cast<uint32_t*>(lde), st);
                 else
-                    p3g::lde_gl(ctx, static_cast<const uint64_t*>(dev), int(tr.log_h), int(cw), int(tr.log_blowup),
+                    p3g::lde_gl(ctx, static_cast<const uint64_t*>(dev), int(tr.log_h), int(c.cw), int(tr.log_blowup),
                                 tr.shift, 1, static_cast<uint64_t*>(lde), st);
                 ctx->release(dev, st);
-                pending = nullptr;
+                staged_in[k] = nullptr;
             }
+            p3g::tree_hash_ready(ctx, t.get(), k + 1, st);  // the row parts this chunk completes
         }
-        p3g::mmcs_build(ctx, t.get(), cap_height, st);
+        p3g::tree_finish(ctx, t.get(), st);
         copy_cap(t.get(), h_cap_out, st);
     } catch (...) {
         if (cs) cudaStreamSynchronize(cs);
-        if (pending) ctx->release(pending, st);
+        for (void* p : staged_in)
+            if (p) ctx->release(p, st);
         p3g::tree_release(ctx, t.get(), st);
         cleanup();
         throw;

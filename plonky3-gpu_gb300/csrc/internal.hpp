@@ -120,8 +120,18 @@ struct p3g_tree {
     // injected-row digest buffer of every layer that has one
     void* d_desc = nullptr;
     std::vector<void*> inj;           // per layer, nullptr when nothing is injected
-    int hash_ngroups = 0;
-    uint64_t hash_units = 0;
+    // Row hashing runs in stages, one launch each: a single stage, or for a
+    // staged build one per commit-order matrix that completes some parts
+    // (stage k may run once matrices 0..ready are written).
+    struct HashStage {
+        size_t ready;
+        uint32_t job0, njobs;         // descriptor range
+        uint64_t units;               // work units of the launch
+    };
+    std::vector<HashStage> stages;
+    size_t stages_done = 0;
+    size_t desc_ents_off = 0;         // byte offset of the entries in d_desc
+    std::vector<void*> stage_bufs;    // sponge states between parts (staged builds)
     bool in_plan = false;             // owned by a plan; p3g_tree_free refuses it
 };
 
@@ -155,8 +165,17 @@ void flat_build(p3g_ctx* ctx, p3g_tree* tree, cudaStream_t st);
 // Two-phase build: tree_prepare allocates every buffer of the tree and uploads
 // its work descriptors (synchronously when `sync_upload`, e.g. before a graph
 // capture); tree_enqueue only launches kernels on `st`.
-void tree_prepare(p3g_ctx* ctx, p3g_tree* tree, unsigned cap_height, bool flat, cudaStream_t st, bool sync_upload);
+void tree_prepare(p3g_ctx* ctx, p3g_tree* tree, unsigned cap_height, bool flat, cudaStream_t st, bool sync_upload,
+                  bool staged = false);
 void tree_enqueue(p3g_ctx* ctx, p3g_tree* tree, cudaStream_t st);
+// Staged build (tree_prepare with staged = true) for callers that write the
+// matrices one by one in commit order: after matrices 0..n_ready-1 are
+// enqueued on `st`, tree_hash_ready hashes every row part they complete (a
+// group's row is cut where its length so far is a multiple of the sponge
+// rate, and the sponge state is carried across the cut); tree_finish hashes
+// the rest and builds the levels.
+void tree_hash_ready(p3g_ctx* ctx, p3g_tree* tree, size_t n_ready, cudaStream_t st);
+void tree_finish(p3g_ctx* ctx, p3g_tree* tree, cudaStream_t st);
 void tree_release(p3g_ctx* ctx, p3g_tree* tree, cudaStream_t st);
 void permute_states(p3g_ctx* ctx, int field, void* d_states, size_t n, cudaStream_t st);
 // DuplexChallenger::grind: smallest witness below `limit` (false if none)

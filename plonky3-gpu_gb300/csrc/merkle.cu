@@ -67,13 +67,17 @@ __global__ void k_open(const OpenMat* mats, int nmats, uint64_t max_h, const uin
 template <class H>
 struct HashFn {
     const typename H::Params* p;
-    void* desc;
+    unsigned long long* counter;
+    const HashGroup<typename H::T>* groups;
     int ngroups;
+    const HashEntry<typename H::T>* ents;
     uint64_t units;
     int sm_count;
     cudaStream_t st;
     template <int D, int RF, int RP>
-    void operator()() const { Launch<H, D, RF, RP>::hash_groups(*p, desc, ngroups, units, sm_count, st); }
+    void operator()() const {
+        Launch<H, D, RF, RP>::hash_groups(*p, counter, groups, ngroups, ents, units, sm_count, st);
+    }
 };
 template <class H>
 struct LevelFn {
@@ -118,7 +122,7 @@ static void dispatch_gl(const p3g_ctx* ctx, const Fn& fn) {
 // ------------------------------------------------------------------ tree build
 template <class H>
 static void prepare(p3g_ctx* ctx, p3g_tree* tree, unsigned cap_height, bool flat, cudaStream_t st,
-                    bool sync_upload) {
+                    bool sync_upload, bool staged) {
     using T = typename H::T;
     const auto& mats = tree->mats;
     const size_t n = mats.size();
@@ -148,7 +152,6 @@ static void prepare(p3g_ctx* ctx, p3g_tree* tree, unsigned cap_height, bool flat
         std::vector<size_t> idx;
         uint64_t rows;
         T* out;
-        uint64_t cost;
     };
     std::vector<G> groups;
     size_t next = 0;
@@ -158,46 +161,88 @@ static void prepare(p3g_ctx* ctx, p3g_tree* tree, unsigned cap_height, bool flat
         return g;
     };
     tree->inj.assign(tree->layer_size.size(), nullptr);
-    groups.push_back({collect(max_h), max_h, dig, 0});
+    groups.push_back({collect(max_h), max_h, dig});
     if (!flat) {
         for (size_t l = 1; l < tree->layer_size.size(); ++l) {
             auto gi = collect(tree->layer_size[l]);
             if (gi.empty()) continue;
             if (!tree->inj[l]) tree->inj[l] = ctx->alloc(sizeof(T) * H::DIG * tree->layer_size[l], st);
-            groups.push_back({gi, tree->layer_size[l], static_cast<T*>(tree->inj[l]), 0});
+            groups.push_back({gi, tree->layer_size[l], static_cast<T*>(tree->inj[l])});
         }
     }
-    if (groups.size() > size_t(MAXG)) throw Error(P3G_EUNSUPPORTED, "more than 64 distinct matrix heights");
+    // Jobs: one per group, or (staged) one per part of a group's row.  A part
+    // ends where the row so far is a multiple of RATE long and the next matrix
+    // has columns, so the sponge resumes there from the saved state; a part
+    // can run once its last matrix (in commit order) is written.
+    struct Job {
+        std::vector<size_t> idx;
+        uint64_t rows;
+        T* out;
+        uint64_t cost;  // permutations per row
+        size_t ready;
+        const T* sin;
+        T* sout;
+    };
+    std::vector<Job> jobs;
     for (auto& g : groups) {
-        if (g.idx.size() > size_t(MAXG)) throw Error(P3G_EUNSUPPORTED, "more than 64 matrices of one height");
-        uint64_t w = 0;
-        for (size_t i : g.idx) w += mats[i].width;
-        g.cost = (w + H::RATE - 1) / H::RATE;  // permutations per row
+        std::vector<std::vector<size_t>> parts(1);
+        uint64_t len = 0;
+        for (size_t i : g.idx) {
+            if (staged && len > 0 && len % H::RATE == 0 && mats[i].width > 0) parts.emplace_back();
+            parts.back().push_back(i);
+            len += mats[i].width;
+        }
+        T* bufs[2] = {nullptr, nullptr};  // states between parts, alternating
+        for (size_t k = 0; k + 1 < parts.size() && k < 2; ++k) {
+            bufs[k] = static_cast<T*>(ctx->alloc(sizeof(T) * H::W * g.rows, st));
+            tree->stage_bufs.push_back(bufs[k]);
+        }
+        for (size_t k = 0; k < parts.size(); ++k) {
+            Job jb{parts[k], g.rows, g.out, 0, staged ? *std::max_element(parts[k].begin(), parts[k].end()) : n - 1,
+                   k > 0 ? bufs[(k - 1) % 2] : nullptr, k + 1 < parts.size() ? bufs[k % 2] : nullptr};
+            uint64_t w = 0;
+            for (size_t i : parts[k]) w += mats[i].width;
+            jb.cost = (w + H::RATE - 1) / H::RATE;
+            if (jb.idx.size() > size_t(MAXG)) throw Error(P3G_EUNSUPPORTED, "more than 64 matrices of one height");
+            jobs.push_back(std::move(jb));
+        }
     }
-    // most expensive rows first, so the queue drains with cheap units
-    std::stable_sort(groups.begin(), groups.end(), [](const G& a, const G& b) { return a.cost > b.cost; });
+    // stages in commit order; within a stage the most expensive rows first,
+    // so the queue drains with cheap units
+    std::stable_sort(jobs.begin(), jobs.end(), [](const Job& a, const Job& b) {
+        return a.ready != b.ready ? a.ready < b.ready : a.cost > b.cost;
+    });
     std::vector<HashGroup<T>> hg;
     std::vector<HashEntry<T>> he;
-    uint64_t units = 0;
-    for (const auto& g : groups) {
+    tree->stages.clear();
+    tree->stages_done = 0;
+    for (const auto& jb : jobs) {
+        if (tree->stages.empty() || tree->stages.back().ready != jb.ready)
+            tree->stages.push_back({jb.ready, uint32_t(hg.size()), 0, 0});
+        auto& stg = tree->stages.back();
+        if (stg.njobs == uint32_t(MAXG)) throw Error(P3G_EUNSUPPORTED, "more than 64 distinct matrix heights");
         HashGroup<T> d{};
-        d.rows = g.rows;
-        d.unit0 = units;
-        d.out = g.out;
+        d.rows = jb.rows;
+        d.unit0 = stg.units;
+        d.out = jb.out;
         d.ent0 = uint32_t(he.size());
-        d.nent = uint32_t(g.idx.size());
+        d.nent = uint32_t(jb.idx.size());
         d.vec = 0;
-        for (size_t i : g.idx) he.push_back({static_cast<const T*>(mats[i].d_data), mats[i].width, 0});
-        if (g.idx.size() == 1 && sizeof(T) == 4 && mats[g.idx[0]].width % 4 == 0 &&
-            reinterpret_cast<uintptr_t>(mats[g.idx[0]].d_data) % 16 == 0)
+        d.state_in = jb.sin;
+        d.state_out = jb.sout;
+        for (size_t i : jb.idx) he.push_back({static_cast<const T*>(mats[i].d_data), mats[i].width, 0});
+        if (jb.idx.size() == 1 && sizeof(T) == 4 && mats[jb.idx[0]].width % 4 == 0 &&
+            reinterpret_cast<uintptr_t>(mats[jb.idx[0]].d_data) % 16 == 0)
             d.vec = 1;
         hg.push_back(d);
-        units += (g.rows + HASH_ROWS - 1) / HASH_ROWS;
+        stg.njobs += 1;
+        stg.units += (jb.rows + HASH_ROWS - 1) / HASH_ROWS;
     }
-    const size_t bytes = HASH_DESC_HEADER + sizeof(HashGroup<T>) * MAXG + sizeof(HashEntry<T>) * std::max<size_t>(he.size(), 1);
+    tree->desc_ents_off = HASH_DESC_HEADER + (sizeof(HashGroup<T>) * hg.size() + 255) / 256 * 256;
+    const size_t bytes = tree->desc_ents_off + sizeof(HashEntry<T>) * std::max<size_t>(he.size(), 1);
     std::vector<char> host(bytes, 0);
     std::memcpy(host.data() + HASH_DESC_HEADER, hg.data(), sizeof(HashGroup<T>) * hg.size());
-    std::memcpy(host.data() + HASH_DESC_HEADER + sizeof(HashGroup<T>) * MAXG, he.data(), sizeof(HashEntry<T>) * he.size());
+    std::memcpy(host.data() + tree->desc_ents_off, he.data(), sizeof(HashEntry<T>) * he.size());
     if (!tree->d_desc) tree->d_desc = ctx->alloc(bytes, st);
     if (sync_upload) {
         P3G_CUDA(cudaStreamSynchronize(st));
@@ -206,23 +251,43 @@ static void prepare(p3g_ctx* ctx, p3g_tree* tree, unsigned cap_height, bool flat
         // pageable source: the copy is staged before cudaMemcpyAsync returns
         P3G_CUDA(cudaMemcpyAsync(tree->d_desc, host.data(), bytes, cudaMemcpyHostToDevice, st));
     }
-    tree->hash_ngroups = int(hg.size());
-    tree->hash_units = units;
+}
+
+// Launches the row-hash stages [stages_done, end) whose matrices are all
+// written (ready < n_ready).
+template <class H>
+static void hash_stages(p3g_ctx* ctx, p3g_tree* tree, const typename H::Params& p, size_t n_ready, cudaStream_t st) {
+    using T = typename H::T;
+    char* base = static_cast<char*>(tree->d_desc);
+    auto* counter = reinterpret_cast<unsigned long long*>(base);
+    auto* groups = reinterpret_cast<const HashGroup<T>*>(base + HASH_DESC_HEADER);
+    auto* ents = reinterpret_cast<const HashEntry<T>*>(base + tree->desc_ents_off);
+    for (; tree->stages_done < tree->stages.size() && tree->stages[tree->stages_done].ready < n_ready;
+         ++tree->stages_done) {
+        const auto& stg = tree->stages[tree->stages_done];
+        HashFn<H> fn{&p, counter, groups + stg.job0, int(stg.njobs), ents, stg.units, ctx->sm_count, st};
+        if constexpr (std::is_same<H, HBB>::value) dispatch_bb(ctx, fn);
+        else dispatch_gl(ctx, fn);
+    }
+}
+
+template <class H>
+static void levels(p3g_ctx* ctx, p3g_tree* tree, const typename H::Params& p, cudaStream_t st) {
+    using T = typename H::T;
+    T* dig = static_cast<T*>(tree->d_digests);
+    for (size_t l = 1; l < tree->layer_size.size(); ++l) {
+        LevelFn<H> fn{&p, dig + tree->layer_off[l - 1] * H::DIG, tree->layer_size[l - 1],
+                      dig + tree->layer_off[l] * H::DIG, tree->layer_size[l], static_cast<const T*>(tree->inj[l]), st};
+        if constexpr (std::is_same<H, HBB>::value) dispatch_bb(ctx, fn);
+        else dispatch_gl(ctx, fn);
+    }
 }
 
 template <class H>
 static void enqueue(p3g_ctx* ctx, p3g_tree* tree, const typename H::Params& p, cudaStream_t st) {
-    using T = typename H::T;
-    auto run = [&](const auto& fnobj) {
-        if constexpr (std::is_same<H, HBB>::value) dispatch_bb(ctx, fnobj);
-        else dispatch_gl(ctx, fnobj);
-    };
-    run(HashFn<H>{&p, tree->d_desc, tree->hash_ngroups, tree->hash_units, ctx->sm_count, st});
-    T* dig = static_cast<T*>(tree->d_digests);
-    for (size_t l = 1; l < tree->layer_size.size(); ++l) {
-        run(LevelFn<H>{&p, dig + tree->layer_off[l - 1] * H::DIG, tree->layer_size[l - 1],
-                       dig + tree->layer_off[l] * H::DIG, tree->layer_size[l], static_cast<const T*>(tree->inj[l]), st});
-    }
+    tree->stages_done = 0;
+    hash_stages<H>(ctx, tree, p, ~size_t(0), st);
+    levels<H>(ctx, tree, p, st);
 }
 
 static void validate_tree(const p3g_tree* tree, bool flat) {
@@ -235,16 +300,22 @@ static void validate_tree(const p3g_tree* tree, bool flat) {
     }
 }
 
-void tree_prepare(p3g_ctx* ctx, p3g_tree* tree, unsigned cap_height, bool flat, cudaStream_t st, bool sync_upload) {
+void tree_prepare(p3g_ctx* ctx, p3g_tree* tree, unsigned cap_height, bool flat, cudaStream_t st, bool sync_upload,
+                  bool staged) {
     validate_tree(tree, flat);
     P3G_REQUIRE(cap_height < 63, "mmcs_commit: cap_height too large");
     if (tree->field == P3G_BABYBEAR) {
         if (!ctx->has_p2bb) throw Error(P3G_ESTATE, "Poseidon2 constants for BabyBear are not set");
-        prepare<HBB>(ctx, tree, cap_height, flat, st, sync_upload);
+        prepare<HBB>(ctx, tree, cap_height, flat, st, sync_upload, staged);
     } else {
         if (!ctx->has_p2gl) throw Error(P3G_ESTATE, "Poseidon2 constants for Goldilocks are not set");
-        prepare<HGL>(ctx, tree, cap_height, flat, st, sync_upload);
+        prepare<HGL>(ctx, tree, cap_height, flat, st, sync_upload, staged);
     }
+}
+
+static void release_stage_bufs(p3g_ctx* ctx, p3g_tree* tree, cudaStream_t st) {
+    for (void* p : tree->stage_bufs) ctx->release(p, st);
+    tree->stage_bufs.clear();
 }
 
 void tree_enqueue(p3g_ctx* ctx, p3g_tree* tree, cudaStream_t st) {
@@ -252,11 +323,28 @@ void tree_enqueue(p3g_ctx* ctx, p3g_tree* tree, cudaStream_t st) {
     else enqueue<HGL>(ctx, tree, ctx->p2gl, st);
 }
 
+void tree_hash_ready(p3g_ctx* ctx, p3g_tree* tree, size_t n_ready, cudaStream_t st) {
+    if (tree->field == P3G_BABYBEAR) hash_stages<HBB>(ctx, tree, ctx->p2bb, n_ready, st);
+    else hash_stages<HGL>(ctx, tree, ctx->p2gl, n_ready, st);
+}
+
+void tree_finish(p3g_ctx* ctx, p3g_tree* tree, cudaStream_t st) {
+    if (tree->field == P3G_BABYBEAR) {
+        hash_stages<HBB>(ctx, tree, ctx->p2bb, ~size_t(0), st);
+        levels<HBB>(ctx, tree, ctx->p2bb, st);
+    } else {
+        hash_stages<HGL>(ctx, tree, ctx->p2gl, ~size_t(0), st);
+        levels<HGL>(ctx, tree, ctx->p2gl, st);
+    }
+    release_stage_bufs(ctx, tree, st);  // stream-ordered: after the last part that reads them
+}
+
 void tree_release(p3g_ctx* ctx, p3g_tree* tree, cudaStream_t st) {
     if (tree->d_digests) ctx->release(tree->d_digests, st);
     if (tree->d_desc) ctx->release(tree->d_desc, st);
     for (void* p : tree->inj) ctx->release(p, st);
     for (void* p : tree->owned) ctx->release(p, st);
+    release_stage_bufs(ctx, tree, st);
     tree->d_digests = tree->d_desc = nullptr;
     tree->inj.clear();
     tree->owned.clear();

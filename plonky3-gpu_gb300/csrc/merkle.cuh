@@ -26,12 +26,15 @@ struct Group {
 
 // Sponge over the concatenated row r of the group (overwrite absorb,
 // padding_free_sponge.hpp:63-87); leaves the state (internal form) in s.
+// s0, when given, is the state (internal form) after an earlier part of the
+// row whose length was a multiple of RATE: the sponge resumes from it.
 template <class H, int D, int RF, int RP>
 __device__ __forceinline__ void hash_group(const Group<typename H::T>& g, uint64_t r,
-                                           const typename H::Params& p, typename H::T* s) {
+                                           const typename H::Params& p, typename H::T* s,
+                                           const typename H::T* s0) {
     using T = typename H::T;
 #pragma unroll
-    for (int i = 0; i < H::W; ++i) s[i] = 0;
+    for (int i = 0; i < H::W; ++i) s[i] = s0 ? s0[i] : T(0);
     int m = 0;
     uint32_t c = 0;
 #pragma unroll 1
@@ -102,8 +105,14 @@ struct HashGroup {
     uint32_t nent;
     uint32_t vec;    // single matrix, width % 4 == 0, 16-byte aligned
     uint32_t pad;
+    // A group hashed in parts (staged build): the sponge states (rows x W,
+    // internal form) the part resumes from, and, for every part but the
+    // last, the states it leaves instead of digests.  Both null otherwise.
+    const T* state_in;
+    T* state_out;
 };
-// Device descriptor block: [counter (8 bytes, zeroed per launch) | groups | entries].
+// Device descriptor block: [counter (8 bytes, zeroed per launch) | groups | entries];
+// a launch takes a run of at most MAXG consecutive groups.
 constexpr size_t HASH_DESC_HEADER = 256;
 
 template <class H, int D, int RF, int RP>
@@ -143,10 +152,16 @@ __global__ void __launch_bounds__(HASH_ROWS) k_hash_groups(typename H::Params p,
         const uint64_t r = (u - sg[g].unit0) * HASH_ROWS + threadIdx.x;
         if (r < sg[g].rows) {
             T s[H::W];
-            hash_group<H, D, RF, RP>(cur, r, p, s);
-            T* o = sg[g].out + r * H::DIG;
+            const T* s0 = sg[g].state_in ? sg[g].state_in + r * H::W : nullptr;
+            hash_group<H, D, RF, RP>(cur, r, p, s, s0);
+            if (T* so = sg[g].state_out) {
 #pragma unroll
-            for (int i = 0; i < H::DIG; ++i) o[i] = H::squeeze(s[i]);
+                for (int i = 0; i < H::W; ++i) so[r * H::W + i] = s[i];
+            } else {
+                T* o = sg[g].out + r * H::DIG;
+#pragma unroll
+                for (int i = 0; i < H::DIG; ++i) o[i] = H::squeeze(s[i]);
+            }
         }
         __syncthreads();  // `unit` and `cur` are rewritten next iteration
     }
@@ -249,9 +264,10 @@ __global__ void __launch_bounds__(128) k_grind(typename H::Params p, GrindArgs<t
 template <class H, int D, int RF, int RP>
 struct Launch {
     using T = typename H::T;
-    // persistent hashing of all groups; `desc` = device descriptor block
-    static void hash_groups(const typename H::Params& p, void* desc, int ngroups, uint64_t total_units,
-                            int sm_count, cudaStream_t st);
+    // persistent hashing of ngroups groups (work counter zeroed first)
+    static void hash_groups(const typename H::Params& p, unsigned long long* counter, const HashGroup<T>* groups,
+                            int ngroups, const HashEntry<T>* ents, uint64_t total_units, int sm_count,
+                            cudaStream_t st);
     static void level(const typename H::Params& p, const T* child, uint64_t nchild, T* parent, uint64_t nparent,
                       const T* inj, cudaStream_t st);
     static void permute(const typename H::Params& p, T* states, uint64_t n, cudaStream_t st);
@@ -261,8 +277,9 @@ struct Launch {
 
 #ifdef P3G_MERKLE_INSTANTIATE
 template <class H, int D, int RF, int RP>
-void Launch<H, D, RF, RP>::hash_groups(const typename H::Params& p, void* desc, int ngroups, uint64_t total_units,
-                                       int sm_count, cudaStream_t st) {
+void Launch<H, D, RF, RP>::hash_groups(const typename H::Params& p, unsigned long long* counter,
+                                       const HashGroup<T>* groups, int ngroups, const HashEntry<T>* ents,
+                                       uint64_t total_units, int sm_count, cudaStream_t st) {
     if (total_units == 0) return;
     static int occ = 0;  // resident CTAs per SM (same for every device of one architecture)
     if (occ == 0) {
@@ -271,10 +288,6 @@ void Launch<H, D, RF, RP>::hash_groups(const typename H::Params& p, void* desc, 
         occ = o > 0 ? o : 1;
     }
     const int grid = occ * sm_count;
-    char* base = static_cast<char*>(desc);
-    auto* counter = reinterpret_cast<unsigned long long*>(base);
-    auto* groups = reinterpret_cast<const HashGroup<T>*>(base + HASH_DESC_HEADER);
-    auto* ents = reinterpret_cast<const HashEntry<T>*>(base + HASH_DESC_HEADER + sizeof(HashGroup<T>) * MAXG);
     P3G_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned long long), st));
     const int blocks = int(std::min<uint64_t>(uint64_t(grid), total_units));
     k_hash_groups<H, D, RF, RP><<<blocks, HASH_ROWS, 0, st>>>(p, groups, ngroups, ents, total_units, counter);

@@ -46,6 +46,22 @@ def test_config1_commit_openings_verify(gpu_ctx):
     d.free()
 
 
+def test_config1_host_commit_equals_device_commit(gpu_ctx):
+    """The end-to-end call (pinned host trace, narrow first chunks, row hashes
+    resumed across chunks) gives every digest layer of the device commit."""
+    rng = np.random.default_rng(22)
+    t = rng.integers(0, O.BB_P, size=(1 << 20, 256), dtype=np.uint32)
+    d = gpu_ctx.to_device(t)
+    dev = gpu_ctx.commit_traces_device(P.BABYBEAR, [(d.ptr, 20, 256, 1, 31)], 0)
+    host = gpu_ctx.commit_traces_host(P.BABYBEAR, [(t.ctypes.data, 20, 256, 1, 31)], 0)
+    for a, b in zip(host.layers(), dev.layers()):
+        assert np.array_equal(a, b)
+    _verify_openings(host, [1 << 21] * 4, [32, 32, 64, 128], 6, 2)  # leaf matrices = the column chunks
+    host.free()
+    dev.free()
+    d.free()
+
+
 def test_config3_batched_plan_openings_verify(gpu_ctx):
     rng = np.random.default_rng(3)
     shapes = [(int(rng.integers(12, 19)), int(rng.integers(8, 513))) for _ in range(64)]

@@ -1,7 +1,9 @@
-"""p3g_commit_traces_host: traces in host memory, copied in 512-byte column
-chunks on a second stream while earlier chunks' LDEs run.  The commitment and
-every opening must equal p3g_commit_traces on the same traces (and the
-oracle's), whatever the chunking."""
+"""p3g_commit_traces_host: traces in host memory, copied in column chunks on a
+second stream while earlier chunks' LDEs and row hashes run (a large first
+trace starts with narrow chunks; each chunk's row hashes resume the sponge
+state of the chunks before it where the row length so far is a multiple of the
+rate).  The commitment and every opening must equal p3g_commit_traces on the
+same traces (and the oracle's), whatever the chunking."""
 import numpy as np
 import pytest
 
@@ -64,3 +66,31 @@ def test_host_commit_rejects_bad_arguments(gpu_ctx):
     t = np.zeros((16, 4), np.uint32)
     with pytest.raises(P.P3GError):
         gpu_ctx.commit_traces_host(P.BABYBEAR, [(t.ctypes.data, 4, 4, 1, P.BB_P)], 0)  # shift not canonical
+
+
+@pytest.mark.parametrize("field,shapes", [
+    # first trace 32+32+64+128+44 columns; then equal-height traces after a
+    # row length that is not a multiple of the rate (no cut), then a cut again
+    (P.BABYBEAR, [(14, 300), (14, 5), (14, 3), (14, 64), (12, 9)]),
+    (P.BABYBEAR, [(15, 256)]),
+    (P.BABYBEAR, [(14, 20), (15, 8)]),  # narrow first trace, shorter than a chunk
+    (P.GOLDILOCKS, [(14, 100), (14, 3), (13, 8)]),
+])
+def test_host_commit_staged_row_hashes(gpu_ctx, field, shapes):
+    rng = np.random.default_rng(63 + len(shapes))
+    p = O.BB_P if field == P.BABYBEAR else O.GL_P
+    dt = np.uint32 if field == P.BABYBEAR else np.uint64
+    shift = 31 if field == P.BABYBEAR else 7
+    traces = [rng.integers(0, p, size=(1 << lh, w), dtype=dt) for lh, w in shapes]
+    bufs = [gpu_ctx.to_device(t) for t in traces]
+    dev = gpu_ctx.commit_traces_device(field, [(b.ptr, lh, w, 1, shift) for b, (lh, w) in zip(bufs, shapes)], 0)
+    host = gpu_ctx.commit_traces_host(field, [(t.ctypes.data, lh, w, 1, shift) for t, (lh, w) in zip(traces, shapes)], 0)
+    for a, b in zip(host.layers(), dev.layers()):
+        assert np.array_equal(a, b)
+    if field == P.GOLDILOCKS:
+        want = O.mmcs_commit(O.gl8_params(), [O.gl_coset_lde(t, 1, 7, True) for t in traces], 0)
+        assert np.array_equal(host.layers()[-1], want[-1])
+    host.free()
+    dev.free()
+    for b in bufs:
+        b.free()
