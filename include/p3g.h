@@ -341,6 +341,66 @@ P3G_API int p3g_grind(p3g_ctx *ctx, int field, const void *h_sponge_state, const
                       uint32_t n_input, uint32_t bits, uint64_t max_witness, uint64_t *witness_out,
                       void *stream);
 
+/* ------------------------------------------------------------ FRI prover
+ * prove_fri (fri_prover.hpp:35-265) for BabyBear / BabyBear^4 over inputs
+ * resident on the device, with the Fiat-Shamir transcript on the device as
+ * well: the challenger is DuplexChallenger<BabyBear, Perm, 16, 8> over the
+ * context's Poseidon2-16, stepped by one device thread, so the rounds run
+ * without a host round trip.  The transcript calls are those of the FRI tests'
+ * transcript wrapper (fri_test.cpp:100-120): observe_commitment observes the
+ * root, sample_challenge draws four samples, observe_challenge observes four
+ * coefficients, observe_arity observes BabyBear(log_arity), grind is
+ * DuplexChallenger::grind. */
+typedef struct {
+    uint32_t log_blowup;
+    uint32_t log_final_poly_len;     /* <= 10 */
+    uint32_t max_log_arity;          /* 1..3 */
+    uint32_t num_queries;            /* <= 1024 */
+    uint32_t commit_proof_of_work_bits;  /* <= 24 */
+    uint32_t query_proof_of_work_bits;   /* <= 24 */
+} p3g_fri_params;                    /* FriParameters (fri_params.hpp:9-24) without the MMCS */
+
+/* DuplexChallenger<BabyBear, Perm, 16, 8>'s state (duplex_challenger.hpp:46-49),
+ * canonical values; input[0..n_input) and output[0..n_output) are live. */
+typedef struct {
+    uint32_t sponge_state[16];
+    uint32_t input[8];
+    uint32_t output[8];
+    uint32_t n_input;   /* < 8 */
+    uint32_t n_output;  /* <= 8 */
+} p3g_challenger;
+
+/* The commit-phase rounds prove_fri makes for these input heights and their
+ * log arities (compute_log_arity_for_round, fri_params.hpp:36-57), for sizing
+ * p3g_fri_prove's outputs.  log_arities has room for 32. */
+P3G_API int p3g_fri_rounds(const uint32_t *log_heights, uint32_t n_inputs, const p3g_fri_params *params,
+                           uint32_t *n_rounds, uint32_t *log_arities);
+
+/* d_inputs[i]: 2^log_heights[i] BabyBear^4 values (the reduced openings, rows
+ * bit-reversed), heights strictly decreasing, the smallest above
+ * log_blowup + log_final_poly_len (fri_prover.hpp:50-67); they are not
+ * modified.  challenger: the state before prove_fri on entry, after it on
+ * return.  Outputs (host, any may be NULL), for R rounds with log arities a_r
+ * on heights 2^h_r:
+ *   h_commits           R x 8      each round's root (commit_phase_commits)
+ *   h_commit_witnesses  R          (commit_pow_witnesses)
+ *   h_final_poly        2^log_final_poly_len x 4
+ *   h_query_witness     1          (query_pow_witness)
+ *   h_query_indices     num_queries (sample_bits(log_max_height), :207)
+ *   h_rows              rounds in order, num_queries x (4 << a_r) each: the
+ *                       committed row holding the query (sibling_values = the
+ *                       row without the query's position, :221-241)
+ *   h_paths             rounds in order, num_queries x (h_r - a_r) x 8 each:
+ *                       the row's Merkle path (opening_proof, :243-244)
+ * The input MMCS openings at the query indices are the caller's (its own trees,
+ * p3g_mmcs_open_batch).  P3G_ENOTFOUND if a proof-of-work search (one bounded
+ * launch of 2^(bits+6) candidates) found no witness.  Synchronises the stream. */
+P3G_API int p3g_fri_prove(p3g_ctx *ctx, const void *const *d_inputs, const uint32_t *log_heights,
+                          uint32_t n_inputs, const p3g_fri_params *params, p3g_challenger *challenger,
+                          uint32_t *h_commits, uint64_t *h_commit_witnesses, uint32_t *h_final_poly,
+                          uint64_t *h_query_witness, uint64_t *h_query_indices, uint32_t *h_rows,
+                          uint32_t *h_paths, void *stream);
+
 /* ------------------------------------------------------------ PCS open
  * TwoAdicFriPcs::open's two passes over a BabyBear LDE resident on the device
  * (two_adic_fri_pcs.hpp:271-410).  d_lde: (1 << log_n) x width evaluations on

@@ -512,6 +512,11 @@ class Transcript:
         self.sample()
         return w
 
+    def sample_bits(self, bits: int) -> int:
+        """sample_bits (duplex_challenger.hpp:129-141) for bits <= 31: one sample."""
+        assert bits <= 31
+        return self.sample() & ((1 << bits) - 1)
+
     def check_witness(self, bits: int, w: int) -> bool:
         self._observe_witness(w)
         return self.sample() & ((1 << bits) - 1) == 0

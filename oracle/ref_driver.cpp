@@ -419,6 +419,21 @@ int main(int argc, char** argv) {
             for (size_t k = 0; k < 4; ++k) put(v[k]);
         // then: the query-phase proof-of-work witness (query_proof_of_work_bits = 8)
         put64(proof.query_pow_witness);
+        // then every query's commit-phase openings: per round the sibling values
+        // and the Merkle path of the committed row
+        put32(uint32_t(proof.query_proofs.size()));
+        for (const auto& qp : proof.query_proofs) {
+            put32(uint32_t(qp.commit_phase_openings.size()));
+            for (const auto& step : qp.commit_phase_openings) {
+                put32(uint32_t(step.log_arity));
+                put32(uint32_t(step.sibling_values.size()));
+                for (const auto& v : step.sibling_values)
+                    for (size_t k = 0; k < 4; ++k) put(v[k]);
+                put32(uint32_t(step.opening_proof.size()));
+                for (const auto& d : step.opening_proof)
+                    for (const auto& e : d) put(e);
+            }
+        }
     } else if (cmd == "grind") {
         // grind <seed> <n_obs> <bits>... : the reference's DuplexChallenger (BB16,
         // rate 8, seeded permutation) observes n_obs seeded values, then for each

@@ -19,7 +19,7 @@ BUILD = os.path.join(PKG, "_build")
 LIBDIR = os.path.join(PKG, "lib")
 LIB = os.path.join(LIBDIR, "libp3g_gb300.so")
 SOURCES = ["capi.cu", "lde_bb.cu", "lde_gl.cu", "dft_bb.cu", "dft_gl.cu", "merkle.cu", "merkle_s1.cu", "merkle_s2.cu",
-           "merkle_s3.cu", "merkle_s4.cu", "fold.cu", "open.cu", "lde_noalloc.cu", "plan.cu", "server.cu"]
+           "merkle_s3.cu", "merkle_s4.cu", "fold.cu", "open.cu", "fri.cu", "lde_noalloc.cu", "plan.cu", "server.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

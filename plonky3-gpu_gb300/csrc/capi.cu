@@ -600,6 +600,26 @@ int p3g_grind(p3g_ctx* ctx, int field, const void* h_sponge_state, const void* h
     API_END
 }
 
+int p3g_fri_rounds(const uint32_t* log_heights, uint32_t n_inputs, const p3g_fri_params* params, uint32_t* n_rounds,
+                   uint32_t* log_arities) {
+    API_BEGIN
+    P3G_REQUIRE(log_heights && params && n_rounds, "fri_rounds: null argument");
+    p3g::fri_rounds(log_heights, n_inputs, *params, n_rounds, log_arities);
+    API_END
+}
+
+int p3g_fri_prove(p3g_ctx* ctx, const void* const* d_inputs, const uint32_t* log_heights, uint32_t n_inputs,
+                  const p3g_fri_params* params, p3g_challenger* challenger, uint32_t* h_commits,
+                  uint64_t* h_commit_witnesses, uint32_t* h_final_poly, uint64_t* h_query_witness,
+                  uint64_t* h_query_indices, uint32_t* h_rows, uint32_t* h_paths, void* stream) {
+    API_BEGIN
+    P3G_REQUIRE(ctx && d_inputs && log_heights && params && challenger, "fri_prove: null argument");
+    DeviceGuard g(ctx->device);
+    p3g::fri_prove(ctx, d_inputs, log_heights, n_inputs, *params, challenger, h_commits, h_commit_witnesses,
+                   h_final_poly, h_query_witness, h_query_indices, h_rows, h_paths, S(stream));
+    API_END
+}
+
 int p3g_pcs_open_values(p3g_ctx* ctx, const void* d_lde, uint32_t log_n, uint32_t width, int bitrev_rows,
                         uint32_t shift, const uint32_t* h_points, uint32_t n_points, uint32_t* h_out, void* stream) {
     API_BEGIN

@@ -18,10 +18,13 @@ namespace p3g {
 
 __device__ __forceinline__ bb4 bb4_mul(const bb4& a, const bb4& b) { return bb4_mul_cm(a, bb4_to_mont(b)); }
 
+// beta_dev, when given, holds beta (canonical) in device memory -- written by
+// the device transcript -- and replaces the by-value argument.
 __global__ void k_fold2(const bb4* __restrict__ in, bb4* __restrict__ out, uint64_t n, int log_height,
-                        bb4 beta_m, uint32_t inv2_m, RootTab<FBB> roots) {
+                        bb4 beta_m, const bb4* beta_dev, uint32_t inv2_m, RootTab<FBB> roots) {
     uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    if (beta_dev) beta_m = bb4_to_mont(*beta_dev);
     const int log_folded = log_height - 1;
     const uint32_t xinv_m = roots.omega_inv(log_height, bitrev_dev(unsigned(i), log_folded));
     const uint32_t inv2x_m = bb::mmul(xinv_m, inv2_m);
@@ -33,10 +36,12 @@ __global__ void k_fold2(const bb4* __restrict__ in, bb4* __restrict__ out, uint6
 
 template <int LA>
 __global__ void k_fold_general(const bb4* __restrict__ in, bb4* __restrict__ out, uint64_t n, int log_height,
-                               bb4 beta, uint32_t w_c, uint32_t winv_c, uint32_t arity_inv_c, RootTab<FBB> roots) {
+                               bb4 beta, const bb4* beta_dev, uint32_t w_c, uint32_t winv_c, uint32_t arity_inv_c,
+                               RootTab<FBB> roots) {
     constexpr int A = 1 << LA;
     uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    if (beta_dev) beta = *beta_dev;
     const int log_folded = log_height - LA;
     const uint32_t x_m = roots.omega(log_height, bitrev_dev(unsigned(i), log_folded));
     const uint32_t x = bb::mmul(x_m, 1u);
@@ -90,29 +95,32 @@ __global__ void k_fold_general(const bb4* __restrict__ in, bb4* __restrict__ out
 }
 
 void fold_bb4(p3g_ctx* ctx, const uint32_t* in, int log_height, int log_arity, const uint32_t beta[4],
-              uint32_t* out, cudaStream_t st) {
+              uint32_t* out, cudaStream_t st, const uint32_t* d_beta) {
     P3G_REQUIRE(log_arity >= 1 && log_arity <= 3, "fold_matrix: log_arity must be 1, 2 or 3");
     P3G_REQUIRE(log_arity <= log_height && log_height <= 27, "fold_matrix: bad log_height");
-    for (int k = 0; k < 4; ++k) P3G_REQUIRE(beta[k] < bb::P, "fold_matrix: beta must be canonical");
+    if (!d_beta)
+        for (int k = 0; k < 4; ++k) P3G_REQUIRE(beta[k] < bb::P, "fold_matrix: beta must be canonical");
     const uint64_t n = (uint64_t(1) << log_height) >> log_arity;
     const bb4* din = reinterpret_cast<const bb4*>(in);
     bb4* dout = reinterpret_cast<bb4*>(out);
-    bb4 b = {{beta[0], beta[1], beta[2], beta[3]}};
+    const bb4* bdev = reinterpret_cast<const bb4*>(d_beta);
+    bb4 b = {{0, 0, 0, 0}};
+    if (!d_beta) b = {{beta[0], beta[1], beta[2], beta[3]}};
     const unsigned grid = unsigned((n + 255) / 256);
     if (log_arity == 1) {
-        bb4 bm = {{bb::to_mont(beta[0]), bb::to_mont(beta[1]), bb::to_mont(beta[2]), bb::to_mont(beta[3])}};
-        k_fold2<<<grid, 256, 0, st>>>(din, dout, n, log_height, bm, bb::to_mont(bb::h_inv(2)), ctx->bb_roots());
+        bb4 bm = {{bb::to_mont(b.c[0]), bb::to_mont(b.c[1]), bb::to_mont(b.c[2]), bb::to_mont(b.c[3])}};
+        k_fold2<<<grid, 256, 0, st>>>(din, dout, n, log_height, bm, bdev, bb::to_mont(bb::h_inv(2)), ctx->bb_roots());
         P3G_LAUNCHED();
     } else {
         const uint32_t w = bb::two_adic_generator(unsigned(log_arity));
         const uint32_t winv = bb::h_pow(w, (uint64_t(1) << log_arity) - 1);
         const uint32_t ainv = bb::h_pow(bb::h_inv(2), uint64_t(log_arity));
         if (log_arity == 2) {
-            k_fold_general<2><<<grid, 256, 0, st>>>(din, dout, n, log_height, b, bb::to_mont(w), bb::to_mont(winv),
-                                                   bb::to_mont(ainv), ctx->bb_roots());
+            k_fold_general<2><<<grid, 256, 0, st>>>(din, dout, n, log_height, b, bdev, bb::to_mont(w),
+                                                   bb::to_mont(winv), bb::to_mont(ainv), ctx->bb_roots());
         } else {
-            k_fold_general<3><<<grid, 256, 0, st>>>(din, dout, n, log_height, b, bb::to_mont(w), bb::to_mont(winv),
-                                                   bb::to_mont(ainv), ctx->bb_roots());
+            k_fold_general<3><<<grid, 256, 0, st>>>(din, dout, n, log_height, b, bdev, bb::to_mont(w),
+                                                   bb::to_mont(winv), bb::to_mont(ainv), ctx->bb_roots());
         }
         P3G_LAUNCHED();
     }
@@ -121,19 +129,23 @@ void fold_bb4(p3g_ctx* ctx, const uint32_t* in, int log_height, int log_arity, c
 
 // y[i] += a * x[i] over BabyBear^4 (a in Montgomery form): prove_fri's mix-in of
 // the next reduced opening, current[k] += beta^arity * next[k] (fri_prover.hpp:127-138).
-__global__ void k_bb4_axpy(bb4* __restrict__ y, const bb4* __restrict__ x, uint64_t n, bb4 am) {
+__global__ void k_bb4_axpy(bb4* __restrict__ y, const bb4* __restrict__ x, uint64_t n, bb4 am, const bb4* a_dev) {
     const uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    if (a_dev) am = bb4_to_mont(*a_dev);
     y[i] = bb4_add(y[i], bb4_mul_cm(x[i], am));
 }
 
-void bb4_axpy(p3g_ctx*, uint32_t* y, const uint32_t* x, uint64_t n, const uint32_t* a, cudaStream_t st) {
-    P3G_REQUIRE(y && x && a, "bb4_axpy: null argument");
-    for (int k = 0; k < 4; ++k) P3G_REQUIRE(a[k] < bb::P, "bb4_axpy: a must be canonical");
+void bb4_axpy(p3g_ctx*, uint32_t* y, const uint32_t* x, uint64_t n, const uint32_t* a, cudaStream_t st,
+              const uint32_t* d_a) {
+    P3G_REQUIRE((n == 0 || (y && x)) && (a || d_a), "bb4_axpy: null argument");
+    if (!d_a)
+        for (int k = 0; k < 4; ++k) P3G_REQUIRE(a[k] < bb::P, "bb4_axpy: a must be canonical");
     if (n == 0) return;
-    const bb4 am = {{bb::to_mont(a[0]), bb::to_mont(a[1]), bb::to_mont(a[2]), bb::to_mont(a[3])}};
+    bb4 am = {{0, 0, 0, 0}};
+    if (!d_a) am = {{bb::to_mont(a[0]), bb::to_mont(a[1]), bb::to_mont(a[2]), bb::to_mont(a[3])}};
     k_bb4_axpy<<<unsigned((n + 255) / 256), 256, 0, st>>>(reinterpret_cast<bb4*>(y), reinterpret_cast<const bb4*>(x),
-                                                         n, am);
+                                                         n, am, reinterpret_cast<const bb4*>(d_a));
     P3G_LAUNCHED();
     P3G_CUDA(cudaGetLastError());
 }

@@ -147,8 +147,17 @@ void pcs_open_values(p3g_ctx* ctx, const uint32_t* lde, int log_n, int w, int bi
 void pcs_reduce(p3g_ctx* ctx, const uint32_t* lde, int log_n, int w, int bitrev_rows, uint32_t shift,
                 const uint32_t* h_points, int m, const uint32_t* h_opened, const uint32_t* h_alpha, uint64_t alpha_pow,
                 int q_bitrev, uint32_t* q, cudaStream_t st);
+// prove_fri with the transcript on the device (fri.cu)
+void fri_rounds(const uint32_t* log_heights, uint32_t n_inputs, const p3g_fri_params& prm, uint32_t* n_rounds,
+                uint32_t* log_arities);
+void fri_prove(p3g_ctx* ctx, const void* const* d_inputs, const uint32_t* log_heights, uint32_t n_inputs,
+               const p3g_fri_params& prm, p3g_challenger* chal, uint32_t* h_commits, uint64_t* h_commit_witnesses,
+               uint32_t* h_final_poly, uint64_t* h_query_witness, uint64_t* h_query_indices, uint32_t* h_rows,
+               uint32_t* h_paths, cudaStream_t st);
 // y += a * x over BabyBear^4 (fold.cu)
-void bb4_axpy(p3g_ctx* ctx, uint32_t* y, const uint32_t* x, uint64_t n, const uint32_t* a, cudaStream_t st);
+// (d_a: a in device memory instead, canonical)
+void bb4_axpy(p3g_ctx* ctx, uint32_t* y, const uint32_t* x, uint64_t n, const uint32_t* a, cudaStream_t st,
+              const uint32_t* d_a = nullptr);
 // device copies of the prepared DFT twiddle tables (cudaMalloc'd; the context frees them)
 void* make_dft_tw_bb();
 void* make_dft_tw_gl();
@@ -183,9 +192,18 @@ bool grind(p3g_ctx* ctx, int field, const void* h_state, const void* h_input, ui
            uint64_t limit, uint64_t* witness, cudaStream_t st);
 void open_batch(p3g_ctx* ctx, const p3g_tree* tree, const uint64_t* h_idx, size_t nq,
                 void* h_rows, void* h_proof, cudaStream_t st);
+// open_batch with the indices, rows and proofs in device memory; no
+// synchronisation.  Indices must be below the tree's leaf count.
+void open_batch_dev(p3g_ctx* ctx, const p3g_tree* tree, const uint64_t* d_idx, size_t nq, void* d_rows,
+                    void* d_proof, cudaStream_t st);
+// The BabyBear proof-of-work search over [0, count) with its arguments in
+// device memory (GrindArgs<uint32_t, 16> in internal form, merkle.cuh);
+// *found must hold ~0 before.
+void grind_bb_dev(p3g_ctx* ctx, const void* d_args, uint64_t count, unsigned long long* found, cudaStream_t st);
 
+// (d_beta: beta in device memory instead, canonical)
 void fold_bb4(p3g_ctx* ctx, const uint32_t* in, int log_height, int log_arity,
-              const uint32_t beta[4], uint32_t* out, cudaStream_t st);
+              const uint32_t beta[4], uint32_t* out, cudaStream_t st, const uint32_t* d_beta = nullptr);
 
 inline int ceil_div(int64_t a, int64_t b) { return int((a + b - 1) / b); }
 

@@ -101,24 +101,6 @@ struct PermFn {
     void operator()() const { Launch<H, D, RF, RP>::permute(*p, s, n, st); }
 };
 
-// Calls fn.template operator()<D, RF, RP>() for a supported round schedule.
-template <class Fn>
-static void dispatch_bb(const p3g_ctx* ctx, const Fn& fn) {
-    if (!ctx->has_p2bb) throw Error(P3G_ESTATE, "Poseidon2 constants for BabyBear are not set");
-    const int d = ctx->bb_d, rf = ctx->bb_rf, rp = ctx->bb_rp;
-    if (rf == 8 && d == 7 && rp == 13) return fn.template operator()<7, 8, 13>();
-    if (rf == 8 && d == 7 && rp == 22) return fn.template operator()<7, 8, 22>();
-    if (rf == 8 && d == 5 && rp == 14) return fn.template operator()<5, 8, 14>();
-    throw Error(P3G_EUNSUPPORTED, "BabyBear Poseidon2 schedule not built (supported: x^7 8+13, x^7 8+22, x^5 8+14)");
-}
-template <class Fn>
-static void dispatch_gl(const p3g_ctx* ctx, const Fn& fn) {
-    if (!ctx->has_p2gl) throw Error(P3G_ESTATE, "Poseidon2 constants for Goldilocks are not set");
-    const int d = ctx->gl_d, rf = ctx->gl_rf, rp = ctx->gl_rp;
-    if (rf == 8 && d == 7 && rp == 22) return fn.template operator()<7, 8, 22>();
-    throw Error(P3G_EUNSUPPORTED, "Goldilocks Poseidon2 schedule not built (supported: x^7 8+22)");
-}
-
 // ------------------------------------------------------------------ tree build
 template <class H>
 static void prepare(p3g_ctx* ctx, p3g_tree* tree, unsigned cap_height, bool flat, cudaStream_t st,
@@ -372,13 +354,13 @@ void permute_states(p3g_ctx* ctx, int field, void* d_states, size_t n, cudaStrea
 template <class H>
 struct GrindFn {
     const typename H::Params* p;
-    const GrindArgs<typename H::T, H::W>* a;
+    const GrindArgs<typename H::T, H::W>* a;  // device
     uint64_t base, count;
     unsigned long long* found;
     int sm_count;
     cudaStream_t st;
     template <int D, int RF, int RP>
-    void operator()() const { Launch<H, D, RF, RP>::grind(*p, *a, base, count, found, sm_count, st); }
+    void operator()() const { Launch<H, D, RF, RP>::grind(*p, a, base, count, found, sm_count, st); }
 };
 
 template <class H>
@@ -390,21 +372,26 @@ static bool grind_impl(p3g_ctx* ctx, const typename H::Params* params, const typ
     for (int i = 0; i < H::W; ++i) a.state[i] = H::absorb(i < int(n_input) ? h_input[i] : h_state[i]);
     a.n_input = n_input;
     a.mask = bits == 64 ? ~uint64_t(0) : (uint64_t(1) << bits) - 1;
-    auto* found = static_cast<unsigned long long*>(ctx->alloc(sizeof(unsigned long long), st));
+    // device block: [found (8 bytes) | arguments]
+    char* blk = static_cast<char*>(ctx->alloc(256 + sizeof a, st));
     struct Release {
         p3g_ctx* c;
         void* p;
         cudaStream_t s;
         ~Release() { c->release(p, s); }
-    } rel{ctx, found, st};
+    } rel{ctx, blk, st};
+    auto* found = reinterpret_cast<unsigned long long*>(blk);
+    auto* d_args = reinterpret_cast<GrindArgs<T, H::W>*>(blk + 256);
     P3G_CUDA(cudaMemsetAsync(found, 0xFF, sizeof(unsigned long long), st));
+    // pageable source: staged before the call returns
+    P3G_CUDA(cudaMemcpyAsync(d_args, &a, sizeof a, cudaMemcpyHostToDevice, st));
     // Launches of at most 2^30 candidates (well under a second each); the
     // first is sized so that it holds a hit with probability 1 - e^-16.
     uint64_t chunk = uint64_t(1) << std::min(30u, std::max(20u, bits + 4));
     unsigned long long hit = ~0ull;
     for (uint64_t base = 0; base < limit; ) {
         const uint64_t count = std::min(chunk, limit - base);
-        GrindFn<H> fn{params, &a, base, count, found, ctx->sm_count, st};
+        GrindFn<H> fn{params, d_args, base, count, found, ctx->sm_count, st};
         if constexpr (std::is_same<H, HBB>::value) dispatch_bb(ctx, fn);
         else dispatch_gl(ctx, fn);
         P3G_CUDA(cudaMemcpyAsync(&hit, found, sizeof hit, cudaMemcpyDeviceToHost, st));
@@ -432,55 +419,82 @@ bool grind(p3g_ctx* ctx, int field, const void* h_state, const void* h_input, ui
                            static_cast<const uint64_t*>(h_input), n_input, bits, limit, witness, st);
 }
 
+// Device descriptors of an opening: matrices and layer tables, uploaded from
+// pageable memory (staged before the call returns).
+static char* open_desc(p3g_ctx* ctx, const p3g_tree* tree, cudaStream_t st, uint32_t* row_elems, size_t* o_loff,
+                       size_t* o_lsz) {
+    std::vector<OpenMat> om(tree->mats.size());
+    uint32_t re = 0;
+    for (size_t i = 0; i < om.size(); ++i) {
+        om[i] = {tree->mats[i].d_data, tree->mats[i].height, tree->mats[i].width, re};
+        re += tree->mats[i].width;
+    }
+    size_t off = 0;
+    auto take = [&](size_t bytes) { size_t o = off; off += (bytes + 255) / 256 * 256; return o; };
+    const size_t o_mats = take(sizeof(OpenMat) * om.size());
+    *o_loff = take(8 * tree->layer_off.size());
+    *o_lsz = take(8 * tree->layer_size.size());
+    char* buf = static_cast<char*>(ctx->alloc(off, st));
+    P3G_CUDA(cudaMemcpyAsync(buf + o_mats, om.data(), sizeof(OpenMat) * om.size(), cudaMemcpyHostToDevice, st));
+    P3G_CUDA(cudaMemcpyAsync(buf + *o_loff, tree->layer_off.data(), 8 * tree->layer_off.size(), cudaMemcpyHostToDevice, st));
+    P3G_CUDA(cudaMemcpyAsync(buf + *o_lsz, tree->layer_size.data(), 8 * tree->layer_size.size(), cudaMemcpyHostToDevice, st));
+    *row_elems = re;
+    return buf;
+}
+
+void open_batch_dev(p3g_ctx* ctx, const p3g_tree* tree, const uint64_t* d_idx, size_t nq, void* d_rows,
+                    void* d_proof, cudaStream_t st) {
+    if (nq == 0) return;
+    const uint64_t max_h = tree->layer_size[0];
+    const int nproof = int(tree->layer_size.size()) - 1;
+    uint32_t row_elems = 0;
+    size_t o_loff = 0, o_lsz = 0;
+    char* buf = open_desc(ctx, tree, st, &row_elems, &o_loff, &o_lsz);
+    const auto* mats = reinterpret_cast<const OpenMat*>(buf);
+    const auto* loff = reinterpret_cast<const uint64_t*>(buf + o_loff);
+    const auto* lsz = reinterpret_cast<const uint64_t*>(buf + o_lsz);
+    if (tree->field == P3G_BABYBEAR)
+        k_open<uint32_t><<<unsigned(nq), 128, 0, st>>>(mats, int(tree->mats.size()), max_h, d_idx,
+                                                       static_cast<const uint32_t*>(tree->d_digests), loff, lsz, nproof,
+                                                       int(tree->digest), tree->flat ? 1 : 0,
+                                                       static_cast<uint32_t*>(d_rows), row_elems,
+                                                       static_cast<uint32_t*>(d_proof));
+    else
+        k_open<uint64_t><<<unsigned(nq), 128, 0, st>>>(mats, int(tree->mats.size()), max_h, d_idx,
+                                                       static_cast<const uint64_t*>(tree->d_digests), loff, lsz, nproof,
+                                                       int(tree->digest), tree->flat ? 1 : 0,
+                                                       static_cast<uint64_t*>(d_rows), row_elems,
+                                                       static_cast<uint64_t*>(d_proof));
+    P3G_LAUNCHED();
+    P3G_CUDA(cudaGetLastError());
+    ctx->release(buf, st);
+}
+
 void open_batch(p3g_ctx* ctx, const p3g_tree* tree, const uint64_t* h_idx, size_t nq, void* h_rows,
                 void* h_proof, cudaStream_t st) {
     if (nq == 0) return;
     const size_t esz = tree->field == P3G_BABYBEAR ? 4 : 8;
     const uint64_t max_h = tree->layer_size[0];
     for (size_t q = 0; q < nq; ++q) P3G_REQUIRE(h_idx[q] < max_h, "open_batch: index out of range");
-    std::vector<OpenMat> om(tree->mats.size());
     uint32_t row_elems = 0;
-    for (size_t i = 0; i < om.size(); ++i) {
-        om[i] = {tree->mats[i].d_data, tree->mats[i].height, tree->mats[i].width, row_elems};
-        row_elems += tree->mats[i].width;
-    }
+    for (const auto& m : tree->mats) row_elems += m.width;
     const int nproof = int(tree->layer_size.size()) - 1;
-    const size_t dig = tree->digest;
-    // one device staging block: descriptors, indices, layer tables, outputs
-    size_t off = 0;
-    auto take = [&](size_t bytes) { size_t o = off; off += (bytes + 255) / 256 * 256; return o; };
-    const size_t o_mats = take(sizeof(OpenMat) * om.size());
-    const size_t o_idx = take(8 * nq);
-    const size_t o_loff = take(8 * tree->layer_off.size());
-    const size_t o_lsz = take(8 * tree->layer_size.size());
-    const size_t rows_bytes = esz * row_elems * nq, proof_bytes = esz * dig * size_t(std::max(nproof, 0)) * nq;
-    const size_t o_rows = take(rows_bytes);
-    const size_t o_proof = take(proof_bytes);
-    char* buf = static_cast<char*>(ctx->alloc(off, st));
-    P3G_CUDA(cudaMemcpyAsync(buf + o_mats, om.data(), sizeof(OpenMat) * om.size(), cudaMemcpyHostToDevice, st));
-    P3G_CUDA(cudaMemcpyAsync(buf + o_idx, h_idx, 8 * nq, cudaMemcpyHostToDevice, st));
-    P3G_CUDA(cudaMemcpyAsync(buf + o_loff, tree->layer_off.data(), 8 * tree->layer_off.size(), cudaMemcpyHostToDevice, st));
-    P3G_CUDA(cudaMemcpyAsync(buf + o_lsz, tree->layer_size.data(), 8 * tree->layer_size.size(), cudaMemcpyHostToDevice, st));
-    if (esz == 4) {
-        k_open<uint32_t><<<unsigned(nq), 128, 0, st>>>(
-            reinterpret_cast<OpenMat*>(buf + o_mats), int(om.size()), max_h, reinterpret_cast<uint64_t*>(buf + o_idx),
-            static_cast<const uint32_t*>(tree->d_digests), reinterpret_cast<uint64_t*>(buf + o_loff),
-            reinterpret_cast<uint64_t*>(buf + o_lsz), nproof, int(dig), tree->flat ? 1 : 0,
-            reinterpret_cast<uint32_t*>(buf + o_rows), row_elems, reinterpret_cast<uint32_t*>(buf + o_proof));
-        P3G_LAUNCHED();
-    } else {
-        k_open<uint64_t><<<unsigned(nq), 128, 0, st>>>(
-            reinterpret_cast<OpenMat*>(buf + o_mats), int(om.size()), max_h, reinterpret_cast<uint64_t*>(buf + o_idx),
-            static_cast<const uint64_t*>(tree->d_digests), reinterpret_cast<uint64_t*>(buf + o_loff),
-            reinterpret_cast<uint64_t*>(buf + o_lsz), nproof, int(dig), tree->flat ? 1 : 0,
-            reinterpret_cast<uint64_t*>(buf + o_rows), row_elems, reinterpret_cast<uint64_t*>(buf + o_proof));
-        P3G_LAUNCHED();
-    }
-    P3G_CUDA(cudaGetLastError());
+    const size_t rows_bytes = esz * row_elems * nq;
+    const size_t proof_bytes = esz * tree->digest * size_t(std::max(nproof, 0)) * nq;
+    // one device staging block: indices, rows, proofs
+    const size_t o_rows = (8 * nq + 255) / 256 * 256, o_proof = o_rows + (rows_bytes + 255) / 256 * 256;
+    char* buf = static_cast<char*>(ctx->alloc(o_proof + std::max<size_t>(proof_bytes, 1), st));
+    P3G_CUDA(cudaMemcpyAsync(buf, h_idx, 8 * nq, cudaMemcpyHostToDevice, st));
+    open_batch_dev(ctx, tree, reinterpret_cast<const uint64_t*>(buf), nq, buf + o_rows, buf + o_proof, st);
     if (h_rows && rows_bytes) P3G_CUDA(cudaMemcpyAsync(h_rows, buf + o_rows, rows_bytes, cudaMemcpyDeviceToHost, st));
     if (h_proof && proof_bytes) P3G_CUDA(cudaMemcpyAsync(h_proof, buf + o_proof, proof_bytes, cudaMemcpyDeviceToHost, st));
     ctx->release(buf, st);
     P3G_CUDA(cudaStreamSynchronize(st));
+}
+
+void grind_bb_dev(p3g_ctx* ctx, const void* d_args, uint64_t count, unsigned long long* found, cudaStream_t st) {
+    dispatch_bb(ctx, GrindFn<HBB>{&ctx->p2bb, static_cast<const GrindArgs<uint32_t, 16>*>(d_args), 0, count, found,
+                                  ctx->sm_count, st});
 }
 
 }  // namespace p3g

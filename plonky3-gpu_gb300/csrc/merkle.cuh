@@ -232,9 +232,12 @@ struct GrindArgs {
 };
 
 template <class H, int D, int RF, int RP>
-__global__ void __launch_bounds__(128) k_grind(typename H::Params p, GrindArgs<typename H::T, H::W> a,
+__global__ void __launch_bounds__(128) k_grind(typename H::Params p, const GrindArgs<typename H::T, H::W>* args,
                                                uint64_t base, uint64_t count, unsigned long long* found) {
     using T = typename H::T;
+    __shared__ GrindArgs<T, H::W> a;  // from device memory: written by the host or by a transcript kernel
+    if (threadIdx.x == 0) a = *args;
+    __syncthreads();
     const int k = int(a.n_input);
     const int passes = k + 1 == H::RATE ? 2 : 1;
     const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
@@ -245,7 +248,7 @@ __global__ void __launch_bounds__(128) k_grind(typename H::Params p, GrindArgs<t
         const T hi = H::absorb(H::from_u32(uint32_t(c >> 32)));
         T s[H::W];
 #pragma unroll
-        for (int i = 0; i < H::W; ++i) s[i] = a.state[i];  // from the parameter bank
+        for (int i = 0; i < H::W; ++i) s[i] = a.state[i];
 #pragma unroll
         for (int i = 0; i < H::RATE; ++i) {
             if (i == k) s[i] = lo;
@@ -260,6 +263,24 @@ __global__ void __launch_bounds__(128) k_grind(typename H::Params p, GrindArgs<t
     }
 }
 
+// Calls fn.template operator()<D, RF, RP>() for a supported round schedule.
+template <class Fn>
+void dispatch_bb(const p3g_ctx* ctx, const Fn& fn) {
+    if (!ctx->has_p2bb) throw Error(P3G_ESTATE, "Poseidon2 constants for BabyBear are not set");
+    const int d = ctx->bb_d, rf = ctx->bb_rf, rp = ctx->bb_rp;
+    if (rf == 8 && d == 7 && rp == 13) return fn.template operator()<7, 8, 13>();
+    if (rf == 8 && d == 7 && rp == 22) return fn.template operator()<7, 8, 22>();
+    if (rf == 8 && d == 5 && rp == 14) return fn.template operator()<5, 8, 14>();
+    throw Error(P3G_EUNSUPPORTED, "BabyBear Poseidon2 schedule not built (supported: x^7 8+13, x^7 8+22, x^5 8+14)");
+}
+template <class Fn>
+void dispatch_gl(const p3g_ctx* ctx, const Fn& fn) {
+    if (!ctx->has_p2gl) throw Error(P3G_ESTATE, "Poseidon2 constants for Goldilocks are not set");
+    const int d = ctx->gl_d, rf = ctx->gl_rf, rp = ctx->gl_rp;
+    if (rf == 8 && d == 7 && rp == 22) return fn.template operator()<7, 8, 22>();
+    throw Error(P3G_EUNSUPPORTED, "Goldilocks Poseidon2 schedule not built (supported: x^7 8+22)");
+}
+
 // Host launchers, explicitly instantiated once per schedule.
 template <class H, int D, int RF, int RP>
 struct Launch {
@@ -271,7 +292,7 @@ struct Launch {
     static void level(const typename H::Params& p, const T* child, uint64_t nchild, T* parent, uint64_t nparent,
                       const T* inj, cudaStream_t st);
     static void permute(const typename H::Params& p, T* states, uint64_t n, cudaStream_t st);
-    static void grind(const typename H::Params& p, const GrindArgs<T, H::W>& a, uint64_t base, uint64_t count,
+    static void grind(const typename H::Params& p, const GrindArgs<T, H::W>* d_args, uint64_t base, uint64_t count,
                       unsigned long long* found, int sm_count, cudaStream_t st);
 };
 
@@ -303,7 +324,7 @@ void Launch<H, D, RF, RP>::level(const typename H::Params& p, const T* child, ui
     P3G_CUDA(cudaGetLastError());
 }
 template <class H, int D, int RF, int RP>
-void Launch<H, D, RF, RP>::grind(const typename H::Params& p, const GrindArgs<T, H::W>& a, uint64_t base,
+void Launch<H, D, RF, RP>::grind(const typename H::Params& p, const GrindArgs<T, H::W>* d_args, uint64_t base,
                                  uint64_t count, unsigned long long* found, int sm_count, cudaStream_t st) {
     if (count == 0) return;
     static int occ = 0;
@@ -313,7 +334,7 @@ void Launch<H, D, RF, RP>::grind(const typename H::Params& p, const GrindArgs<T,
         occ = o > 0 ? o : 1;
     }
     const uint64_t blocks = std::min<uint64_t>(uint64_t(occ) * sm_count, (count + 127) / 128);
-    k_grind<H, D, RF, RP><<<unsigned(blocks), 128, 0, st>>>(p, a, base, count, found);
+    k_grind<H, D, RF, RP><<<unsigned(blocks), 128, 0, st>>>(p, d_args, base, count, found);
     P3G_LAUNCHED();
     P3G_CUDA(cudaGetLastError());
 }

@@ -29,7 +29,7 @@ EXPORTS = [
     "p3g_coset_lde_bb_noalloc", "p3g_plan_commit", "p3g_plan_launch", "p3g_plan_info",
     "p3g_plan_destroy", "p3g_server_create", "p3g_server_submit", "p3g_server_poll",
     "p3g_server_pending", "p3g_server_open", "p3g_server_release", "p3g_server_destroy",
-    "p3g_pcs_open_values", "p3g_pcs_reduce", "p3g_bb4_axpy", "p3g_grind",
+    "p3g_pcs_open_values", "p3g_pcs_reduce", "p3g_bb4_axpy", "p3g_grind", "p3g_fri_rounds", "p3g_fri_prove",
 ]
 
 
@@ -41,6 +41,17 @@ class P3GError(RuntimeError):
     def __init__(self, status: int, msg: str):
         super().__init__(f"p3g status {status}: {msg}")
         self.status = status
+
+
+class FriParams(C.Structure):
+    _fields_ = [("log_blowup", C.c_uint32), ("log_final_poly_len", C.c_uint32), ("max_log_arity", C.c_uint32),
+                ("num_queries", C.c_uint32), ("commit_proof_of_work_bits", C.c_uint32),
+                ("query_proof_of_work_bits", C.c_uint32)]
+
+
+class Challenger(C.Structure):
+    _fields_ = [("sponge_state", C.c_uint32 * 16), ("input", C.c_uint32 * 8), ("output", C.c_uint32 * 8),
+                ("n_input", C.c_uint32), ("n_output", C.c_uint32)]
 
 
 class Matrix(C.Structure):
@@ -125,6 +136,8 @@ def load(path: str | None = None):
     L.p3g_pcs_open_values.argtypes = [vp, vp, u32, u32, i32, u32, vp, u32, vp, vp]
     L.p3g_bb4_axpy.argtypes = [vp, vp, vp, u64, vp, vp]
     L.p3g_grind.argtypes = [vp, C.c_int, vp, vp, u32, u32, u64, vp, vp]
+    L.p3g_fri_rounds.argtypes = [vp, u32, vp, vp, vp]
+    L.p3g_fri_prove.argtypes = [vp, vp, vp, u32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]
     L.p3g_pcs_reduce.argtypes = [vp, vp, u32, u32, i32, u32, vp, u32, vp, vp, u64, i32, vp, vp]
     for name in EXPORTS:
         if name not in ("p3g_version", "p3g_status_string", "p3g_kernel_launches"):
@@ -525,6 +538,54 @@ class Context:
         check(load().p3g_grind(self.handle, field, _np_ptr(st), _np_ptr(inp) if inp.size else None, inp.size,
                                bits, max_witness, C.byref(w), stream))
         return w.value
+
+    # -- FRI prover with the transcript on the device
+    def fri_prove_device(self, inputs, params: dict, state, pending, outputs, stream=None) -> dict:
+        """prove_fri over device BabyBear^4 vectors: inputs = [(device ptr,
+        log_height)], tallest first; the challenger's sponge state, pending
+        inputs and pending outputs.  Returns the proof's parts and the
+        challenger afterwards."""
+        prm = FriParams(**params)
+        lh = (C.c_uint32 * len(inputs))(*[h for _, h in inputs])
+        nr = C.c_uint32()
+        las = (C.c_uint32 * 32)()
+        check(load().p3g_fri_rounds(lh, len(inputs), C.byref(prm), C.byref(nr), las))
+        R, nq = nr.value, prm.num_queries
+        arities = [las[r] for r in range(R)]
+        heights, h = [], inputs[0][1]
+        for la in arities:
+            heights.append(h)
+            h -= la
+        ch = Challenger()
+        ch.sponge_state[:] = [int(x) for x in state]
+        for i, v in enumerate(pending):
+            ch.input[i] = int(v)
+        for i, v in enumerate(outputs):
+            ch.output[i] = int(v)
+        ch.n_input, ch.n_output = len(pending), len(outputs)
+        commits = np.zeros((R, 8), np.uint32)
+        wits = np.zeros(R, np.uint64)
+        final = np.zeros((1 << prm.log_final_poly_len, 4), np.uint32)
+        qw = C.c_uint64()
+        qidx = np.zeros(max(nq, 1), np.uint64)
+        rows_w = sum(nq * (4 << la) for la in arities)
+        path_w = sum(nq * (hh - la) * 8 for hh, la in zip(heights, arities))
+        rows = np.zeros(max(rows_w, 1), np.uint32)
+        paths = np.zeros(max(path_w, 1), np.uint32)
+        ptrs = (C.c_void_p * len(inputs))(*[p for p, _ in inputs])
+        check(load().p3g_fri_prove(self.handle, ptrs, lh, len(inputs), C.byref(prm), C.byref(ch), _np_ptr(commits),
+                                   _np_ptr(wits), _np_ptr(final), C.byref(qw), _np_ptr(qidx), _np_ptr(rows),
+                                   _np_ptr(paths), stream))
+        out_rows, out_paths, ro, po = [], [], 0, 0
+        for hh, la in zip(heights, arities):
+            out_rows.append(rows[ro:ro + nq * (4 << la)].reshape(nq, 4 << la))
+            ro += nq * (4 << la)
+            out_paths.append(paths[po:po + nq * (hh - la) * 8].reshape(nq, hh - la, 8))
+            po += nq * (hh - la) * 8
+        return {"log_arities": arities, "commits": commits, "commit_witnesses": wits, "final_poly": final,
+                "query_witness": qw.value, "query_indices": qidx[:nq], "rows": out_rows, "paths": out_paths,
+                "state": np.array(ch.sponge_state[:], np.uint32), "pending": list(ch.input[:ch.n_input]),
+                "outputs": list(ch.output[:ch.n_output])}
 
     # -- PCS open
     def pcs_open_values_device(self, d_lde: int, log_n: int, width: int, bitrev_rows: bool, shift: int, points,

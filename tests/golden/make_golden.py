@@ -185,13 +185,32 @@ def main() -> int:
         end = tail + 9 + 8 * rounds + 4 * nf
         final = raw[tail + 9 + 8 * rounds:end].reshape(nf, 4).tolist()
         pow_witness = int(raw[end]) | (int(raw[end + 1]) << 32)
+        cur = [end + 2]
+
+        def take(n):
+            v = raw[cur[0]:cur[0] + n]
+            cur[0] += n
+            return v
+
+        queries = []
+        for _ in range(int(take(1)[0])):
+            steps = []
+            for _ in range(int(take(1)[0])):
+                la = int(take(1)[0])
+                ns = int(take(1)[0])
+                sib = take(4 * ns).reshape(ns, 4).tolist()
+                npf = int(take(1)[0])
+                steps.append({"log_arity": la, "siblings": sib, "path": take(8 * npf).reshape(npf, 8).tolist()})
+            queries.append(steps)
+        assert cur[0] == raw.size, (cur[0], raw.size)
         opens.append({"seed": seed, "shapes": shapes, "log_blowup": 1, "shift": 1,
                       "fri": {"log_final_poly_len": 0, "max_log_arity": 1, "commit_pow_bits": 0,
                               "query_pow_bits": 8, "query_pow_witness": pow_witness},
                       "zeta": raw[0:4].tolist(), "alpha": raw[4:8].tolist(),
                       "opened": raw[8:o].tolist(), "fri_rounds": rounds,
                       "log_arity0": int(raw[o + 1]), "commit0": raw[o + 2:o + 10].tolist(),
-                      "pcs_root": raw[tail:tail + 8].tolist(), "commits": commits, "final_poly": final})
+                      "pcs_root": raw[tail:tail + 8].tolist(), "commits": commits, "final_poly": final,
+                      "num_queries": 10, "query_openings": queries})
     g["pcs_open"] = opens
 
     grinds = []

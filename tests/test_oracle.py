@@ -390,6 +390,32 @@ def fri_query_pow(case, tr, final, arities, grind):
     return grind(tr, case["fri"]["query_pow_bits"])
 
 
+def fri_query_openings(case, tr, rounds):
+    """prove_fri's query phase (fri_prover.hpp:199-257) after the query proof
+    of work: sample each query index, then per round the committed row holding
+    it (siblings = the row without the query's position) and the row's Merkle
+    path.  rounds: per round (committed matrix rows x 4 arity, its layers, log
+    arity).  Returns (indices, openings in the golden's layout)."""
+    fri = case["fri"]
+    log_max = case["log_blowup"] + fri["log_final_poly_len"] + sum(la for _, _, la in rounds)
+    idx = [tr.sample_bits(log_max) for _ in range(case["num_queries"])]
+    out = []
+    for q in idx:
+        steps, cur = [], q
+        for mat, layers, la in rounds:
+            row, pos = cur >> la, cur & ((1 << la) - 1)
+            vals = mat[row].reshape(-1, 4)
+            sib = [vals[j].tolist() for j in range(1 << la) if j != pos]
+            path = []
+            for lvl in range(len(layers) - 1):
+                s = (row >> lvl) ^ 1
+                path.append(layers[lvl][s].tolist() if s < len(layers[lvl]) else [0] * 8)
+            steps.append({"log_arity": la, "siblings": sib, "path": path})
+            cur = row
+        out.append(steps)
+    return idx, out
+
+
 def open_transcript(case):
     """The transcript up to prove_fri: observe the PCS commitment, sample zeta
     (the caller's opening point) and alpha (TwoAdicFriPcs::open's first sample)."""
@@ -408,15 +434,24 @@ def test_transcript_and_fri_commit_phase_vs_reference(golden):
         for v in opened.reshape(-1, 4):  # two_adic_fri_pcs.hpp:338-346
             tr.observe_ext(v)
         inputs = [_bitrev_rows(qs[h]) for h in sorted(qs, reverse=True)]
+        committed = []
+
+        def commit(cur, arity):
+            mat = cur.reshape(-1, 4 * arity)
+            layers = O.commit_matrix(O.bb16_params(), mat)
+            committed.append((mat, layers, arity.bit_length() - 1))
+            return layers[-1][0]
+
         roots, final, arities = fri_commit_phase(
-            case, inputs, tr,
-            commit=lambda cur, arity: O.commit_matrix(O.bb16_params(), cur.reshape(-1, 4 * arity))[-1][0],
+            case, inputs, tr, commit=commit,
             fold=lambda cur, lh, la, beta: O.fold_matrix_bb4(cur, lh, la, beta),
             axpy=O.bb4_axpy, length=len, download=lambda c: c)
         assert [r.tolist() for r in roots] == case["commits"]
         assert final.tolist() == case["final_poly"]
         w = fri_query_pow(case, tr, final, arities, lambda t, bits: t.grind_py(bits))
         assert w == case["fri"]["query_pow_witness"]
+        _, openings = fri_query_openings(case, tr, committed)
+        assert openings == case["query_openings"]
         for pc in golden["pcs_commit"]:  # the same commitment where the commit cases overlap
             if pc["seed"] == case["seed"] and pc["shapes"] == case["shapes"]:
                 assert pc["root"] == case["pcs_root"]
