@@ -62,35 +62,61 @@ struct ChalStep {
     uint32_t* err;                    // set when a search found no witness
 };
 
-template <int D, int RF, int RP>
-__device__ __noinline__ void chal_duplex(DevChal& c, const P2BB16& p) {
-    uint32_t s[16];
-    for (int i = 0; i < 16; ++i) s[i] = HBB::absorb(i < int(c.n_in) ? c.in[i] : c.st[i]);
-    p2_bb16<D, RF, RP>(s, p);
-    for (int i = 0; i < 16; ++i) c.st[i] = HBB::squeeze(s[i]);
-    c.n_in = 0;
-    for (int i = 0; i < 8; ++i) c.out[i] = c.st[i];
-    c.n_out = 8;
-}
-template <int D, int RF, int RP>
-__device__ void chal_absorb(DevChal& c, uint32_t v, const P2BB16& p) {
-    c.in[c.n_in++] = v;
-    if (c.n_in == 8) chal_duplex<D, RF, RP>(c, p);
-}
-template <int D, int RF, int RP>
-__device__ uint32_t chal_sample(DevChal& c, const P2BB16& p) {
-    if (c.n_in > 0 || c.n_out == 0) chal_duplex<D, RF, RP>(c, p);
-    return c.out[--c.n_out];
-}
 __device__ __forceinline__ bb4 bb4_mul_cc(const bb4& a, const bb4& b) { return bb4_mul_cm(a, bb4_to_mont(b)); }
 
+// The challenger's steps, run by one warp on a shared-memory copy of its
+// state: every lane follows the same (uniform) control flow, lane 0 keeps the
+// books, lanes 0-15 hold one state word each through the permutation
+// (p2_bb16_coop).  __syncwarp orders the shared-memory updates.
 template <int D, int RF, int RP>
-__global__ void k_transcript(P2BB16 p, DevChal* dc, ChalStep s) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    DevChal c = *dc;
+__device__ __noinline__ void chal_duplex(DevChal& c, const P2BB16& p, const CoopConsts& cc) {
+    const int lane = threadIdx.x, i = lane & 15;
+    uint32_t x = HBB::absorb(i < int(c.n_in) ? c.in[i] : c.st[i]);
+    x = p2_bb16_coop<D, RF, RP>(x, p, cc, i);
+    __syncwarp();
+    if (lane < 16) c.st[i] = HBB::squeeze(x);
+    __syncwarp();
+    if (lane < 8) c.out[lane] = c.st[lane];
+    if (lane == 0) {
+        c.n_in = 0;
+        c.n_out = 8;
+    }
+    __syncwarp();
+}
+template <int D, int RF, int RP>
+__device__ void chal_absorb(DevChal& c, uint32_t v, const P2BB16& p, const CoopConsts& cc) {
+    if (threadIdx.x == 0) c.in[c.n_in++] = v;
+    __syncwarp();
+    if (c.n_in == 8) chal_duplex<D, RF, RP>(c, p, cc);
+}
+template <int D, int RF, int RP>
+__device__ uint32_t chal_sample(DevChal& c, const P2BB16& p, const CoopConsts& cc) {
+    if (c.n_in > 0 || c.n_out == 0) chal_duplex<D, RF, RP>(c, p, cc);
+    const uint32_t v = c.out[c.n_out - 1];
+    __syncwarp();
+    if (threadIdx.x == 0) --c.n_out;
+    __syncwarp();
+    return v;
+}
+__device__ __forceinline__ void chal_clear_outputs(DevChal& c) {
+    if (threadIdx.x == 0) c.n_out = 0;
+    __syncwarp();
+}
+
+template <int D, int RF, int RP>
+__global__ void __launch_bounds__(32) k_transcript(P2BB16 pp, DevChal* dc, ChalStep s) {
+    __shared__ P2BB16 p;  // round constants for the out-of-line permutation
+    __shared__ DevChal c;
+    const int lane = threadIdx.x;
+    for (int k = lane; k < int(sizeof(P2BB16) / 4); k += 32)
+        reinterpret_cast<uint32_t*>(&p)[k] = reinterpret_cast<const uint32_t*>(&pp)[k];
+    for (int k = lane; k < int(sizeof(DevChal) / 4); k += 32)
+        reinterpret_cast<uint32_t*>(&c)[k] = reinterpret_cast<const uint32_t*>(dc)[k];
+    __syncwarp();
+    const CoopConsts cc = coop_consts(p, lane & 15);
     if (s.observe_root) {  // observe_merkle_cap with one digest
-        c.n_out = 0;
-        for (int i = 0; i < 8; ++i) chal_absorb<D, RF, RP>(c, s.observe_root[i], p);
+        chal_clear_outputs(c);
+        for (int k = 0; k < 8; ++k) chal_absorb<D, RF, RP>(c, s.observe_root[k], p, cc);
     }
     if (s.final_cur) {
         const int n = 1 << s.log_fpl;
@@ -104,65 +130,88 @@ __global__ void k_transcript(P2BB16 p, DevChal* dc, ChalStep s) {
                 sum = bb4_add(sum, bb4_scale_m(s.final_cur[jr], wkj));
                 wkj = bb::mmul(wkj, wk);
             }
-            s.final_out[k] = bb4_scale_m(sum, nim);
+            const bb4 coef = bb4_scale_m(sum, nim);
+            if (lane == 0) s.final_out[k] = coef;
+            chal_clear_outputs(c);  // observe_challenge
+            for (int e = 0; e < 4; ++e) chal_absorb<D, RF, RP>(c, coef.c[e], p, cc);
             wk = bb::mmul(wk, wm);
         }
-        for (int k = 0; k < n; ++k) {  // observe_challenge per coefficient
-            c.n_out = 0;
-            for (int e = 0; e < 4; ++e) chal_absorb<D, RF, RP>(c, s.final_out[k].c[e], p);
-        }
         for (int r = 0; r < s.n_arities; ++r) {  // observe_arity: observe(BabyBear(log_arity))
-            c.n_out = 0;
-            chal_absorb<D, RF, RP>(c, s.arities[r], p);
+            chal_clear_outputs(c);
+            chal_absorb<D, RF, RP>(c, s.arities[r], p, cc);
         }
     }
-    if (s.grind_args) {  // the search runs next, from this state
-        GrindArgs<uint32_t, 16> a;
-        for (int i = 0; i < 16; ++i) a.state[i] = HBB::absorb(i < int(c.n_in) ? c.in[i] : c.st[i]);
-        a.n_input = c.n_in;
-        a.mask = (uint64_t(1) << s.pow_bits) - 1;
-        *s.grind_args = a;
+    if (s.grind_args && lane < 16) {  // the search runs next, from this state
+        const int i = lane;
+        s.grind_args->state[i] = HBB::absorb(i < int(c.n_in) ? c.in[i] : c.st[i]);
+        if (i == 0) {
+            s.grind_args->n_input = c.n_in;
+            s.grind_args->mask = (uint64_t(1) << s.pow_bits) - 1;
+        }
     }
     if (s.take_witness) {  // grind's accepted witness: observe_witness + one sample
         uint64_t w = 0;
         if (s.found) {
             w = *s.found;
             if (w == ~0ull) {
-                *s.err = 1;
+                if (lane == 0) *s.err = 1;
                 w = 0;
             }
         }
-        c.n_out = 0;
-        chal_absorb<D, RF, RP>(c, uint32_t(w) % bb::P, p);
-        chal_absorb<D, RF, RP>(c, uint32_t(w >> 32) % bb::P, p);
-        chal_sample<D, RF, RP>(c, p);
-        *s.witness_out = w;
+        chal_clear_outputs(c);
+        chal_absorb<D, RF, RP>(c, uint32_t(w) % bb::P, p, cc);
+        chal_absorb<D, RF, RP>(c, uint32_t(w >> 32) % bb::P, p, cc);
+        chal_sample<D, RF, RP>(c, p, cc);
+        if (lane == 0) *s.witness_out = w;
     }
     if (s.beta_out) {
         bb4 b;
-        for (int e = 0; e < 4; ++e) b.c[e] = chal_sample<D, RF, RP>(c, p);
-        *s.beta_out = b;
+        for (int e = 0; e < 4; ++e) b.c[e] = chal_sample<D, RF, RP>(c, p, cc);
+        if (lane == 0) *s.beta_out = b;
         for (int k = 0; k < s.log_arity; ++k) b = bb4_mul_cc(b, b);
-        *s.beta_pow_out = b;
+        if (lane == 0) *s.beta_pow_out = b;
     }
     for (int q = 0; q < s.num_queries; ++q) {  // sample_bits: one 31-bit sample covers log_max_height
-        const uint32_t v = chal_sample<D, RF, RP>(c, p);
-        s.query_out[q] = uint64_t(v) & ((uint64_t(1) << s.log_max_height) - 1);
+        const uint32_t v = chal_sample<D, RF, RP>(c, p, cc);
+        if (lane == 0) s.query_out[q] = uint64_t(v) & ((uint64_t(1) << s.log_max_height) - 1);
     }
-    *dc = c;
+    __syncwarp();
+    for (int k = lane; k < int(sizeof(DevChal) / 4); k += 32)
+        reinterpret_cast<uint32_t*>(dc)[k] = reinterpret_cast<const uint32_t*>(&c)[k];
 }
 
-// Row index of every query in round r's committed matrix: the query index
-// shifted right by the log arities of rounds 0..r.
-__global__ void k_query_rows(const uint64_t* qidx, int nq, int shift, uint64_t rows, uint64_t* out, uint32_t* err) {
-    const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= nq) return;
-    uint64_t r = qidx[q] >> shift;
-    if (r >= rows) {  // cannot happen for sampled indices; keep the opening in bounds regardless
-        *err = 2;
-        r = 0;
+// Every round's opening of every query (fri_prover.hpp:211-257), one block
+// per (query, round): the committed row holding the query -- its index is the
+// query index shifted right by the log arities of rounds 0..r -- and the
+// row's Merkle path (flat tree: a missing sibling is the zero digest).
+constexpr int FRI_MAX_DEPTH = 28;
+struct FriOpenRound {
+    const uint32_t* mat;      // the committed matrix, rows x width
+    const uint32_t* digests;  // its tree's layers
+    uint32_t* rows_out;       // nq x width
+    uint32_t* path_out;       // nq x depth x 8
+    uint64_t rows;
+    uint32_t width, depth, shift, pad;
+    uint64_t layer_off[FRI_MAX_DEPTH];  // in digests
+    uint64_t layer_size[FRI_MAX_DEPTH];
+};
+
+__global__ void k_fri_open(const FriOpenRound* rounds, const uint64_t* qidx, uint32_t* err) {
+    const int q = blockIdx.x;
+    const FriOpenRound& rd = rounds[blockIdx.y];
+    uint64_t row = qidx[q] >> rd.shift;
+    if (row >= rd.rows) {  // cannot happen for sampled indices; stay in bounds regardless
+        if (threadIdx.x == 0) *err = 2;
+        row = 0;
     }
-    out[q] = r;
+    for (uint32_t c = threadIdx.x; c < rd.width; c += blockDim.x)
+        rd.rows_out[uint64_t(q) * rd.width + c] = rd.mat[row * rd.width + c];
+    for (uint32_t e = threadIdx.x; e < rd.depth * 8; e += blockDim.x) {
+        const uint32_t l = e / 8, i = e % 8;
+        const uint64_t sib = (row >> l) ^ 1;
+        rd.path_out[(uint64_t(q) * rd.depth + l) * 8 + i] =
+            sib < rd.layer_size[l] ? rd.digests[(rd.layer_off[l] + sib) * 8 + i] : 0u;
+    }
 }
 
 struct TranscriptFn {
@@ -172,7 +221,7 @@ struct TranscriptFn {
     cudaStream_t st;
     template <int D, int RF, int RP>
     void operator()() const {
-        k_transcript<D, RF, RP><<<1, 1, 0, st>>>(*p, c, *s);
+        k_transcript<D, RF, RP><<<1, 32, 0, st>>>(*p, c, *s);
         P3G_LAUNCHED();
         P3G_CUDA(cudaGetLastError());
     }
@@ -263,13 +312,13 @@ void fri_prove(p3g_ctx* ctx, const void* const* d_inputs, const uint32_t* log_he
     const size_t o_qidx = take(8 * std::max(nq, 1));
     const size_t o_err = take(8);
     const size_t o_roots = take(32 * std::max(R, 1));
-    std::vector<size_t> o_rowidx(R), o_rows(R), o_paths(R);
+    std::vector<size_t> o_rows(R), o_paths(R);
     for (int r = 0; r < R; ++r) {
         const int lrows = rounds[r].log_h - rounds[r].log_arity;
-        o_rowidx[r] = take(8 * std::max(nq, 1));
         o_rows[r] = take(4 * size_t(nq) * (4u << rounds[r].log_arity) + 4);
         o_paths[r] = take(4 * size_t(nq) * lrows * 8 + 4);
     }
+    const size_t o_open = take(sizeof(FriOpenRound) * std::max(R, 1));
     const size_t out_bytes = off;
     struct Bufs {  // everything allocated here, released in stream order on every exit
         p3g_ctx* ctx;
@@ -309,6 +358,30 @@ void fri_prove(p3g_ctx* ctx, const void* const* d_inputs, const uint32_t* log_he
         t->mats.push_back(p3g_matrix{cur[r], n_next, 4u << rounds[r].log_arity, 0});
         tree_prepare(ctx, t, 0, true, st, false);
     }
+
+    // the openings' table, uploaded with the rest before any launch
+    std::vector<FriOpenRound> open_tab(R);
+    for (int r = 0; r < R; ++r) {
+        const p3g_tree* t = bufs.trees[r];
+        FriOpenRound& o = open_tab[r];
+        std::memset(&o, 0, sizeof o);
+        o.mat = cur[r];
+        o.digests = static_cast<const uint32_t*>(t->d_digests);
+        o.rows_out = reinterpret_cast<uint32_t*>(blk + o_rows[r]);
+        o.path_out = reinterpret_cast<uint32_t*>(blk + o_paths[r]);
+        o.rows = t->layer_size[0];
+        o.width = 4u << rounds[r].log_arity;
+        o.depth = uint32_t(t->layer_size.size() - 1);
+        P3G_REQUIRE(o.depth <= uint32_t(FRI_MAX_DEPTH), "fri: tree too deep");
+        int shift = 0;
+        for (int k = 0; k <= r; ++k) shift += rounds[k].log_arity;
+        o.shift = uint32_t(shift);
+        for (uint32_t l = 0; l < o.depth; ++l) {
+            o.layer_off[l] = t->layer_off[l];
+            o.layer_size[l] = t->layer_size[l];
+        }
+    }
+    if (R) P3G_CUDA(cudaMemcpyAsync(blk + o_open, open_tab.data(), sizeof(FriOpenRound) * R, cudaMemcpyHostToDevice, st));
 
     auto transcript = [&](const ChalStep& s) { dispatch_bb(ctx, TranscriptFn{&ctx->p2bb, dchal, &s, st}); };
     auto search = [&](int slot, uint32_t bits) {  // one bounded launch: a miss has probability e^-64
@@ -381,16 +454,12 @@ void fri_prove(p3g_ctx* ctx, const void* const* d_inputs, const uint32_t* log_he
         s.log_max_height = log_max;
         transcript(s);
     }
-    // ---- query openings of every round's tree
-    int shift = 0;
-    for (int r = 0; r < R && nq > 0; ++r) {
-        shift += rounds[r].log_arity;
-        auto* ridx = reinterpret_cast<uint64_t*>(blk + o_rowidx[r]);
-        k_query_rows<<<(nq + 127) / 128, 128, 0, st>>>(reinterpret_cast<const uint64_t*>(blk + o_qidx), nq, shift,
-                                                       bufs.trees[r]->layer_size[0], ridx, err);
+    // ---- query openings of every round's tree, one launch
+    if (R && nq > 0) {
+        k_fri_open<<<dim3(unsigned(nq), unsigned(R)), 64, 0, st>>>(reinterpret_cast<const FriOpenRound*>(blk + o_open),
+                                                                 reinterpret_cast<const uint64_t*>(blk + o_qidx), err);
         P3G_LAUNCHED();
         P3G_CUDA(cudaGetLastError());
-        open_batch_dev(ctx, bufs.trees[r], ridx, size_t(nq), blk + o_rows[r], blk + o_paths[r], st);
     }
     // ---- results
     std::vector<char> host(out_bytes);

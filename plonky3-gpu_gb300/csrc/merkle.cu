@@ -92,6 +92,23 @@ struct LevelFn {
     void operator()() const { Launch<H, D, RF, RP>::level(*p, child, nchild, parent, npar, inj, st); }
 };
 template <class H>
+struct TailFn {
+    const typename H::Params* p;
+    const TailLevels<typename H::T>* t;
+    cudaStream_t st;
+    template <int D, int RF, int RP>
+    void operator()() const { Launch<H, D, RF, RP>::tail(*p, *t, st); }
+};
+template <class H>
+struct CoopFn {
+    const typename H::Params* p;
+    const TailLevels<typename H::T>* t;
+    unsigned blocks;
+    cudaStream_t st;
+    template <int D, int RF, int RP>
+    void operator()() const { Launch<H, D, RF, RP>::coop(*p, *t, blocks, st); }
+};
+template <class H>
 struct PermFn {
     const typename H::Params* p;
     typename H::T* s;
@@ -253,15 +270,46 @@ static void hash_stages(p3g_ctx* ctx, p3g_tree* tree, const typename H::Params& 
     }
 }
 
+// Levels of many nodes: one launch each, one thread per node.  The small
+// levels are latency-bound: BabyBear runs them with one 16-lane group per
+// node (a launch per level up to COOP_MAX_NODES nodes, then one CTA for every
+// level of at most COOP_TAIL_NODES), Goldilocks with one CTA for every level
+// of at most TAIL_NODES.
 template <class H>
 static void levels(p3g_ctx* ctx, p3g_tree* tree, const typename H::Params& p, cudaStream_t st) {
     using T = typename H::T;
+    constexpr bool BB = std::is_same<H, HBB>::value;
     T* dig = static_cast<T*>(tree->d_digests);
-    for (size_t l = 1; l < tree->layer_size.size(); ++l) {
-        LevelFn<H> fn{&p, dig + tree->layer_off[l - 1] * H::DIG, tree->layer_size[l - 1],
-                      dig + tree->layer_off[l] * H::DIG, tree->layer_size[l], static_cast<const T*>(tree->inj[l]), st};
-        if constexpr (std::is_same<H, HBB>::value) dispatch_bb(ctx, fn);
+    const size_t nl = tree->layer_size.size();
+    const uint64_t tail_max = BB ? COOP_TAIL_NODES : uint64_t(TAIL_NODES);
+    size_t first_tail = nl;
+    while (first_tail > 1 && tree->layer_size[first_tail - 1] <= tail_max &&
+           nl - (first_tail - 1) <= size_t(TAIL_MAX_LEVELS))
+        --first_tail;
+    auto run = [&](const auto& fn) {
+        if constexpr (BB) dispatch_bb(ctx, fn);
         else dispatch_gl(ctx, fn);
+    };
+    auto level = [&](size_t l) -> typename TailLevels<T>::Level {
+        return {dig + tree->layer_off[l - 1] * H::DIG, dig + tree->layer_off[l] * H::DIG,
+                static_cast<const T*>(tree->inj[l]), uint32_t(tree->layer_size[l - 1]), uint32_t(tree->layer_size[l])};
+    };
+    for (size_t l = 1; l < first_tail; ++l) {
+        const uint64_t np = tree->layer_size[l];
+        if (BB && np <= COOP_MAX_NODES) {
+            TailLevels<T> t{};
+            t.lev[t.n++] = level(l);
+            run(CoopFn<H>{&p, &t, unsigned((np * 16 + COOP_THREADS - 1) / COOP_THREADS), st});
+        } else {
+            run(LevelFn<H>{&p, dig + tree->layer_off[l - 1] * H::DIG, tree->layer_size[l - 1],
+                           dig + tree->layer_off[l] * H::DIG, np, static_cast<const T*>(tree->inj[l]), st});
+        }
+    }
+    if (first_tail < nl) {
+        TailLevels<T> t{};
+        for (size_t l = first_tail; l < nl; ++l) t.lev[t.n++] = level(l);
+        if constexpr (BB) run(CoopFn<H>{&p, &t, 1u, st});
+        else run(TailFn<H>{&p, &t, st});
     }
 }
 

@@ -171,12 +171,10 @@ __global__ void __launch_bounds__(HASH_ROWS) k_hash_groups(typename H::Params p,
 // parent[j] = compress(parent[j], inj[j]) (merkle_tree.hpp:149-176,
 // fri_merkle_tree_mmcs.hpp:77-92).
 template <class H, int D, int RF, int RP>
-__global__ void __launch_bounds__(128) k_compress_level(typename H::Params p, const typename H::T* __restrict__ child,
-                                                        uint64_t nchild, typename H::T* __restrict__ parent,
-                                                        uint64_t nparent, const typename H::T* __restrict__ inj) {
+__device__ __forceinline__ void compress_node(const typename H::Params& p, const typename H::T* __restrict__ child,
+                                              uint64_t nchild, typename H::T* __restrict__ parent, uint64_t j,
+                                              const typename H::T* __restrict__ inj) {
     using T = typename H::T;
-    uint64_t j = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (j >= nparent) return;
     T s[H::W];
     const int iters = inj ? 2 : 1;
 #pragma unroll 1
@@ -200,6 +198,78 @@ __global__ void __launch_bounds__(128) k_compress_level(typename H::Params p, co
     }
 #pragma unroll
     for (int i = 0; i < H::DIG; ++i) parent[j * H::DIG + i] = H::squeeze(s[i]);
+}
+
+template <class H, int D, int RF, int RP>
+__global__ void __launch_bounds__(128) k_compress_level(typename H::Params p, const typename H::T* __restrict__ child,
+                                                        uint64_t nchild, typename H::T* __restrict__ parent,
+                                                        uint64_t nparent, const typename H::T* __restrict__ inj) {
+    uint64_t j = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (j >= nparent) return;
+    compress_node<H, D, RF, RP>(p, child, nchild, parent, j, inj);
+}
+
+// The top levels of a tree, each of at most TAIL_NODES parents, in one CTA,
+// one level after the other: the compressions of k_compress_level without a
+// launch per level (small trees and the tops of large ones are latency-bound).
+constexpr int TAIL_NODES = 256;
+constexpr int TAIL_MAX_LEVELS = 40;
+template <class T>
+struct TailLevels {
+    int n;
+    struct Level {
+        const T* child;
+        T* parent;
+        const T* inj;
+        uint32_t nchild, nparent;
+    } lev[TAIL_MAX_LEVELS];
+};
+
+template <class H, int D, int RF, int RP>
+__global__ void __launch_bounds__(TAIL_NODES) k_compress_tail(typename H::Params p, TailLevels<typename H::T> t) {
+#pragma unroll 1
+    for (int l = 0; l < t.n; ++l) {
+        const auto& lv = t.lev[l];
+        if (threadIdx.x < lv.nparent) compress_node<H, D, RF, RP>(p, lv.child, lv.nchild, lv.parent, threadIdx.x, lv.inj);
+        __syncthreads();  // the next level reads this one's digests
+    }
+}
+
+// BabyBear: compressions with one 16-lane group per node (p2_bb16_coop), for
+// levels too small to fill the GPU with one thread per node.  With one level
+// the grid covers its nodes; with several (the top of a tree) one CTA of
+// COOP_THREADS runs them in order.
+constexpr int COOP_THREADS = 1024;
+constexpr uint64_t COOP_TAIL_NODES = COOP_THREADS / 16;  // nodes of one pass of the CTA
+constexpr uint64_t COOP_MAX_NODES = 8192;                // larger levels: one thread per node
+
+template <int D, int RF, int RP>
+__global__ void __launch_bounds__(COOP_THREADS) k_compress_coop(P2BB16 p, TailLevels<uint32_t> t) {
+    const int i = threadIdx.x & 15;
+    const CoopConsts cc = coop_consts(p, i);
+    const uint64_t g = (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 4;
+    const uint64_t ng = (uint64_t(gridDim.x) * blockDim.x) >> 4;
+#pragma unroll 1
+    for (int l = 0; l < t.n; ++l) {
+        const auto& lv = t.lev[l];
+#pragma unroll 1
+        for (uint64_t base = 0; base < lv.nparent; base += ng) {  // uniform trip count: every lane shuffles
+            const uint64_t j = base + g;
+            const bool on = j < lv.nparent;
+            uint32_t x = 0;
+            if (on) {
+                if (i < 8) x = lv.child[2 * j * 8 + i];
+                else if (2 * j + 1 < lv.nchild) x = lv.child[(2 * j + 1) * 8 + i - 8];
+            }
+            x = p2_bb16_coop<D, RF, RP>(HBB::absorb(x), p, cc, i);
+            if (lv.inj) {  // compress(node, injected row digest)
+                if (i >= 8) x = HBB::absorb(on ? lv.inj[j * 8 + i - 8] : 0u);
+                x = p2_bb16_coop<D, RF, RP>(x, p, cc, i);
+            }
+            if (on && i < 8) lv.parent[j * 8 + i] = HBB::squeeze(x);
+        }
+        if (t.n > 1) __syncthreads();  // one CTA: the next level reads this one
+    }
 }
 
 template <class H, int D, int RF, int RP>
@@ -291,6 +361,9 @@ struct Launch {
                             cudaStream_t st);
     static void level(const typename H::Params& p, const T* child, uint64_t nchild, T* parent, uint64_t nparent,
                       const T* inj, cudaStream_t st);
+    static void tail(const typename H::Params& p, const TailLevels<T>& t, cudaStream_t st);
+    // BabyBear only: k_compress_coop on `blocks` CTAs (1 when t has several levels)
+    static void coop(const typename H::Params& p, const TailLevels<T>& t, unsigned blocks, cudaStream_t st);
     static void permute(const typename H::Params& p, T* states, uint64_t n, cudaStream_t st);
     static void grind(const typename H::Params& p, const GrindArgs<T, H::W>* d_args, uint64_t base, uint64_t count,
                       unsigned long long* found, int sm_count, cudaStream_t st);
@@ -337,6 +410,24 @@ void Launch<H, D, RF, RP>::grind(const typename H::Params& p, const GrindArgs<T,
     k_grind<H, D, RF, RP><<<unsigned(blocks), 128, 0, st>>>(p, d_args, base, count, found);
     P3G_LAUNCHED();
     P3G_CUDA(cudaGetLastError());
+}
+template <class H, int D, int RF, int RP>
+void Launch<H, D, RF, RP>::tail(const typename H::Params& p, const TailLevels<T>& t, cudaStream_t st) {
+    if (t.n == 0) return;
+    k_compress_tail<H, D, RF, RP><<<1, TAIL_NODES, 0, st>>>(p, t);
+    P3G_LAUNCHED();
+    P3G_CUDA(cudaGetLastError());
+}
+template <class H, int D, int RF, int RP>
+void Launch<H, D, RF, RP>::coop(const typename H::Params& p, const TailLevels<T>& t, unsigned blocks, cudaStream_t st) {
+    if constexpr (std::is_same<H, HBB>::value) {
+        if (t.n == 0) return;
+        k_compress_coop<D, RF, RP><<<blocks, COOP_THREADS, 0, st>>>(p, t);
+        P3G_LAUNCHED();
+        P3G_CUDA(cudaGetLastError());
+    } else {
+        throw Error(P3G_EUNSUPPORTED, "cooperative compression is BabyBear only");
+    }
 }
 template <class H, int D, int RF, int RP>
 void Launch<H, D, RF, RP>::permute(const typename H::Params& p, T* states, uint64_t n, cudaStream_t st) {

@@ -107,6 +107,71 @@ __device__ __forceinline__ void p2_bb16(uint32_t* s, const P2BB16& p) {
     }
 }
 
+// ------------------------------------------------------------------ BabyBear 16, one lane per word
+// The same permutation on 16 lanes of a warp (lanes 16g..16g+15 hold the
+// state of permutation g, one word each): for the latency-bound callers --
+// the small top levels of a tree and the transcript -- where one thread per
+// permutation waits on a long chain of dependent products.  Every lane runs
+// the same field operations as p2_bb16 on its word; MDS-light gathers the
+// lane's 4-chunk by shuffles and adds the column sums by an xor-reduction
+// over the chunks; a partial round reduces the 16 words the same way.
+// All 32 lanes of the warp must call it together.
+struct CoopConsts {  // this lane's constants
+    uint32_t ini[4], ter[4];
+    uint32_t shoup;  // floor(2^(32+i) / p) for the diagonal 2^i, i = lane
+};
+__device__ __forceinline__ CoopConsts coop_consts(const P2BB16& p, int i) {
+    CoopConsts c;
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        c.ini[r] = p.initial[r][i];
+        c.ter[r] = p.terminal[r][i];
+    }
+    c.shoup = c_bb_shoup_pow2[i];
+    return c;
+}
+
+__device__ __forceinline__ uint32_t coop_mds_light(uint32_t x, int i) {
+    const int base = i & ~3, pos = i & 3;
+    const uint32_t x0 = __shfl_sync(0xffffffffu, x, base, 16), x1 = __shfl_sync(0xffffffffu, x, base + 1, 16);
+    const uint32_t x2 = __shfl_sync(0xffffffffu, x, base + 2, 16), x3 = __shfl_sync(0xffffffffu, x, base + 3, 16);
+    const uint32_t t01 = bb::add(x0, x1), t23 = bb::add(x2, x3), t0123 = bb::add(t01, t23);
+    const uint32_t t01123 = bb::add(t0123, x1), t01233 = bb::add(t0123, x3);
+    uint32_t y;  // mat4 [2 3 1 1] row pos (external.hpp:67-77)
+    if (pos == 0) y = bb::add(t01123, t01);
+    else if (pos == 1) y = bb::add(t01123, bb::add(x2, x2));
+    else if (pos == 2) y = bb::add(t01233, t23);
+    else y = bb::add(t01233, bb::add(x0, x0));
+    uint32_t col = bb::add(y, __shfl_xor_sync(0xffffffffu, y, 4, 16));
+    col = bb::add(col, __shfl_xor_sync(0xffffffffu, col, 8, 16));
+    return bb::add(y, col);
+}
+
+template <int D, int RF, int RP>
+__device__ __forceinline__ uint32_t p2_bb16_coop(uint32_t x, const P2BB16& p, const CoopConsts& c, int i) {
+    x = coop_mds_light(x, i);
+#pragma unroll
+    for (int r = 0; r < RF / 2; ++r) x = coop_mds_light(bb_sbox(bb::add(x, c.ini[r]), D), i);
+#pragma unroll 1
+    for (int r = 0; r < RP; ++r) {
+        if (i == 0) x = bb_sbox(bb::add(x, p.internal[r]), D);
+        uint32_t sum = bb::add(x, __shfl_xor_sync(0xffffffffu, x, 1, 16));
+        sum = bb::add(sum, __shfl_xor_sync(0xffffffffu, sum, 2, 16));
+        sum = bb::add(sum, __shfl_xor_sync(0xffffffffu, sum, 4, 16));
+        sum = bb::add(sum, __shfl_xor_sync(0xffffffffu, sum, 8, 16));
+        uint32_t d = x;  // x * 2^i (diag[0] = 1)
+        if (i > 0) {
+            const uint32_t q = __umulhi(x, c.shoup);
+            const uint32_t r0 = (x << i) - q * bb::P, r1 = r0 - bb::P;
+            d = r0 < r1 ? r0 : r1;
+        }
+        x = bb::add(d, sum);
+    }
+#pragma unroll
+    for (int r = 0; r < RF / 2; ++r) x = coop_mds_light(bb_sbox(bb::add(x, c.ter[r]), D), i);
+    return x;
+}
+
 // ------------------------------------------------------------------ Goldilocks 8
 // x^d with the intermediate powers left below 2^64 but unreduced mod p
 // (a product accepts any u64 operands); only the result is canonical.
