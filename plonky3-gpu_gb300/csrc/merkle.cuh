@@ -254,6 +254,7 @@ __global__ void __launch_bounds__(COOP_THREADS) k_compress_coop(P2BB16 p, TailLe
         const auto& lv = t.lev[l];
 #pragma unroll 1
         for (uint64_t base = 0; base < lv.nparent; base += ng) {  // uniform trip count: every lane shuffles
+            if (base + (g & ~uint64_t(1)) >= lv.nparent) break;  // both groups of this warp idle from here on
             const uint64_t j = base + g;
             const bool on = j < lv.nparent;
             uint32_t x = 0;
