@@ -21,6 +21,7 @@ so no L2 flush is needed between steps.
 from __future__ import annotations
 
 import argparse
+import gc
 import json
 import os
 import statistics
@@ -420,6 +421,8 @@ def run_ours(args):
         torch.distributed.barrier()
     torch.cuda.synchronize(dev)
     l0 = P.kernel_launches()
+    gc.collect()
+    gc.disable()
     with ClockSampler(local) as clk:
         with torch.cuda.stream(stream):
             for i in range(args.steps):
@@ -427,6 +430,7 @@ def run_ours(args):
                 step()
             evs[-1].record(stream)
         torch.cuda.synchronize(dev)
+    gc.enable()
     launches = P.kernel_launches() - l0
     step_ms = [evs[i].elapsed_time(evs[i + 1]) for i in range(args.steps)]
     total_ms = evs[0].elapsed_time(evs[-1])
@@ -457,6 +461,8 @@ def run_ours(args):
     pinned.numpy().view(np.uint32)[:] = trace.reshape(-1)
     cap = np.zeros((1, 8), np.uint32)
     e2e_ms = []
+    gc.collect()
+    gc.disable()  # the interpreter's collector paused in the timed loop, as the timeit module does
     for i in range(args.warmup + args.steps):
         t0 = time.perf_counter()
         tree = ctx.commit_traces_host(P.BABYBEAR, [(pinned.data_ptr(), LOG_H, WIDTH, LOG_B, SHIFT)], 0,
@@ -465,6 +471,7 @@ def run_ours(args):
         dt = (time.perf_counter() - t0) * 1e3
         if i >= args.warmup:
             e2e_ms.append(dt)
+    gc.enable()
     torch.cuda.synchronize(dev)
     e2e_value, e2e_mean = job_throughput(float(elems), statistics.mean(e2e_ms), dev)
 
@@ -559,6 +566,7 @@ def run_ours(args):
                           f"{elems * 4 / 2**20:.0f} MiB LDE); no flush") if h * WIDTH * 4 > 129e6
                          else "inputs smaller than L2 (profiling case)",
                    "parallelism": f"replicas x{ws}"},
+        "python_gc": "collected before, paused during the timed loops (as the timeit module does)",
         "e2e": {"value": e2e_value, "unit": UNIT,
                 "h2d_bytes_per_step": h * WIDTH * 4, "d2h_bytes_per_step": 32,
                 "p50_ms": float(np.percentile(e2e_ms, 50)), "p99_ms": float(np.percentile(e2e_ms, 99)),
