@@ -475,44 +475,46 @@ def run_ours(args):
     torch.cuda.synchronize(dev)
     e2e_value, e2e_mean = job_throughput(float(elems), statistics.mean(e2e_ms), dev)
 
-    # ---- PCS open on the commit's resident bit-reversed LDE (2^21 x 256):
-    # opened values at 2 points and the reduced opening into a q vector
-    tree = ctx.commit_traces_device(P.BABYBEAR, [(d_trace.ptr, LOG_H, WIDTH, LOG_B, SHIFT)], 0, stream=sptr)
-    log_n = LOG_H + LOG_B
-    pts = rng.integers(0, BB_P, size=(2, 4), dtype=np.uint32)
-    alpha = rng.integers(0, BB_P, size=4, dtype=np.uint32)
-    d_q = ctx.alloc(H * 16, sptr)
-    ov = ctx.pcs_open_values_device(tree.leaf_ptr(0), log_n, WIDTH, True, SHIFT, pts, stream=sptr)
-    ctx.pcs_reduce_device(tree.leaf_ptr(0), log_n, WIDTH, True, SHIFT, pts, ov, alpha, 0, True, d_q.ptr, sptr)
-    torch.cuda.synchronize(dev)
-    open_reps = 5
-    e0.record(stream)
-    for _ in range(open_reps):
-        ctx.pcs_open_values_device(tree.leaf_ptr(0), log_n, WIDTH, True, SHIFT, pts, stream=sptr)
-    e1.record(stream)
-    torch.cuda.synchronize(dev)
-    open_ms = e0.elapsed_time(e1) / open_reps
-    e0.record(stream)
-    for _ in range(open_reps):
+    prover = {}
+    if not args.no_prover:
+        # ---- PCS open on the commit's resident bit-reversed LDE (2^21 x 256):
+        # opened values at 2 points and the reduced opening into a q vector
+        tree = ctx.commit_traces_device(P.BABYBEAR, [(d_trace.ptr, LOG_H, WIDTH, LOG_B, SHIFT)], 0, stream=sptr)
+        log_n = LOG_H + LOG_B
+        pts = rng.integers(0, BB_P, size=(2, 4), dtype=np.uint32)
+        alpha = rng.integers(0, BB_P, size=4, dtype=np.uint32)
+        d_q = ctx.alloc(H * 16, sptr)
+        ov = ctx.pcs_open_values_device(tree.leaf_ptr(0), log_n, WIDTH, True, SHIFT, pts, stream=sptr)
         ctx.pcs_reduce_device(tree.leaf_ptr(0), log_n, WIDTH, True, SHIFT, pts, ov, alpha, 0, True, d_q.ptr, sptr)
-    e1.record(stream)
-    torch.cuda.synchronize(dev)
-    reduce_ms = e0.elapsed_time(e1) / open_reps
-    # ---- prove_fri on that reduced opening (2^21 BabyBear^4), transcript on the
-    # device: commit-phase rounds, final polynomial, 16-bit query proof of work,
-    # 100 query indices and every round's openings (host clock; the call synchronises)
-    fri_params = dict(log_blowup=LOG_B, log_final_poly_len=0, max_log_arity=1, num_queries=100,
-                      commit_proof_of_work_bits=0, query_proof_of_work_bits=16)
-    st0 = rng.integers(0, BB_P, size=16, dtype=np.uint32)
-    ctx.fri_prove_device([(d_q.ptr, log_n)], fri_params, st0, [], [], stream=sptr)
-    fri_ms = []
-    for _ in range(3):
-        t0 = time.perf_counter()
-        fri_res = ctx.fri_prove_device([(d_q.ptr, log_n)], fri_params, st0, [], [], stream=sptr)
-        fri_ms.append((time.perf_counter() - t0) * 1e3)
-    d_q.free(sptr)
-    tree.free(sptr)
-    torch.cuda.synchronize(dev)
+        torch.cuda.synchronize(dev)
+        open_reps = 5
+        e0.record(stream)
+        for _ in range(open_reps):
+            ctx.pcs_open_values_device(tree.leaf_ptr(0), log_n, WIDTH, True, SHIFT, pts, stream=sptr)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        open_ms = e0.elapsed_time(e1) / open_reps
+        e0.record(stream)
+        for _ in range(open_reps):
+            ctx.pcs_reduce_device(tree.leaf_ptr(0), log_n, WIDTH, True, SHIFT, pts, ov, alpha, 0, True, d_q.ptr, sptr)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        reduce_ms = e0.elapsed_time(e1) / open_reps
+        # ---- prove_fri on that reduced opening (2^21 BabyBear^4), transcript on the
+        # device: commit-phase rounds, final polynomial, 16-bit query proof of work,
+        # 100 query indices and every round's openings (host clock; the call synchronises)
+        fri_params = dict(log_blowup=LOG_B, log_final_poly_len=0, max_log_arity=1, num_queries=100,
+                          commit_proof_of_work_bits=0, query_proof_of_work_bits=16)
+        st0 = rng.integers(0, BB_P, size=16, dtype=np.uint32)
+        ctx.fri_prove_device([(d_q.ptr, log_n)], fri_params, st0, [], [], stream=sptr)
+        fri_ms = []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            fri_res = ctx.fri_prove_device([(d_q.ptr, log_n)], fri_params, st0, [], [], stream=sptr)
+            fri_ms.append((time.perf_counter() - t0) * 1e3)
+        d_q.free(sptr)
+        tree.free(sptr)
+        torch.cuda.synchronize(dev)
 
     # ---- permutation ceiling: the same Poseidon2-16 on 2^22 register-resident
     # states (p3g_poseidon2_permute), no sponge or tree around it
@@ -530,18 +532,37 @@ def run_ours(args):
     perm_peak = n_states / (e0.elapsed_time(e1) / reps / 1e3)
     d_states.free()
 
-    # ---- proof-of-work search (DuplexChallenger::grind, p3g_grind) at 26 bits
-    # from 4 random challenger states: candidates searched per second, host
-    # clock around each call (the call synchronises)
-    grind_bits, grind_cand, grind_s = 26, 0, 0.0
-    ctx.grind(P.BABYBEAR, np.zeros(16, np.uint32), [], 8, stream=sptr)
-    for k in range(4):
-        st = rng.integers(0, BB_P, size=16, dtype=np.uint32)
-        t0 = time.perf_counter()
-        w = ctx.grind(P.BABYBEAR, st, [int(x) for x in st[:k]], grind_bits, stream=sptr)
-        grind_s += time.perf_counter() - t0
-        grind_cand += w + 1
+    if not args.no_prover:
+        # ---- proof-of-work search (DuplexChallenger::grind, p3g_grind) at 26 bits
+        # from 4 random challenger states: candidates searched per second, host
+        # clock around each call (the call synchronises)
+        grind_bits, grind_cand, grind_s = 26, 0, 0.0
+        ctx.grind(P.BABYBEAR, np.zeros(16, np.uint32), [], 8, stream=sptr)
+        for k in range(4):
+            st = rng.integers(0, BB_P, size=16, dtype=np.uint32)
+            t0 = time.perf_counter()
+            w = ctx.grind(P.BABYBEAR, st, [int(x) for x in st[:k]], grind_bits, stream=sptr)
+            grind_s += time.perf_counter() - t0
+            grind_cand += w + 1
 
+    if not args.no_prover:
+        prover = {
+            "pcs_open": {"workload": f"TwoAdicFriPcs::open passes on the resident bit-reversed LDE 2^{LOG_H + LOG_B} x "
+                                     f"{WIDTH}, 2 BabyBear^4 points",
+                         "open_values_ms": open_ms, "reduce_ms": reduce_ms,
+                         "lde_bytes": elems * 4,
+                         "open_values_gbs": elems * 4 / (open_ms / 1e3) / 1e9,
+                         "reduce_gbs": elems * 4 / (reduce_ms / 1e3) / 1e9},
+            "fri_prove": {"workload": f"prove_fri over the 2^{log_n} BabyBear^4 reduced opening above: "
+                                      f"{len(fri_res['log_arities'])} rounds of arity 2, final polynomial of 1, "
+                                      "16-bit query proof of work, 100 queries with openings; transcript on the device",
+                          "ms": statistics.median(fri_ms), "samples_ms": [round(x, 3) for x in fri_ms]},
+            "pow_grind": {"workload": f"DuplexChallenger::grind, {grind_bits} bits, 4 challenger states "
+                                      "(0-3 pending inputs), Poseidon2-16",
+                          "candidates": grind_cand, "ms": grind_s * 1e3,
+                          "perms_per_s": grind_cand / grind_s,
+                          "frac_of_perm_peak": grind_cand / grind_s / perm_peak},
+        }
     hbm, src = peaks()
     lde_bytes = 4 * WIDTH * (h + H)
     lde_gbs = lde_bytes / (lde_ms / 1e3) / 1e9
@@ -579,21 +600,6 @@ def run_ours(args):
                      "peak_source": src, "algorithmic_bytes": lde_bytes, "ms": lde_ms},
         "stages": {"lde_ms": lde_ms, "merkle_ms": hash_ms, "perms": perms,
                    "perms_per_s": perms / (hash_ms / 1e3) if hash_ms > 0 else None},
-        "pcs_open": {"workload": f"TwoAdicFriPcs::open passes on the resident bit-reversed LDE 2^{LOG_H + LOG_B} x "
-                                 f"{WIDTH}, 2 BabyBear^4 points",
-                     "open_values_ms": open_ms, "reduce_ms": reduce_ms,
-                     "lde_bytes": elems * 4,
-                     "open_values_gbs": elems * 4 / (open_ms / 1e3) / 1e9,
-                     "reduce_gbs": elems * 4 / (reduce_ms / 1e3) / 1e9},
-        "fri_prove": {"workload": f"prove_fri over the 2^{log_n} BabyBear^4 reduced opening above: "
-                                  f"{len(fri_res['log_arities'])} rounds of arity 2, final polynomial of 1, "
-                                  "16-bit query proof of work, 100 queries with openings; transcript on the device",
-                      "ms": statistics.median(fri_ms), "samples_ms": [round(x, 3) for x in fri_ms]},
-        "pow_grind": {"workload": f"DuplexChallenger::grind, {grind_bits} bits, 4 challenger states "
-                                  "(0-3 pending inputs), Poseidon2-16",
-                      "candidates": grind_cand, "ms": grind_s * 1e3,
-                      "perms_per_s": grind_cand / grind_s,
-                      "frac_of_perm_peak": grind_cand / grind_s / perm_peak},
         "hash_roofline": {"kernel": "Merkle stage (k_hash_groups leaf sponge + k_compress_level)",
                           "bound": "integer multiply pipe (permutation issue)",
                           "achieved": perms / (hash_ms / 1e3) if hash_ms > 0 else None, "unit": "perms/s",
@@ -601,6 +607,7 @@ def run_ours(args):
                           "peak_source": "isolated Poseidon2-16 permutation throughput, same run",
                           "frac": perms / (hash_ms / 1e3) / perm_peak if hash_ms > 0 else None},
     }
+    result.update(prover)
     if not args.no_goldilocks:
         result["config2"] = run_goldilocks(P, torch, ctx, dev, stream, max(3, args.steps // 2), args.warmup)
     if not args.no_batched:
@@ -633,6 +640,8 @@ def main():
     ap.add_argument("--no-goldilocks", action="store_true", help="skip the Goldilocks 2^18 x 128 commit")
     ap.add_argument("--no-batched", action="store_true", help="skip the 64-trace batched comparison")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop latency sweep")
+    ap.add_argument("--no-prover", action="store_true",
+                    help="skip the PCS-open, FRI and proof-of-work measurements (profiling the commit alone)")
     ap.add_argument("--serving-requests", type=int, default=200, help="requests per arrival rate")
     ap.add_argument("--log-h", type=int, default=LOG_H, help="trace log2 height (profiling cases)")
     ap.add_argument("--width", type=int, default=WIDTH, help="trace width (profiling cases)")
