@@ -59,3 +59,49 @@ def test_seeded_constants_match_oracle():
     oi, ot, on = O.example_constants_gl8()
     assert [int(x) for x in ini] == [int(x) for x in oi.reshape(-1)]
     assert [int(x) for x in inr] == [int(x) for x in on]
+
+
+def _fri_rounds(heights, **kw):
+    prm = P.FriParams(**{**dict(log_blowup=1, log_final_poly_len=0, max_log_arity=1, num_queries=4,
+                                commit_proof_of_work_bits=0, query_proof_of_work_bits=0), **kw})
+    lh = (C.c_uint32 * len(heights))(*heights)
+    n = C.c_uint32()
+    las = (C.c_uint32 * 32)()
+    st = P.load().p3g_fri_rounds(lh, len(heights), C.byref(prm), C.byref(n), las)
+    return st, [las[i] for i in range(n.value)]
+
+
+@pytest.mark.parametrize("heights,max_la,log_fpl", [
+    ([21], 1, 0), ([12, 10, 9, 5], 3, 2), ([14], 2, 0), ([9, 8, 7, 6, 5, 4], 1, 1), ([11, 6], 3, 3),
+    ([27, 3], 3, 0)])
+def test_fri_rounds_follow_compute_log_arity_for_round(heights, max_la, log_fpl):
+    """p3g_fri_rounds (host logic, no GPU) against the oracle's restatement of
+    compute_log_arity_for_round (fri_params.hpp:36-57) driving prove_fri's loop."""
+    import oracle as O
+    st, got = _fri_rounds(heights, max_log_arity=max_la, log_final_poly_len=log_fpl)
+    assert st == 0
+    log_final = 1 + log_fpl
+    want, cur, idx = [], heights[0], 1
+    while cur > log_final:
+        has_next = idx < len(heights)
+        la = O.fri_log_arity(cur, has_next, heights[idx] if has_next else 0, log_final, max_la)
+        if la == 0:
+            break
+        want.append(la)
+        cur -= la
+        if has_next and heights[idx] == cur:
+            idx += 1
+    assert got == want
+
+
+@pytest.mark.parametrize("heights,kw,status", [
+    ([6, 6], {}, 1),                           # heights must strictly decrease
+    ([6], dict(max_log_arity=0), 1),
+    ([6], dict(max_log_arity=4), 5),           # fold arities up to 8
+    ([1], {}, 1),                              # smallest input not above the final domain (2^1)
+    ([28], {}, 1),
+    ([12], dict(num_queries=1025), 1),
+    ([12], dict(commit_proof_of_work_bits=25), 1),
+])
+def test_fri_rounds_rejects_bad_arguments(heights, kw, status):
+    assert _fri_rounds(heights, **kw)[0] == status
