@@ -22,3 +22,20 @@ def test_adapters_drop_into_reference_types(tmp_path):
     rc, log = compile_cpp("adapters_reference.cpp", str(tmp_path / "ref"), ["-I", REF_INCLUDE])
     assert rc == 0, log
     assert os.path.exists(tmp_path / "ref")
+
+
+@pytest.mark.skipif(not os.path.isdir(REF_INCLUDE), reason="reference headers not present")
+def test_proof_wire_format_round_trips_through_reference_verifier(tmp_path):
+    """include/p3g_proof.hpp: a TwoAdicFriPcs proof and its opened values made by
+    the reference's own prover survive encode/decode byte for byte, the
+    reference's verifier accepts the decoded objects and rejects a changed
+    opened value, and malformed input is refused (tests/cpp/proof_wire.cpp;
+    host code only, so it runs here)."""
+    import subprocess
+    out = str(tmp_path / "wire")
+    rc, log = compile_cpp("proof_wire.cpp", out, ["-I", REF_INCLUDE])
+    assert rc == 0, log
+    assert "warning" not in log, log
+    r = subprocess.run([out], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "ALL OK" in r.stdout
