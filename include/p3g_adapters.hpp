@@ -473,6 +473,28 @@ public:
         return (v & mask) == 0;
     }
 
+    // The state as p3g_fri_prove takes and returns it (BabyBear), so a device
+    // prove_fri can continue this transcript and hand it back.
+    p3g_challenger state() const {
+        static_assert(sizeof(F) == 4, "p3g_challenger holds the BabyBear challenger");
+        p3g_challenger c{};
+        for (size_t i = 0; i < WIDTH; ++i) c.sponge_state[i] = uint32_t(canonical(state_[i]));
+        for (size_t i = 0; i < in_.size(); ++i) c.input[i] = uint32_t(canonical(in_[i]));
+        for (size_t i = 0; i < out_.size(); ++i) c.output[i] = uint32_t(canonical(out_[i]));
+        c.n_input = uint32_t(in_.size());
+        c.n_output = uint32_t(out_.size());
+        return c;
+    }
+    void set_state(const p3g_challenger& c) {
+        static_assert(sizeof(F) == 4, "p3g_challenger holds the BabyBear challenger");
+        if (c.n_input >= RATE || c.n_output > RATE) throw std::invalid_argument("set_state: buffers out of range");
+        for (size_t i = 0; i < WIDTH; ++i) state_[i] = F(c.sponge_state[i]);
+        in_.clear();
+        for (uint32_t i = 0; i < c.n_input; ++i) in_.push_back(F(c.input[i]));
+        out_.clear();
+        for (uint32_t i = 0; i < c.n_output; ++i) out_.push_back(F(c.output[i]));
+    }
+
 private:
     void absorb(F v) {
         in_.push_back(v);

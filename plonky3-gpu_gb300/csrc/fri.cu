@@ -292,8 +292,9 @@ void fri_prove(p3g_ctx* ctx, const void* const* d_inputs, const uint32_t* log_he
     for (uint32_t i = 0; i < n_inputs; ++i) P3G_REQUIRE(d_inputs[i], "fri: null input");
     P3G_REQUIRE(chal->n_input < 8 && chal->n_output <= 8, "fri: challenger buffers out of range");
     for (int i = 0; i < 16; ++i) P3G_REQUIRE(chal->sponge_state[i] < bb::P, "fri: challenger state not canonical");
-    for (int i = 0; i < 8; ++i)
-        P3G_REQUIRE(chal->input[i] < bb::P && chal->output[i] < bb::P, "fri: challenger buffers not canonical");
+    for (uint32_t i = 0; i < chal->n_input; ++i) P3G_REQUIRE(chal->input[i] < bb::P, "fri: challenger input not canonical");
+    for (uint32_t i = 0; i < chal->n_output; ++i)
+        P3G_REQUIRE(chal->output[i] < bb::P, "fri: challenger output not canonical");
     if (!ctx->has_p2bb) throw Error(P3G_ESTATE, "Poseidon2 constants for BabyBear are not set");
     const auto rounds = plan_rounds(log_heights, n_inputs, prm);
     const int R = int(rounds.size());

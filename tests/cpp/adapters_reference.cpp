@@ -182,6 +182,9 @@ int main() {
             cpu.observe_algebra_element(a);
             gpu.observe_algebra_element(b);
         }
+        p3g::GpuDuplexChallenger<BB, Wrap, 16, 8> resumed(Wrap{pos});
+        resumed.set_state(gpu.state());
+        for (int k = 0; k < 10; ++k) ok = ok && resumed.sample() == cpu.sample();
         fails += report("DuplexChallenger with grind on the GPU", ok);
     }
     std::printf("%s\n", fails ? "MISMATCH" : "ALL OK");

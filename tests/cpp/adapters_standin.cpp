@@ -171,6 +171,12 @@ static int run_challenger(int argc, char** a) {
         out.insert(out.end(), reinterpret_cast<const unsigned char*>(&w), reinterpret_cast<const unsigned char*>(&w) + 8);
         out.insert(out.end(), reinterpret_cast<const unsigned char*>(&v), reinterpret_cast<const unsigned char*>(&v) + 4);
     }
+    // state() / set_state() carry the transcript over: a copy continues identically
+    ch.observe(BabyBear(5u));
+    p3g::GpuDuplexChallenger<BabyBear, DevicePermBB, 16, 8> copy{DevicePermBB{}};
+    copy.set_state(ch.state());
+    for (int k = 0; k < 10; ++k)
+        if (!(copy.sample() == ch.sample())) return 6;
     write_file(a[2], out);
     return 0;
 }
