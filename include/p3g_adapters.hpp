@@ -14,6 +14,7 @@
 //   GpuInputMmcs<p3_merkle::MerkleTreeMmcs<...>>   commit_matrix        (fri_merkle_tree_mmcs.hpp:55)
 //   GpuMerkleTreeMmcs<p3_merkle_tree::MerkleTreeMmcs<...>> commit       (merkle_tree_mmcs.hpp:100)
 //   gpu_fold_matrix<Val, Challenge>(...)          fold_matrix           (fri_folding.hpp:200)
+//   fold_matrix_cuda / fold_matrix_cuda_device     the reference's GPU fold (fri_fold_cuda.hpp:250-348)
 //   GpuDuplexChallenger<F, Perm, WIDTH, RATE>     DuplexChallenger with grind on the GPU
 //                                                  (duplex_challenger.hpp:42-285)
 //
@@ -373,6 +374,31 @@ std::vector<Challenge> gpu_fold_matrix(size_t log_height, size_t log_arity, cons
         }
     }
     return res;
+}
+
+// fold_matrix_cuda (fri_fold_cuda.hpp:300-348): the reference's GPU fold, same
+// arguments in its order (beta first), host vectors in and out.
+template <class Val, class Challenge>
+std::vector<Challenge> fold_matrix_cuda(const Challenge& beta, size_t log_arity, size_t log_height,
+                                        const std::vector<Challenge>& current) {
+    return gpu_fold_matrix<Val, Challenge>(log_height, log_arity, beta, current);
+}
+
+// fold_matrix_cuda_device (fri_fold_cuda.hpp:250-277): device buffers already
+// sized (d_input n * 2^log_arity values, d_output n), no allocation or copy,
+// synchronises the device before returning like the reference.  Challenge is
+// BabyBear4 (four canonical u32 coefficients in memory, as the kernel reads them).
+template <class Val, class Challenge>
+void fold_matrix_cuda_device(const Challenge* d_input, Challenge* d_output, const Challenge& beta, size_t log_arity,
+                             size_t log_height, size_t n) {
+    static_assert(sizeof(Val) == 4 && sizeof(Challenge) == 16, "fold runs over BabyBear^4");
+    if (log_arity < 1 || log_arity > 3) throw std::invalid_argument("log_arity must be 1, 2, or 3");
+    if (log_height < log_arity || n != (size_t(1) << log_height) >> log_arity)
+        throw std::invalid_argument("fold_matrix_cuda_device: n must be 2^log_height / 2^log_arity");
+    const uint32_t b[4] = {beta[0].value(), beta[1].value(), beta[2].value(), beta[3].value()};
+    check(p3g_fold_matrix_bb4(Context::get().handle(), d_input, uint32_t(log_height), uint32_t(log_arity), b, d_output,
+                              nullptr));
+    check(p3g_stream_synchronize(Context::get().handle(), nullptr));
 }
 
 // ----------------------------------------------------------------- challenger

@@ -158,8 +158,9 @@ int main() {
             const BabyBear4 beta({r(), r(), r(), r()});
             auto want = p3_fri::TwoAdicFriFolding<BB, BabyBear4>::fold_matrix(log_h, la, beta, v);
             auto got = p3g::gpu_fold_matrix<BB, BabyBear4>(log_h, la, beta, v);
+            auto got_cuda = p3g::fold_matrix_cuda<BB, BabyBear4>(beta, la, log_h, v);  // fri_fold_cuda.hpp's order
             fails += report(la == 1 ? "fold_matrix arity 2" : la == 2 ? "fold_matrix arity 4" : "fold_matrix arity 8",
-                            want == got);
+                            want == got && want == got_cuda);
         }
     }
     // 5. the challenger

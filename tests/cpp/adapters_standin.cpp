@@ -10,6 +10,7 @@
 //   adapters_standin commit_matrix <in> <out> <height> <width>
 //   adapters_standin mmcs <bb|gl> <in> <out> <cap_height> <h0> <w0> [<h1> <w1> ...]
 //   adapters_standin fold <in> <out> <log_height> <log_arity>
+//   adapters_standin fold_cuda <in> <out> <log_height> <log_arity>   (host and device forms)
 //   adapters_standin dft <bb|gl> <in> <out> <log_h> <width> <kind 0-3> <shift>
 //   adapters_standin challenger <out> <seed> <n_obs> <bits>...
 //
@@ -254,6 +255,32 @@ int main(int argc, char** argv) {
             std::vector<unsigned char> out;
             append_layers(out, pd.tree);
             write_file(argv[3], out);
+            return 0;
+        }
+        if (cmd == "fold_cuda") {  // fold_matrix_cuda (host) and fold_matrix_cuda_device must agree
+            auto in = read_file(argv[2]);
+            const size_t log_h = std::strtoul(argv[4], nullptr, 0), la = std::strtoul(argv[5], nullptr, 0);
+            auto words = p3g::from_words<BabyBear>(in.data(), 4 + (size_t(4) << log_h));
+            BabyBear4 beta;
+            for (int k = 0; k < 4; ++k) beta[k] = words[k];
+            std::vector<BabyBear4> cur(size_t(1) << log_h);
+            for (size_t i = 0; i < cur.size(); ++i)
+                for (int k = 0; k < 4; ++k) cur[i][k] = words[4 + 4 * i + k];
+            auto host = p3g::fold_matrix_cuda<BabyBear, BabyBear4>(beta, la, log_h, cur);
+            const size_t n = cur.size() >> la;
+            p3g::DeviceBuffer din(cur.size() * 16), dout(n * 16);
+            din.upload(cur.data(), cur.size() * 16);
+            p3g::fold_matrix_cuda_device<BabyBear, BabyBear4>(static_cast<const BabyBear4*>(din.get()),
+                                                              static_cast<BabyBear4*>(dout.get()), beta, la, log_h, n);
+            std::vector<BabyBear4> dev(n);
+            dout.download(dev.data(), n * 16);
+            std::vector<BabyBear> flat;
+            for (size_t i = 0; i < n; ++i)
+                for (int k = 0; k < 4; ++k) {
+                    if (!(dev[i][k] == host[i][k])) return 7;
+                    flat.push_back(host[i][k]);
+                }
+            write_file(argv[3], p3g::to_words(flat));
             return 0;
         }
         if (cmd == "fold") {

@@ -129,6 +129,20 @@ def test_gpu_fold_matrix(prog, tmp_path, log_arity):
     assert np.array_equal(got, O.fold_matrix_bb4(v, log_h, log_arity, beta))
 
 
+@pytest.mark.parametrize("log_arity", [1, 2, 3])
+def test_fold_matrix_cuda_forms(prog, tmp_path, log_arity):
+    """fold_matrix_cuda / fold_matrix_cuda_device (the reference's GPU fold
+    signatures, fri_fold_cuda.hpp:250-348) agree with each other and the oracle."""
+    rng = np.random.default_rng(60 + log_arity)
+    log_h = 12
+    v = rng.integers(0, O.BB_P, size=(1 << log_h, 4), dtype=np.uint32)
+    beta = rng.integers(0, O.BB_P, size=4, dtype=np.uint32)
+    rc, err, fout = _run(prog, tmp_path, "fold_cuda", None, [log_h, log_arity], np.concatenate([beta, v.reshape(-1)]))
+    assert rc == 0, err
+    got = np.fromfile(fout, dtype=np.uint32).reshape(-1, 4)
+    assert np.array_equal(got, O.fold_matrix_bb4(v, log_h, log_arity, beta))
+
+
 def test_gpu_duplex_challenger_grind(prog, tmp_path, golden):
     """GpuDuplexChallenger's observe / grind / sample sequence gives the
     witnesses and samples of the reference's DuplexChallenger."""
