@@ -15,6 +15,7 @@
 //   GpuMerkleTreeMmcs<p3_merkle_tree::MerkleTreeMmcs<...>> commit       (merkle_tree_mmcs.hpp:100)
 //   gpu_fold_matrix<Val, Challenge>(...)          fold_matrix           (fri_folding.hpp:200)
 //   fold_matrix_cuda / fold_matrix_cuda_device     the reference's GPU fold (fri_fold_cuda.hpp:250-348)
+//   build_merkle_tree_cuda<F, WIDTH, RATE, ...>    the reference's GPU tree build (merkle_tree_cuda.hpp:358)
 //   GpuDuplexChallenger<F, Perm, WIDTH, RATE>     DuplexChallenger with grind on the GPU
 //                                                  (duplex_challenger.hpp:42-285)
 //
@@ -40,6 +41,11 @@
 #include <vector>
 
 #include "p3g.h"
+
+namespace p3_merkle_tree {  // the reference's tree type (merkle_tree.hpp:45-58), for build_merkle_tree_cuda
+template <typename F, typename W, size_t DIGEST_ELEMS>
+struct MerkleTree;
+}  // namespace p3_merkle_tree
 
 namespace p3g {
 
@@ -374,6 +380,41 @@ std::vector<Challenge> gpu_fold_matrix(size_t log_height, size_t log_arity, cons
         }
     }
     return res;
+}
+
+// build_merkle_tree_cuda (merkle_tree_cuda.hpp:358-621): the reference's GPU
+// tree build with the same template parameters and arguments, returning the
+// reference's MerkleTree<F, F, DIGEST_ELEMS> (leaves moved in, every digest
+// layer).  The context takes h_poseidon's constants.  Supported: BabyBear
+// WIDTH 16 RATE 8 DIGEST 8, Goldilocks WIDTH 8 RATE 4 DIGEST 4.
+template <typename F, size_t WIDTH, size_t RATE, size_t DIGEST_ELEMS, size_t ROUNDS_F, size_t ROUNDS_P, uint64_t D,
+          class Mat, class Pos>
+p3_merkle_tree::MerkleTree<F, F, DIGEST_ELEMS> build_merkle_tree_cuda(std::vector<Mat> matrices, const Pos& h_poseidon,
+                                                                      size_t cap_height) {
+    static_assert((sizeof(F) == 4 && WIDTH == 16 && RATE == 8 && DIGEST_ELEMS == 8) ||
+                      (sizeof(F) == 8 && WIDTH == 8 && RATE == 4 && DIGEST_ELEMS == 4),
+                  "BabyBear 16/8/8 or Goldilocks 8/4/4");
+    constexpr size_t E = sizeof(F);
+    if (matrices.empty()) throw std::invalid_argument("need at least one matrix");
+    Context::get().set_poseidon2(h_poseidon.initial_external_constants, h_poseidon.terminal_external_constants,
+                                 h_poseidon.internal_constants, uint32_t(D));
+    std::vector<std::unique_ptr<DeviceBuffer>> bufs;
+    std::vector<p3g_matrix> descs;
+    for (const auto& m : matrices) {
+        auto words = to_words(m.values);
+        bufs.emplace_back(new DeviceBuffer(std::max<size_t>(words.size(), E)));
+        if (!words.empty()) bufs.back()->upload(words.data(), words.size());
+        descs.push_back(p3g_matrix{bufs.back()->get(), uint64_t(m.height()), uint32_t(m.width()), 0});
+    }
+    p3g_ctx* ctx = Context::get().handle();
+    p3g_tree* tree = nullptr;
+    check(p3g_mmcs_commit(ctx, field_id<F>(), descs.data(), descs.size(), uint32_t(cap_height), &tree, nullptr,
+                          nullptr));
+    p3_merkle_tree::MerkleTree<F, F, DIGEST_ELEMS> out;
+    out.digest_layers = download_layers<std::array<F, DIGEST_ELEMS>>(ctx, tree);
+    check(p3g_tree_free(ctx, tree, nullptr));
+    out.leaves = std::move(matrices);
+    return out;
 }
 
 // fold_matrix_cuda (fri_fold_cuda.hpp:300-348): the reference's GPU fold, same

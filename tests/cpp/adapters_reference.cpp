@@ -24,6 +24,7 @@
 #include "padding_free_sponge.hpp"
 #include "truncated_permutation.hpp"
 #include "merkle_tree_mmcs.hpp"
+#include "merkle_tree_cuda.hpp"
 #include "fri_merkle_tree_mmcs.hpp"
 #include "fri_extension_mmcs.hpp"
 #include "fri_folding.hpp"
@@ -129,6 +130,10 @@ int main() {
             ok = ok && cpu.verify_batch(cap_gpu, dims, index, opening);
         }
         fails += report("open_batch on the GPU tree verifies", ok);
+        // the reference's GPU tree-build signature (its CPU fallback in this build)
+        auto want = p3_merkle_tree::build_merkle_tree_cuda<BB, 16, 8, 8, 8, 13, 7>(mats(), pos, 1);
+        auto got = p3g::build_merkle_tree_cuda<BB, 16, 8, 8, 8, 13, 7>(mats(), pos, 1);
+        fails += report("build_merkle_tree_cuda digest layers", want.digest_layers == got.digest_layers);
     }
 
     // 3. the other Dft members against Radix2Dit

@@ -9,6 +9,7 @@
 //   adapters_standin lde <bb|gl> <in> <out> <log_h> <width> <added_bits> <shift>
 //   adapters_standin commit_matrix <in> <out> <height> <width>
 //   adapters_standin mmcs <bb|gl> <in> <out> <cap_height> <h0> <w0> [<h1> <w1> ...]
+//   adapters_standin build_tree <bb|gl> <in> <out> <cap_height> <h0> <w0> ...   (build_merkle_tree_cuda)
 //   adapters_standin fold <in> <out> <log_height> <log_arity>
 //   adapters_standin fold_cuda <in> <out> <log_height> <log_arity>   (host and device forms)
 //   adapters_standin dft <bb|gl> <in> <out> <log_h> <width> <kind 0-3> <shift>
@@ -102,7 +103,22 @@ struct MixedMmcs {
     MixedMmcs(Sponge, Trunc, size_t) {}
 };
 
+template <class F, size_t W, size_t RF, size_t RP, uint64_t D>
+struct Poseidon2Cuda {  // the members build_merkle_tree_cuda reads (poseidon2_cuda.hpp:37-45)
+    F initial_external_constants[RF / 2][W];
+    F terminal_external_constants[RF / 2][W];
+    F internal_constants[RP];
+};
+
 }  // namespace standin
+
+namespace p3_merkle_tree {  // the reference's tree type, as the adapter's declaration expects
+template <typename F, typename W, size_t DIGEST_ELEMS>
+struct MerkleTree {
+    std::vector<standin::RowMajorMatrix<F>> leaves;
+    std::vector<std::vector<std::array<W, DIGEST_ELEMS>>> digest_layers;
+};
+}  // namespace p3_merkle_tree
 
 using namespace standin;
 
@@ -233,6 +249,47 @@ static int run_mmcs(int argc, char** a) {
     return 0;
 }
 
+// build_merkle_tree_cuda with the seeded constants in a Poseidon2Cuda-like struct
+template <class F>
+static int run_build_tree(int argc, char** a) {
+    auto in = read_file(a[3]);
+    const size_t cap = std::strtoul(a[5], nullptr, 0);
+    constexpr size_t E = sizeof(F);
+    std::vector<RowMajorMatrix<F>> mats;
+    size_t off = 0;
+    for (int i = 6; i + 1 < argc; i += 2) {
+        const size_t h = std::strtoul(a[i], nullptr, 0), w = std::strtoul(a[i + 1], nullptr, 0);
+        mats.emplace_back(p3g::from_words<F>(in.data() + off, h * w), w);
+        off += h * w * E;
+    }
+    std::vector<unsigned char> out;
+    if constexpr (E == 4) {
+        Poseidon2Cuda<F, 16, 8, 13, 7> pos;
+        std::mt19937 r32(0xdeadbeef);
+        for (size_t r = 0; r < 4; ++r)
+            for (size_t i = 0; i < 16; ++i) {
+                pos.initial_external_constants[r][i] = F(uint32_t(r32() % F::PRIME));
+                pos.terminal_external_constants[r][i] = F(uint32_t(r32() % F::PRIME));
+            }
+        for (size_t r = 0; r < 13; ++r) pos.internal_constants[r] = F(uint32_t(r32() % F::PRIME));
+        auto tree = p3g::build_merkle_tree_cuda<F, 16, 8, 8, 8, 13, 7>(std::move(mats), pos, cap);
+        append_layers(out, tree.digest_layers);
+    } else {
+        Poseidon2Cuda<F, 8, 8, 22, 7> pos;
+        std::mt19937_64 r64(12345);
+        for (size_t r = 0; r < 4; ++r)
+            for (size_t i = 0; i < 8; ++i) {
+                pos.initial_external_constants[r][i] = F(r64() % F::PRIME);
+                pos.terminal_external_constants[r][i] = F(r64() % F::PRIME);
+            }
+        for (size_t r = 0; r < 22; ++r) pos.internal_constants[r] = F(r64() % F::PRIME);
+        auto tree = p3g::build_merkle_tree_cuda<F, 8, 4, 4, 8, 22, 7>(std::move(mats), pos, cap);
+        append_layers(out, tree.digest_layers);
+    }
+    write_file(a[4], out);
+    return 0;
+}
+
 int main(int argc, char** argv) {
     if (argc < 4) return 2;
     const std::string cmd = argv[1];
@@ -244,6 +301,9 @@ int main(int argc, char** argv) {
             if (argc < 9) return 2;
             return std::string(argv[2]) == "bb" ? run_dft<BabyBear>(argv) : run_dft<Goldilocks>(argv);
         }
+        if (cmd == "build_tree")
+            return std::string(argv[2]) == "bb" ? run_build_tree<BabyBear>(argc, argv)
+                                                : run_build_tree<Goldilocks>(argc, argv);
         if (cmd == "mmcs")
             return std::string(argv[2]) == "bb" ? run_mmcs<BabyBear, 8>(argc, argv) : run_mmcs<Goldilocks, 4>(argc, argv);
         if (cmd == "commit_matrix") {

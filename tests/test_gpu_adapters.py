@@ -99,6 +99,18 @@ def test_gpu_input_mmcs_commit_matrix(prog, tmp_path, h, w):
     ("gl", 1, [(256, 5), (128, 3), (256, 1)]),
 ])
 def test_gpu_merkle_tree_mmcs_commit(prog, tmp_path, field, cap, shapes):
+    _mixed_tree(prog, tmp_path, "mmcs", field, cap, shapes)
+
+
+@pytest.mark.parametrize("field,cap,shapes", [
+    ("bb", 0, [(64, 9), (32, 4), (64, 16)]), ("bb", 2, [(256, 8)]), ("gl", 1, [(128, 5), (32, 3), (128, 2)])])
+def test_build_merkle_tree_cuda_adapter(prog, tmp_path, field, cap, shapes):
+    """build_merkle_tree_cuda with the reference's signature (constants taken
+    from a Poseidon2Cuda-like struct) builds the oracle's layers."""
+    _mixed_tree(prog, tmp_path, "build_tree", field, cap, shapes)
+
+
+def _mixed_tree(prog, tmp_path, cmd, field, cap, shapes):
     rng = np.random.default_rng(len(shapes) * 7 + cap)
     if field == "bb":
         mats = [rng.integers(0, O.BB_P, size=s, dtype=np.uint32) for s in shapes]
@@ -108,7 +120,7 @@ def test_gpu_merkle_tree_mmcs_commit(prog, tmp_path, field, cap, shapes):
         params, digest = O.gl8_params(), 4
     flat = np.concatenate([m.reshape(-1) for m in mats])
     rest = [cap] + [x for s in shapes for x in s]
-    rc, err, fout = _run(prog, tmp_path, "mmcs", field, rest, flat)
+    rc, err, fout = _run(prog, tmp_path, cmd, field, rest, flat)
     assert rc == 0, err
     want = O.mmcs_commit(params, mats, cap)
     got = _layers(np.fromfile(fout, dtype=flat.dtype), [l.shape[0] for l in want], digest)
