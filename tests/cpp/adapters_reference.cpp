@@ -10,7 +10,8 @@
 //      against the stock Pcs (same commitment);
 //   2. GpuMerkleTreeMmcs<mixed-height MMCS>::commit against the stock one (all
 //      digest layers), then the stock open_batch / verify_batch on the GPU tree;
-//   3. GpuDft's dft / idft / coset_dft / coset_idft against Radix2Dit's;
+//   3. GpuDft's dft / idft / coset_dft / coset_idft against Radix2Dit's, and
+//      GpuDft over the reference's NttCuda;
 //   4. gpu_fold_matrix against TwoAdicFriFolding<BB, BB4>::fold_matrix;
 //   5. GpuDuplexChallenger against DuplexChallenger: the same observations,
 //      samples, sample_bits and grind witnesses.
@@ -19,6 +20,7 @@
 #include "extension_field.hpp"
 #include "dense_matrix.hpp"
 #include "radix2_dit.hpp"
+#include "ntt_cuda.hpp"
 #include "util.hpp"
 #include "poseidon2_cuda.hpp"
 #include "padding_free_sponge.hpp"
@@ -150,6 +152,13 @@ int main() {
             ok = ok && cpu.coset_idft_batch(m(), shift).values == gpu.coset_idft_batch(m(), shift).values;
         }
         fails += report("dft_batch / idft_batch / coset_dft_batch / coset_idft_batch", ok);
+        // the same adapter over the reference's own GPU NTT class
+        p3g::GpuDft<p3_dft::NttCuda<BB>> gpu_ntt;
+        auto m = [&] { return rand_matrix(size_t(1) << 12, 6, 400); };
+        bool ok2 = cpu.coset_lde_batch(m(), 1, BB(uint32_t(31))).values ==
+                       gpu_ntt.coset_lde_batch(m(), 1, BB(uint32_t(31))).values &&
+                   cpu.dft_batch(m()).values == gpu_ntt.dft_batch(m()).values;
+        fails += report("GpuDft<NttCuda<BabyBear>> in place of NttCuda", ok2);
     }
 
     // 4. fold_matrix
