@@ -16,6 +16,8 @@
 //   gpu_fold_matrix<Val, Challenge>(...)          fold_matrix           (fri_folding.hpp:200)
 //   fold_matrix_cuda / fold_matrix_cuda_device     the reference's GPU fold (fri_fold_cuda.hpp:250-348)
 //   build_merkle_tree_cuda<F, WIDTH, RATE, ...>    the reference's GPU tree build (merkle_tree_cuda.hpp:358)
+//   gpu_prove_fri<Val, Challenge, ...>(...)        prove_fri, data and transcript on the GPU
+//                                                  (fri_prover.hpp:35-265)
 //   GpuDuplexChallenger<F, Perm, WIDTH, RATE>     DuplexChallenger with grind on the GPU
 //                                                  (duplex_challenger.hpp:42-285)
 //
@@ -46,6 +48,12 @@ namespace p3_merkle_tree {  // the reference's tree type (merkle_tree.hpp:45-58)
 template <typename F, typename W, size_t DIGEST_ELEMS>
 struct MerkleTree;
 }  // namespace p3_merkle_tree
+namespace p3_fri {  // the reference's FRI types (fri_params.hpp:9-24, fri_proof.hpp:25-32), for gpu_prove_fri
+template <typename FriMmcs>
+struct FriParameters;
+template <typename Challenge, typename FriMmcs, typename Witness, typename InputProof>
+struct FriProof;
+}  // namespace p3_fri
 
 namespace p3g {
 
@@ -583,5 +591,118 @@ private:
     std::array<F, WIDTH> state_;
     std::vector<F> in_, out_;
 };
+
+// ----------------------------------------------------------------- prove_fri
+namespace detail {
+template <class T, class = void>
+struct has_state : std::false_type {};
+template <class T>
+struct has_state<T, std::void_t<decltype(std::declval<T&>().state())>> : std::true_type {};
+// The GpuDuplexChallenger behind a transcript: the challenger itself, or the
+// `inner` challenger of a wrapper (as the FRI tests' transcript holds it).
+template <class Challenger>
+auto& gpu_challenger(Challenger& c) {
+    if constexpr (has_state<Challenger>::value) return c;
+    else return c.inner;
+}
+}  // namespace detail
+
+// prove_fri (fri_prover.hpp:35-265) with the reference's signature, every data
+// step and the Fiat-Shamir transcript on the GPU (p3g_fri_prove, one call):
+// BabyBear / BabyBear^4, the commit phase's flat MMCS over the context's
+// Poseidon2-16, arities 2 to 8.  The challenger is a GpuDuplexChallenger, or a
+// wrapper whose `inner` member is one, with the transcript calls of the FRI
+// tests' wrapper (fri_test.cpp:100-120); it comes back advanced exactly as the
+// reference's prove_fri leaves it.  The input openings are the input MMCS's own
+// (input_mmcs.open at each query index, on the host).  Returns the reference's
+// FriProof.
+template <typename Val, typename Challenge, typename FriMmcs, typename Challenger, typename Witness,
+          typename InputMmcs, typename InputProof>
+p3_fri::FriProof<Challenge, FriMmcs, Witness, InputProof> gpu_prove_fri(
+    const p3_fri::FriParameters<FriMmcs>& params, std::vector<std::vector<Challenge>> inputs, Challenger& challenger,
+    const std::vector<typename InputMmcs::ProverData>& input_data, const InputMmcs& input_mmcs) {
+    static_assert(sizeof(Val) == 4 && sizeof(Challenge) == 16, "FRI over BabyBear^4");
+    using Proof = p3_fri::FriProof<Challenge, FriMmcs, Witness, InputProof>;
+    if (inputs.empty()) throw std::invalid_argument("prove_fri: no input vectors");
+    auto& ch = detail::gpu_challenger(challenger);
+    p3g_fri_params fp{uint32_t(params.log_blowup), uint32_t(params.log_final_poly_len), uint32_t(params.max_log_arity),
+                      uint32_t(params.num_queries), uint32_t(params.commit_proof_of_work_bits),
+                      uint32_t(params.query_proof_of_work_bits)};
+    std::vector<uint32_t> log_h;
+    std::vector<std::unique_ptr<DeviceBuffer>> bufs;
+    std::vector<const void*> ptrs;
+    for (const auto& v : inputs) {
+        log_h.push_back(uint32_t(log2_strict(v.size())));
+        std::vector<uint32_t> w(v.size() * 4);
+        for (size_t i = 0; i < v.size(); ++i)
+            for (int k = 0; k < 4; ++k) w[4 * i + k] = uint32_t(v[i][k].value());
+        bufs.emplace_back(new DeviceBuffer(w.size() * 4));
+        bufs.back()->upload(w.data(), w.size() * 4);
+        ptrs.push_back(bufs.back()->get());
+    }
+    uint32_t nr = 0, las[32];
+    check(p3g_fri_rounds(log_h.data(), uint32_t(log_h.size()), &fp, &nr, las));
+    const size_t nq = params.num_queries, fpl = size_t(1) << params.log_final_poly_len;
+    size_t row_words = 0, path_words = 0;
+    std::vector<uint32_t> heights(nr);
+    for (uint32_t r = 0, h = log_h[0]; r < nr; h -= las[r], ++r) {
+        heights[r] = h;
+        row_words += nq * (size_t(4) << las[r]);
+        path_words += nq * (h - las[r]) * 8;
+    }
+    std::vector<uint32_t> commits(size_t(nr) * 8), final_poly(fpl * 4), rows(std::max<size_t>(row_words, 1)),
+        paths(std::max<size_t>(path_words, 1));
+    std::vector<uint64_t> wits(std::max<uint32_t>(nr, 1)), qidx(std::max<size_t>(nq, 1));
+    uint64_t qwit = 0;
+    p3g_challenger st = ch.state();
+    check(p3g_fri_prove(Context::get().handle(), ptrs.data(), log_h.data(), uint32_t(log_h.size()), &fp, &st,
+                        commits.data(), wits.data(), final_poly.data(), &qwit, qidx.data(), rows.data(), paths.data(),
+                        nullptr));
+    ch.set_state(st);
+
+    auto ext = [](const uint32_t* w) {
+        Challenge c{};
+        for (int k = 0; k < 4; ++k) c[k] = Val(w[k]);
+        return c;
+    };
+    Proof proof;
+    using Commitment = typename decltype(proof.commit_phase_commits)::value_type;
+    using Digest = typename Commitment::value_type;
+    auto digest = [](const uint32_t* w) {
+        Digest d{};
+        for (size_t k = 0; k < d.size(); ++k) d[k] = Val(w[k]);
+        return d;
+    };
+    for (uint32_t r = 0; r < nr; ++r) {
+        Commitment c;
+        c.push_back(digest(&commits[8 * r]));
+        proof.commit_phase_commits.push_back(std::move(c));
+        proof.commit_pow_witnesses.push_back(Witness(wits[r]));
+    }
+    for (size_t k = 0; k < fpl; ++k) proof.final_poly.push_back(ext(&final_poly[4 * k]));
+    proof.query_pow_witness = Witness(qwit);
+    using QP = typename decltype(proof.query_proofs)::value_type;
+    for (size_t q = 0; q < nq; ++q) {
+        QP qp;
+        input_mmcs.open(size_t(qidx[q]), input_data, qp.input_proof);
+        size_t ro = 0, po = 0, cur = size_t(qidx[q]);
+        for (uint32_t r = 0; r < nr; ++r) {
+            const size_t arity = size_t(1) << las[r], depth = heights[r] - las[r];
+            typename decltype(qp.commit_phase_openings)::value_type step;
+            step.log_arity = uint8_t(las[r]);
+            const uint32_t* row = &rows[ro + q * 4 * arity];
+            for (size_t j = 0; j < arity; ++j)
+                if (j != (cur & (arity - 1))) step.sibling_values.push_back(ext(row + 4 * j));
+            const uint32_t* path = &paths[po + q * depth * 8];
+            for (size_t l = 0; l < depth; ++l) step.opening_proof.push_back(digest(path + 8 * l));
+            qp.commit_phase_openings.push_back(std::move(step));
+            ro += nq * 4 * arity;
+            po += nq * depth * 8;
+            cur >>= las[r];
+        }
+        proof.query_proofs.push_back(std::move(qp));
+    }
+    return proof;
+}
 
 }  // namespace p3g

@@ -14,7 +14,9 @@
 //      GpuDft over the reference's NttCuda;
 //   4. gpu_fold_matrix against TwoAdicFriFolding<BB, BB4>::fold_matrix;
 //   5. GpuDuplexChallenger against DuplexChallenger: the same observations,
-//      samples, sample_bits and grind witnesses.
+//      samples, sample_bits and grind witnesses;
+//   6. gpu_prove_fri against prove_fri: the same FriProof (byte for byte in
+//      p3g_proof.hpp's format) and the same transcript afterwards.
 
 #include "baby_bear.hpp"
 #include "extension_field.hpp"
@@ -33,8 +35,10 @@
 #include "fri_params.hpp"
 #include "two_adic_fri_pcs.hpp"
 #include "duplex_challenger.hpp"
+#include "fri_prover.hpp"
 
 #include "p3g_adapters.hpp"
+#include "p3g_proof.hpp"
 
 #include <cstdio>
 #include <random>
@@ -72,6 +76,30 @@ static RowMajorMatrix<BB> rand_matrix(size_t h, size_t w, uint32_t seed) {
     for (auto& e : v) e = BB(uint32_t(rng() % BB::PRIME));
     return RowMajorMatrix<BB>(std::move(v), w);
 }
+
+// prove_fri's input MMCS for check 6: the opening records the index.
+struct IndexMmcs {
+    struct ProverData {};
+    struct OpeningProof {
+        size_t row_index = 0;
+        std::vector<BB> row_values;
+    };
+    void open(size_t index, const std::vector<ProverData>&, OpeningProof& p) const { p.row_index = index; }
+};
+template <class Inner>
+struct FriTranscript {  // the FRI tests' wrapper (fri_test.cpp:100-120)
+    Inner inner;
+    template <typename C>
+    void observe_commitment(const C& c) { inner.observe_merkle_cap(c); }
+    template <typename EF = BabyBear4>
+    EF sample_challenge() { return inner.template sample_algebra_element<EF>(); }
+    template <typename EF>
+    void observe_challenge(const EF& v) { inner.template observe_algebra_element<EF>(v); }
+    void observe_arity(size_t la) { inner.observe(BB(static_cast<uint32_t>(la))); }
+    uint64_t grind(size_t bits) { return inner.grind(bits); }
+    bool check_witness(size_t bits, uint64_t w) { return inner.check_witness(bits, w); }
+    size_t sample_bits(size_t n) { return inner.sample_bits(n); }
+};
 
 static int report(const char* what, bool ok) {
     std::printf("%s %s\n", ok ? "ok  " : "FAIL", what);
@@ -201,6 +229,30 @@ int main() {
         resumed.set_state(gpu.state());
         for (int k = 0; k < 10; ++k) ok = ok && resumed.sample() == cpu.sample();
         fails += report("DuplexChallenger with grind on the GPU", ok);
+    }
+    // 6. prove_fri with the data and the transcript on the GPU
+    {
+        using Cpu = FriTranscript<p3_challenger::DuplexChallenger<BB, Wrap, 16, 8>>;
+        using Gpu = FriTranscript<p3g::GpuDuplexChallenger<BB, Wrap, 16, 8>>;
+        Cpu cpu{p3_challenger::DuplexChallenger<BB, Wrap, 16, 8>(Wrap{pos})};
+        Gpu gpu{p3g::GpuDuplexChallenger<BB, Wrap, 16, 8>(Wrap{pos})};
+        std::mt19937 rng(13);
+        auto r = [&] { return BB(uint32_t(rng() % BB::PRIME)); };
+        std::vector<std::vector<BabyBear4>> inputs;
+        for (size_t lh : {size_t(11), size_t(9), size_t(6)}) {
+            std::vector<BabyBear4> v(size_t(1) << lh);
+            for (auto& e : v) e = BabyBear4({r(), r(), r(), r()});
+            inputs.push_back(std::move(v));
+        }
+        p3_fri::FriParameters<EFMmcs> fp{1, 1, 3, 20, 4, 10, EFMmcs(flat())};
+        std::vector<IndexMmcs::ProverData> none;
+        auto want = p3_fri::prove_fri<BB, BabyBear4, EFMmcs, Cpu, uint64_t, IndexMmcs, IndexMmcs::OpeningProof>(
+            fp, inputs, cpu, none, IndexMmcs{});
+        auto got = p3g::gpu_prove_fri<BB, BabyBear4, EFMmcs, Gpu, uint64_t, IndexMmcs, IndexMmcs::OpeningProof>(
+            fp, inputs, gpu, none, IndexMmcs{});
+        bool ok = p3g::wire::encode(want) == p3g::wire::encode(got);
+        for (int k = 0; k < 8; ++k) ok = ok && cpu.inner.sample() == gpu.inner.sample();
+        fails += report("gpu_prove_fri: the same FriProof and transcript as prove_fri", ok);
     }
     std::printf("%s\n", fails ? "MISMATCH" : "ALL OK");
     return fails ? 1 : 0;

@@ -14,6 +14,7 @@
 //   adapters_standin fold_cuda <in> <out> <log_height> <log_arity>   (host and device forms)
 //   adapters_standin dft <bb|gl> <in> <out> <log_h> <width> <kind 0-3> <shift>
 //   adapters_standin challenger <out> <seed> <n_obs> <bits>...
+//   adapters_standin prove_fri <in> <out> <challenger> <nq> <log_blowup> <log_fpl> <max_la> <cpow> <qpow> <log_h>...
 //
 // <in> holds canonical little-endian words (u32 BabyBear, u64 Goldilocks;
 // for mmcs the matrices back to back; for fold 4 beta coefficients, then
@@ -30,6 +31,7 @@
 
 #include <cstdio>
 #include <cstdlib>
+#include <cstring>
 #include <fstream>
 #include <iterator>
 #include <random>
@@ -111,6 +113,34 @@ struct Poseidon2Cuda {  // the members build_merkle_tree_cuda reads (poseidon2_c
 };
 
 }  // namespace standin
+
+namespace p3_fri {  // the reference's FRI types (fri_params.hpp, fri_proof.hpp), as the adapter declares them
+template <typename FriMmcs>
+struct FriParameters {
+    size_t log_blowup, log_final_poly_len, max_log_arity, num_queries, commit_proof_of_work_bits,
+        query_proof_of_work_bits;
+    FriMmcs mmcs;
+};
+template <typename Challenge, typename FriMmcs>
+struct CommitPhaseProofStep {
+    uint8_t log_arity = 0;
+    std::vector<Challenge> sibling_values;
+    typename FriMmcs::OpeningProof opening_proof;
+};
+template <typename Challenge, typename FriMmcs, typename InputProof>
+struct QueryProof {
+    InputProof input_proof;
+    std::vector<CommitPhaseProofStep<Challenge, FriMmcs>> commit_phase_openings;
+};
+template <typename Challenge, typename FriMmcs, typename Witness, typename InputProof>
+struct FriProof {
+    std::vector<typename FriMmcs::Commitment> commit_phase_commits;
+    std::vector<Witness> commit_pow_witnesses;
+    std::vector<QueryProof<Challenge, FriMmcs, InputProof>> query_proofs;
+    std::vector<Challenge> final_poly;
+    Witness query_pow_witness{};
+};
+}  // namespace p3_fri
 
 namespace p3_merkle_tree {  // the reference's tree type, as the adapter's declaration expects
 template <typename F, typename W, size_t DIGEST_ELEMS>
@@ -195,6 +225,83 @@ static int run_challenger(int argc, char** a) {
     for (int k = 0; k < 10; ++k)
         if (!(copy.sample() == ch.sample())) return 6;
     write_file(a[2], out);
+    return 0;
+}
+
+// gpu_prove_fri with stand-ins for the FRI MMCS (its Commitment / OpeningProof
+// types) and an input MMCS whose opening records the index.
+struct FriMmcsStandin {
+    using Digest = std::array<BabyBear, 8>;
+    using Commitment = std::vector<Digest>;
+    using OpeningProof = std::vector<Digest>;
+};
+struct IndexMmcs {
+    struct ProverData {};
+    struct OpeningProof {
+        size_t row_index = 0;
+    };
+    void open(size_t index, const std::vector<ProverData>&, OpeningProof& p) const { p.row_index = index; }
+};
+struct FriTranscript {  // the wrapper shape of fri_test.cpp:100-120
+    p3g::GpuDuplexChallenger<BabyBear, DevicePermBB, 16, 8> inner{DevicePermBB{}};
+};
+
+// prove_fri <in> <out> <challenger> <num_queries> <log_blowup> <log_final_poly_len> <max_log_arity>
+//           <commit_pow_bits> <query_pow_bits> <log_h0> [<log_h1> ...]
+static int run_prove_fri(int argc, char** a) {
+    auto in = read_file(a[2]);
+    auto chb = read_file(a[4]);
+    if (chb.size() != sizeof(p3g_challenger)) return 2;
+    p3g_challenger st;
+    std::memcpy(&st, chb.data(), sizeof st);
+    p3_fri::FriParameters<FriMmcsStandin> prm{std::strtoul(a[6], nullptr, 0), std::strtoul(a[7], nullptr, 0),
+                                              std::strtoul(a[8], nullptr, 0), std::strtoul(a[5], nullptr, 0),
+                                              std::strtoul(a[9], nullptr, 0), std::strtoul(a[10], nullptr, 0),
+                                              FriMmcsStandin{}};
+    std::vector<std::vector<BabyBear4>> inputs;
+    size_t off = 0;
+    for (int i = 11; i < argc; ++i) {
+        const size_t n = size_t(1) << std::strtoul(a[i], nullptr, 0);
+        auto words = p3g::from_words<BabyBear>(in.data() + off, 4 * n);
+        std::vector<BabyBear4> v(n);
+        for (size_t k = 0; k < n; ++k)
+            for (int e = 0; e < 4; ++e) v[k][e] = words[4 * k + e];
+        inputs.push_back(std::move(v));
+        off += 16 * n;
+    }
+    FriTranscript tr;
+    tr.inner.set_state(st);
+    auto proof = p3g::gpu_prove_fri<BabyBear, BabyBear4, FriMmcsStandin, FriTranscript, uint64_t, IndexMmcs,
+                                    IndexMmcs::OpeningProof>(prm, std::move(inputs), tr, {}, IndexMmcs{});
+    // out: rounds, roots, final polynomial, query witness, per query its index and per round the
+    // siblings and the path, then the challenger afterwards
+    std::vector<unsigned char> out;
+    auto put32 = [&](uint32_t v) { out.insert(out.end(), reinterpret_cast<unsigned char*>(&v), reinterpret_cast<unsigned char*>(&v) + 4); };
+    auto put64 = [&](uint64_t v) { out.insert(out.end(), reinterpret_cast<unsigned char*>(&v), reinterpret_cast<unsigned char*>(&v) + 8); };
+    put32(uint32_t(proof.commit_phase_commits.size()));
+    for (const auto& c : proof.commit_phase_commits)
+        for (const auto& e : c.at(0)) put32(e.value());
+    put32(uint32_t(proof.final_poly.size()));
+    for (const auto& v : proof.final_poly)
+        for (int e = 0; e < 4; ++e) put32(v[e].value());
+    put64(proof.query_pow_witness);
+    put32(uint32_t(proof.query_proofs.size()));
+    for (const auto& qp : proof.query_proofs) {
+        put64(qp.input_proof.row_index);
+        for (const auto& step : qp.commit_phase_openings) {
+            put32(step.log_arity);
+            put32(uint32_t(step.sibling_values.size()));
+            for (const auto& v : step.sibling_values)
+                for (int e = 0; e < 4; ++e) put32(v[e].value());
+            put32(uint32_t(step.opening_proof.size()));
+            for (const auto& d : step.opening_proof)
+                for (const auto& e : d) put32(e.value());
+        }
+    }
+    const p3g_challenger after = tr.inner.state();
+    const unsigned char* ab = reinterpret_cast<const unsigned char*>(&after);
+    out.insert(out.end(), ab, ab + sizeof after);
+    write_file(a[3], out);
     return 0;
 }
 
@@ -296,6 +403,7 @@ int main(int argc, char** argv) {
     try {
         set_constants();
         if (cmd == "challenger") return run_challenger(argc, argv);
+        if (cmd == "prove_fri") return run_prove_fri(argc, argv);
         if (cmd == "lde") return std::string(argv[2]) == "bb" ? run_lde<BabyBear>(argv) : run_lde<Goldilocks>(argv);
         if (cmd == "dft") {
             if (argc < 9) return 2;

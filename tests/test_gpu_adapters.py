@@ -11,6 +11,7 @@ import pytest
 
 import oracle as O
 from conftest import compile_cpp
+from test_gpu_fri import _oracle_fri, _params, reduced_openings
 
 pytestmark = pytest.mark.gpu
 
@@ -153,6 +154,62 @@ def test_fold_matrix_cuda_forms(prog, tmp_path, log_arity):
     assert rc == 0, err
     got = np.fromfile(fout, dtype=np.uint32).reshape(-1, 4)
     assert np.array_equal(got, O.fold_matrix_bb4(v, log_h, log_arity, beta))
+
+
+def test_gpu_prove_fri_adapter(prog, tmp_path, gpu_ctx, golden):
+    """p3g::gpu_prove_fri with the reference's prove_fri signature (stand-in
+    proof types, a transcript wrapper holding a GpuDuplexChallenger) builds the
+    reference's proofs -- roots, final polynomial, query witness, every query's
+    siblings and path -- and leaves the challenger where the oracle's does."""
+    for case in golden["pcs_open"]:
+        tr, qs = reduced_openings(gpu_ctx, case)
+        heights = sorted(qs, reverse=True)
+        vectors = [qs[h].download(np.uint32, (1 << h, 4)) for h in heights]
+        before = tr.copy()
+        st = np.zeros(16 + 8 + 8 + 2, np.uint32)
+        st[:16] = tr.state
+        st[16:16 + len(tr.inp)] = tr.inp
+        st[24:24 + len(tr.out)] = tr.out
+        st[32], st[33] = len(tr.inp), len(tr.out)
+        fch = tmp_path / "ch.bin"
+        st.tofile(fch)
+        prm = _params(case)
+        rc, err, fout = _run(prog, tmp_path, "prove_fri", None,
+                             [str(fch), prm["num_queries"], prm["log_blowup"], prm["log_final_poly_len"],
+                              prm["max_log_arity"], prm["commit_proof_of_work_bits"],
+                              prm["query_proof_of_work_bits"]] + heights, np.concatenate(vectors).reshape(-1))
+        assert rc == 0, err
+        raw = np.fromfile(fout, dtype=np.uint8)
+        pos = [0]
+
+        def take(n, dt=np.uint32):
+            v = raw[pos[0]:pos[0] + n * np.dtype(dt).itemsize].view(dt)
+            pos[0] += n * np.dtype(dt).itemsize
+            return v
+
+        nr = int(take(1)[0])
+        assert take(8 * nr).reshape(nr, 8).tolist() == case["commits"]
+        nf = int(take(1)[0])
+        assert take(4 * nf).reshape(nf, 4).tolist() == case["final_poly"]
+        assert int(take(1, np.uint64)[0]) == case["fri"]["query_pow_witness"]
+        nq = int(take(1)[0])
+        _, _, _, idx, openings = _oracle_fri(case, before, vectors)
+        assert openings == case["query_openings"]
+        for q in range(nq):
+            assert int(take(1, np.uint64)[0]) == idx[q]
+            for step in case["query_openings"][q]:
+                assert int(take(1)[0]) == step["log_arity"]
+                ns = int(take(1)[0])
+                assert take(4 * ns).reshape(ns, 4).tolist() == step["siblings"]
+                npth = int(take(1)[0])
+                assert take(8 * npth).reshape(npth, 8).tolist() == step["path"]
+        after = take(34)
+        assert after[:16].tolist() == [int(x) for x in before.state]
+        assert after[32] == len(before.inp) and after[16:16 + after[32]].tolist() == before.inp
+        assert after[33] == len(before.out) and after[24:24 + after[33]].tolist() == before.out
+        assert pos[0] == raw.size
+        for b in qs.values():
+            b.free()
 
 
 def test_gpu_duplex_challenger_grind(prog, tmp_path, golden):

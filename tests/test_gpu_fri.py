@@ -134,29 +134,40 @@ def _params(case):
                 commit_proof_of_work_bits=fri["commit_pow_bits"], query_proof_of_work_bits=fri["query_pow_bits"])
 
 
+def reduced_openings(gpu_ctx, case):
+    """TwoAdicFriPcs::open up to prove_fri for a golden case, on the GPU: the
+    transcript (oracle) after zeta, alpha and the opened values, and the
+    bit-reversed reduced openings per LDE height (device buffers)."""
+    tr, zeta, alpha = open_transcript(case)
+    shapes = [tuple(int(v) for v in s.split("x")) for s in case["shapes"]]
+    qs, ap, keep = {}, 0, []
+    for i, (lh, w) in enumerate(shapes):
+        t = O.bb_random_matrix(1 << lh, w, case["seed"] + i)
+        d_t = gpu_ctx.to_device(t)
+        log_n = lh + case["log_blowup"]
+        d_lde = gpu_ctx.alloc((1 << log_n) * w * 4)
+        gpu_ctx.coset_lde_device(P.BABYBEAR, d_t.ptr, lh, w, case["log_blowup"], case["shift"], False, d_lde.ptr)
+        ov = gpu_ctx.pcs_open_values_device(d_lde.ptr, log_n, w, False, case["shift"], [zeta])
+        for v in ov.reshape(-1, 4):
+            tr.observe_ext(v)
+        if log_n not in qs:
+            qs[log_n] = gpu_ctx.to_device(np.zeros((1 << log_n, 4), np.uint32))
+        gpu_ctx.pcs_reduce_device(d_lde.ptr, log_n, w, False, case["shift"], [zeta], ov, alpha, ap, True,
+                                  qs[log_n].ptr)
+        ap += w
+        keep += [d_t, d_lde]
+    for b in keep:
+        b.free()
+    return tr, qs
+
+
 def test_fri_prove_on_device_vs_reference(gpu_ctx, golden):
     """p3g_fri_prove -- every round, the transcript and the query openings on
     the device -- against the reference's proofs: roots, final polynomial,
     query proof-of-work witness and every query's siblings and Merkle path."""
     for case in golden["pcs_open"]:
-        tr, zeta, alpha = open_transcript(case)
-        shapes = [tuple(int(v) for v in s.split("x")) for s in case["shapes"]]
-        qs, ap, keep = {}, 0, []
-        for i, (lh, w) in enumerate(shapes):
-            t = O.bb_random_matrix(1 << lh, w, case["seed"] + i)
-            d_t = gpu_ctx.to_device(t)
-            log_n = lh + case["log_blowup"]
-            d_lde = gpu_ctx.alloc((1 << log_n) * w * 4)
-            gpu_ctx.coset_lde_device(P.BABYBEAR, d_t.ptr, lh, w, case["log_blowup"], case["shift"], False, d_lde.ptr)
-            ov = gpu_ctx.pcs_open_values_device(d_lde.ptr, log_n, w, False, case["shift"], [zeta])
-            for v in ov.reshape(-1, 4):
-                tr.observe_ext(v)
-            if log_n not in qs:
-                qs[log_n] = gpu_ctx.to_device(np.zeros((1 << log_n, 4), np.uint32))
-            gpu_ctx.pcs_reduce_device(d_lde.ptr, log_n, w, False, case["shift"], [zeta], ov, alpha, ap, True,
-                                      qs[log_n].ptr)
-            ap += w
-            keep += [d_t, d_lde]
+        tr, qs = reduced_openings(gpu_ctx, case)
+        keep = []
         heights = sorted(qs, reverse=True)
         before = tr.copy()
         res = gpu_ctx.fri_prove_device([(qs[h].ptr, h) for h in heights], _params(case), tr.state, tr.inp, tr.out)
