@@ -516,6 +516,30 @@ def run_ours(args):
         tree.free(sptr)
         torch.cuda.synchronize(dev)
 
+        # ---- FRI fold (p3g_fold_matrix_bb4): the config-3 quotient size (2^19
+        # BabyBear^4, L2-resident) and a 2^25-value vector (512 MiB in, larger
+        # than L2) for the HBM roofline; CUDA events on the stream
+        fold = {}
+        for log_f in (19, 25):
+            d_in = ctx.to_device(rng.integers(0, BB_P, size=(1 << log_f, 4), dtype=np.uint32))
+            d_out = ctx.alloc((1 << log_f) * 16 // 2, sptr)
+            beta_f = rng.integers(0, BB_P, size=4, dtype=np.uint32)
+            for la in (1, 2, 3):
+                ctx.fold_matrix_bb4_device(d_in.ptr, log_f, la, beta_f, d_out.ptr, sptr)
+                torch.cuda.synchronize(dev)
+                e0.record(stream)
+                for _ in range(reps):
+                    ctx.fold_matrix_bb4_device(d_in.ptr, log_f, la, beta_f, d_out.ptr, sptr)
+                e1.record(stream)
+                torch.cuda.synchronize(dev)
+                ms = e0.elapsed_time(e1) / reps
+                nbytes = 16 * ((1 << log_f) + ((1 << log_f) >> la))
+                fold[f"2^{log_f}_arity{1 << la}"] = {"ms": ms, "algorithmic_bytes": nbytes,
+                                                     "gbs": nbytes / (ms / 1e3) / 1e9}
+            d_out.free(sptr)
+            d_in.free()
+        torch.cuda.synchronize(dev)
+
     # ---- permutation ceiling: the same Poseidon2-16 on 2^22 register-resident
     # states (p3g_poseidon2_permute), no sponge or tree around it
     n_states = 1 << 22
@@ -557,6 +581,9 @@ def run_ours(args):
                                       f"{len(fri_res['log_arities'])} rounds of arity 2, final polynomial of 1, "
                                       "16-bit query proof of work, 100 queries with openings; transcript on the device",
                           "ms": statistics.median(fri_ms), "samples_ms": [round(x, 3) for x in fri_ms]},
+            "fold": {"workload": "fold_matrix over BabyBear^4 (p3g_fold_matrix_bb4), arities 2/4/8: 2^19 values "
+                                 "(config 3's quotient, L2-resident) and 2^25 values (512 MiB, HBM)",
+                     **fold, "hbm_frac_2^25_arity2": fold["2^25_arity2"]["gbs"] / peaks()[0]},
             "pow_grind": {"workload": f"DuplexChallenger::grind, {grind_bits} bits, 4 challenger states "
                                       "(0-3 pending inputs), Poseidon2-16",
                           "candidates": grind_cand, "ms": grind_s * 1e3,

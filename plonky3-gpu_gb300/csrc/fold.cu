@@ -8,9 +8,11 @@
 // Arity 2 uses the closed form (e0 + e1)/2 + beta (e0 - e1) / (2x), which is
 // the same field element as the reference's Lagrange sum (and also covers its
 // beta == t_j early return).  x^-1 comes from the context's root table, not a
-// per-thread exponentiation.  Arity 4 and 8 evaluate the reference's formula
-// term for term, L_i = N * a^-1 / ((beta - t_i) x^(a-1) w^-(i)) with
-// N = prod_j (beta - t_j), including its early return when beta equals a node.
+// per-thread exponentiation.  Arity 4 and 8 evaluate the reference's weights
+// L_i = N * a^-1 / ((beta - t_i) x^(a-1) w^-(i)), N = prod_j (beta - t_j),
+// as the same field elements without an inversion: N / (beta - t_i) is the
+// product of the other factors, and 1 / (x^(a-1) w^-i) = x^-(a-1) w^i.  Its
+// early return when beta equals a node is kept.
 #include "internal.hpp"
 #include "ntt.cuh"
 
@@ -61,35 +63,38 @@ __global__ void k_fold_general(const bb4* __restrict__ in, bb4* __restrict__ out
     for (int j = 0; j < A; ++j) ev[j] = in[i * A + j];
     const bool beta_base = beta.c[1] == 0 && beta.c[2] == 0 && beta.c[3] == 0;
     if (beta_base) {
+#pragma unroll
         for (int j = 0; j < A; ++j)
             if (beta.c[0] == t[j]) {
                 out[i] = ev[j];
                 return;
             }
     }
-    bb4 full = {{1, 0, 0, 0}};
+    // L_j = N a^-1 / ((beta - t_j) x^(a-1) w^-j) with N = prod_k (beta - t_k):
+    // N / (beta - t_j) is the product of the other factors, so
+    // L_j = a^-1 x^-(a-1) w^j prod_{k != j} (beta - t_k) -- the same field
+    // element with no inversion (prefix products, then a running suffix).
     bb4 bmt[A];
 #pragma unroll
     for (int j = 0; j < A; ++j) {
         bmt[j] = beta;
         bmt[j].c[0] = bb::sub(beta.c[0], t[j]);
-        full = bb4_mul(full, bmt[j]);
     }
-    // x^(a-1)
-    uint32_t xp_m = bb::mmul(x, bb::R2);  // Montgomery x
-    uint32_t xam1_m = bb::R1;
+    bb4 pre[A];
+    pre[0] = {{1, 0, 0, 0}};
 #pragma unroll
-    for (int k = 0; k < A - 1; ++k) xam1_m = bb::mmul(xam1_m, xp_m);
-    const bb4 num = bb4_scale_m(full, arity_inv_c);
-    bb4 res = {{0, 0, 0, 0}};
-    uint32_t winv_i = bb::R1;  // Montgomery
+    for (int j = 1; j < A; ++j) pre[j] = bb4_mul(pre[j - 1], bmt[j - 1]);
+    const uint32_t xinv_m = roots.omega_inv(log_height, bitrev_dev(unsigned(i), log_folded));
+    uint32_t s_m = arity_inv_c;  // a^-1 x^-(a-1) w^(A-1), Montgomery
 #pragma unroll
-    for (int j = 0; j < A; ++j) {
-        const uint32_t bd_m = bb::mmul(xam1_m, winv_i);
-        const bb4 denom = bb4_scale_m(bmt[j], bd_m);
-        const bb4 L = bb4_mul(num, bb4_inv(denom));
+    for (int k = 0; k < A - 1; ++k) s_m = bb::mmul(bb::mmul(s_m, xinv_m), w_c);
+    bb4 suf = {{1, 0, 0, 0}}, res = {{0, 0, 0, 0}};
+#pragma unroll
+    for (int j = A - 1; j >= 0; --j) {
+        const bb4 L = bb4_scale_m(bb4_mul(pre[j], suf), s_m);
         res = bb4_add(res, bb4_mul(ev[j], L));
-        winv_i = bb::mmul(winv_i, winv_c);
+        suf = bb4_mul(suf, bmt[j]);
+        s_m = bb::mmul(s_m, winv_c);
     }
     out[i] = res;
 }
