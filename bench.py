@@ -27,6 +27,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -82,7 +83,8 @@ class ClockSampler:
     def __init__(self, device: int):
         self.device = device
         self.proc = None
-        self.path = os.path.join(REPO, "gpurun_out", f"clocks_{device}.csv")
+        # the raw samples (the JSON line carries their summary); P3G_CLOCKS_DIR keeps them
+        self.path = os.path.join(os.environ.get("P3G_CLOCKS_DIR", tempfile.gettempdir()), f"clocks_{device}.csv")
 
     def __enter__(self):
         os.makedirs(os.path.dirname(self.path), exist_ok=True)
