@@ -91,6 +91,10 @@ int p3g_last_error(char* buf, size_t len) {
 
 // Frees the context's device tables and pool (null members are skipped).
 static void free_ctx_resources(p3g_ctx* ctx) {
+    for (cudaEvent_t e : ctx->events) cudaEventDestroy(e);
+    ctx->events.clear();
+    if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
+    ctx->copy_stream = nullptr;
     cudaFree(ctx->bb_lo);
     cudaFree(ctx->bb_hi);
     cudaFree(ctx->gl_lo);
@@ -502,18 +506,20 @@ int p3g_commit_traces_host(p3g_ctx* ctx, int field, const p3g_trace* traces, siz
     }
     auto t = std::make_unique<p3g_tree>();
     t->field = field;
-    cudaStream_t cs = nullptr;
-    cudaEvent_t start = nullptr;
-    std::vector<cudaEvent_t> evs;
+    // The context's copy stream and events, created once and reused: event 0
+    // orders the copies after the caller's work, event 1 + k marks chunk k's copy.
+    if (!ctx->copy_stream) P3G_CUDA(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
+    while (ctx->events.size() < chunks.size() + 1) {
+        cudaEvent_t e;
+        P3G_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        ctx->events.push_back(e);
+    }
+    cudaStream_t cs = ctx->copy_stream;
+    cudaEvent_t start = ctx->events[0];
     // Device copies of the chunks, allocated on `st` before anything else is
     // queued (the pool then reuses them call after call on the same stream),
     // filled on the copy stream, handed back on `st` after each chunk's LDE.
     std::vector<void*> staged_in(chunks.size(), nullptr);
-    auto cleanup = [&] {
-        for (cudaEvent_t e : evs) cudaEventDestroy(e);
-        if (start) cudaEventDestroy(start);
-        if (cs) cudaStreamDestroy(cs);
-    };
     try {
         for (const Chunk& c : chunks) {  // the tree's leaf matrices: every chunk's LDE, in order
             const uint64_t H = uint64_t(1) << (traces[c.trace].log_h + traces[c.trace].log_blowup);
@@ -525,8 +531,6 @@ int p3g_commit_traces_host(p3g_ctx* ctx, int field, const p3g_trace* traces, siz
         for (size_t k = 0; k < chunks.size(); ++k)
             if (chunks[k].cw > 0)
                 staged_in[k] = ctx->alloc(esz * (uint64_t(1) << traces[chunks[k].trace].log_h) * chunks[k].cw, st);
-        P3G_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
-        P3G_CUDA(cudaEventCreateWithFlags(&start, cudaEventDisableTiming));
         P3G_CUDA(cudaEventRecord(start, st));
         P3G_CUDA(cudaStreamWaitEvent(cs, start, 0));
         for (size_t k = 0; k < chunks.size(); ++k) {
@@ -538,9 +542,7 @@ int p3g_commit_traces_host(p3g_ctx* ctx, int field, const p3g_trace* traces, siz
                 void* dev = staged_in[k];
                 P3G_CUDA(cudaMemcpy2DAsync(dev, esz * c.cw, static_cast<const char*>(tr.d_trace) + esz * c.c0,
                                            esz * tr.width, esz * c.cw, h, cudaMemcpyHostToDevice, cs));
-                cudaEvent_t ev;
-                P3G_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
-                evs.push_back(ev);
+                cudaEvent_t ev = ctx->events[1 + k];
                 P3G_CUDA(cudaEventRecord(ev, cs));
                 // compute stream: the chunk's LDE as soon as its copy lands
                 P3G_CUDA(cudaStreamWaitEvent(st, ev, 0));
@@ -559,14 +561,12 @@ int p3g_commit_traces_host(p3g_ctx* ctx, int field, const p3g_trace* traces, siz
         p3g::tree_finish(ctx, t.get(), st);
         copy_cap(t.get(), h_cap_out, st);
     } catch (...) {
-        if (cs) cudaStreamSynchronize(cs);
+        cudaStreamSynchronize(cs);
         for (void* p : staged_in)
             if (p) ctx->release(p, st);
         p3g::tree_release(ctx, t.get(), st);
-        cleanup();
         throw;
     }
-    cleanup();
     *tree_out = t.release();
     API_END
 }

@@ -101,6 +101,11 @@ struct p3g_ctx {
     p3g::P2BB16 p2bb{};
     p3g::P2GL8 p2gl{};
 
+    // host-trace commits: a copy stream and events kept across calls (created on
+    // first use; the context is used by one host thread at a time)
+    cudaStream_t copy_stream = nullptr;
+    std::vector<cudaEvent_t> events;
+
     p3g::RootTab<p3g::FBB> bb_roots() const { return {bb_lo, bb_hi}; }
     p3g::RootTab<p3g::FGL> gl_roots() const { return {gl_lo, gl_hi}; }
     void* alloc(size_t bytes, cudaStream_t st);
