@@ -73,6 +73,12 @@ P3G_API int p3g_ctx_create(int device, p3g_ctx **out);
 P3G_API int p3g_ctx_destroy(p3g_ctx *ctx);
 P3G_API int p3g_stream_synchronize(p3g_ctx *ctx, void *stream);
 
+/* The context's device memory pool: bytes the pool holds from the driver
+ * (reserved) and bytes handed out (used), now and at their peaks.  Any output
+ * may be NULL. */
+P3G_API int p3g_ctx_memory(p3g_ctx *ctx, uint64_t *reserved, uint64_t *used, uint64_t *reserved_high,
+                           uint64_t *used_high);
+
 /* Stream-ordered allocations from the context pool (what the library itself
  * uses for scratch and outputs), plus copies, so that callers without a CUDA
  * runtime binding can drive the library. */

@@ -185,6 +185,26 @@ int p3g_stream_synchronize(p3g_ctx* ctx, void* stream) {
     API_END
 }
 
+int p3g_ctx_memory(p3g_ctx* ctx, uint64_t* reserved, uint64_t* used, uint64_t* reserved_high, uint64_t* used_high) {
+    API_BEGIN
+    P3G_REQUIRE(ctx, "null context");
+    DeviceGuard g(ctx->device);
+    const struct {
+        uint64_t* out;
+        cudaMemPoolAttr attr;
+    } q[] = {{reserved, cudaMemPoolAttrReservedMemCurrent},
+             {used, cudaMemPoolAttrUsedMemCurrent},
+             {reserved_high, cudaMemPoolAttrReservedMemHigh},
+             {used_high, cudaMemPoolAttrUsedMemHigh}};
+    for (const auto& e : q)
+        if (e.out) {
+            unsigned long long v = 0;  // the attribute is a cuuint64_t (64-bit unsigned)
+            P3G_CUDA(cudaMemPoolGetAttribute(ctx->pool, e.attr, &v));
+            *e.out = uint64_t(v);
+        }
+    API_END
+}
+
 int p3g_malloc(p3g_ctx* ctx, size_t bytes, void** d_ptr, void* stream) {
     API_BEGIN
     P3G_REQUIRE(ctx && d_ptr, "malloc: null argument");

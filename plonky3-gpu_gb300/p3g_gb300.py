@@ -29,7 +29,7 @@ EXPORTS = [
     "p3g_coset_lde_bb_noalloc", "p3g_plan_commit", "p3g_plan_launch", "p3g_plan_info",
     "p3g_plan_destroy", "p3g_server_create", "p3g_server_submit", "p3g_server_poll",
     "p3g_server_pending", "p3g_server_open", "p3g_server_release", "p3g_server_destroy",
-    "p3g_pcs_open_values", "p3g_pcs_reduce", "p3g_bb4_axpy", "p3g_grind", "p3g_fri_rounds", "p3g_fri_prove",
+    "p3g_pcs_open_values", "p3g_pcs_reduce", "p3g_bb4_axpy", "p3g_grind", "p3g_fri_rounds", "p3g_fri_prove", "p3g_ctx_memory",
 ]
 
 
@@ -137,6 +137,7 @@ def load(path: str | None = None):
     L.p3g_bb4_axpy.argtypes = [vp, vp, vp, u64, vp, vp]
     L.p3g_grind.argtypes = [vp, C.c_int, vp, vp, u32, u32, u64, vp, vp]
     L.p3g_fri_rounds.argtypes = [vp, u32, vp, vp, vp]
+    L.p3g_ctx_memory.argtypes = [vp, vp, vp, vp, vp]
     L.p3g_fri_prove.argtypes = [vp, vp, vp, u32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]
     L.p3g_pcs_reduce.argtypes = [vp, vp, u32, u32, i32, u32, vp, u32, vp, vp, u64, i32, vp, vp]
     for name in EXPORTS:
@@ -526,6 +527,13 @@ class Context:
         """y += a * x for n BabyBear^4 values on the device."""
         aa = np.ascontiguousarray(a, dtype=np.uint32).reshape(4)
         check(load().p3g_bb4_axpy(self.handle, d_y, d_x, n, _np_ptr(aa), stream))
+
+    # -- memory
+    def memory(self) -> dict:
+        """The context pool's reserved and used bytes, current and peak."""
+        v = [C.c_uint64() for _ in range(4)]
+        check(load().p3g_ctx_memory(self.handle, *[C.byref(x) for x in v]))
+        return dict(zip(("reserved", "used", "reserved_high", "used_high"), (x.value for x in v)))
 
     # -- proof of work
     def grind(self, field: int, sponge_state, pending, bits: int, max_witness: int = 0, stream=None) -> int:

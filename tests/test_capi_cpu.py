@@ -105,3 +105,7 @@ def test_fri_rounds_follow_compute_log_arity_for_round(heights, max_la, log_fpl)
 ])
 def test_fri_rounds_rejects_bad_arguments(heights, kw, status):
     assert _fri_rounds(heights, **kw)[0] == status
+
+
+def test_pool_statistics_reject_null_context():
+    assert P.load().p3g_ctx_memory(None, None, None, None, None) == 1
