@@ -7,7 +7,8 @@
 // TwoAdicFriFolding unchanged.  Run on a machine with a GPU it prints one
 // line per check and exits non-zero on any mismatch:
 //   1. TwoAdicFriPcs<BB, BB4, GpuDft<Radix2Dit>, GpuInputMmcs<flat MMCS>, ...>::commit
-//      against the stock Pcs (same commitment);
+//      against the stock Pcs (same commitment), and its open with the FRI MMCS
+//      ExtensionMmcs<..., GpuInputMmcs<...>> (same opened values and proof);
 //   2. GpuMerkleTreeMmcs<mixed-height MMCS>::commit against the stock one (all
 //      digest layers), then the stock open_batch / verify_batch on the GPU tree;
 //   3. GpuDft's dft / idft / coset_dft / coset_idft against Radix2Dit's, and
@@ -136,6 +137,26 @@ int main() {
         auto [c_cpu, pd_cpu] = cpu.commit(evals(cpu));
         auto [c_gpu, pd_gpu] = gpu.commit(evals(gpu));
         fails += report("TwoAdicFriPcs::commit with GpuDft + GpuInputMmcs", c_cpu == c_gpu);
+
+        // the reference's own open / prove_fri with every FRI round committed on the GPU
+        // (ExtensionMmcs over GpuInputMmcs as the FRI MMCS)
+        using GpuEF = p3_merkle::ExtensionMmcs<BB, BabyBear4, p3g::GpuInputMmcs<Flat>>;
+        using GpuFri = p3_fri::TwoAdicFriPcs<BB, BabyBear4, p3g::GpuDft<p3_dft::Radix2Dit<BB>>,
+                                             p3g::GpuInputMmcs<Flat>, GpuEF>;
+        p3_fri::FriParameters<GpuEF> fri_c{1, 0, 1, 10, 0, 8, GpuEF(p3g::GpuInputMmcs<Flat>(flat()))};
+        GpuFri gpu_fri(p3g::GpuDft<p3_dft::Radix2Dit<BB>>(), p3g::GpuInputMmcs<Flat>(flat()), std::move(fri_c));
+        auto [c_fri, pd_fri] = gpu_fri.commit(evals(gpu_fri));
+        using Tr = FriTranscript<p3_challenger::DuplexChallenger<BB, Wrap, 16, 8>>;
+        auto open = [&](auto& pcs, const auto& commit, const auto& pd) {
+            Tr t{p3_challenger::DuplexChallenger<BB, Wrap, 16, 8>(Wrap{pos})};
+            t.observe_commitment(commit);
+            const BabyBear4 z = t.template sample_challenge<BabyBear4>();
+            std::vector<std::vector<BabyBear4>> pts(shapes.size(), std::vector<BabyBear4>{z});
+            auto [ov, proof] = pcs.open({{&pd, pts}}, t);
+            return std::make_pair(p3g::wire::encode(ov), p3g::wire::encode(proof));
+        };
+        fails += report("TwoAdicFriPcs::open with GPU-committed FRI rounds: the same opened values and proof",
+                        open(cpu, c_cpu, pd_cpu) == open(gpu_fri, c_fri, pd_fri));
     }
 
     // 2. mixed-height MMCS commit, then the stock opening and verification
