@@ -111,7 +111,9 @@ P3G_API int p3g_poseidon2_permute(p3g_ctx *ctx, int field, void *d_states, size_
  *   and, if bitrev_out, reverse_matrix_index_bits(out)      (util.hpp:33-45)
  * in:  (1 << log_h) x width, natural order;  out: (1 << (log_h + log_blowup)) x width.
  * Replaces NttCuda<F>::coset_lde_batch (ntt_cuda.hpp:369-378, 607-649).
- * in and out must not overlap.  Supports log_h <= 21. */
+ * in and out must not overlap.  Supports log_h <= 26 (P3G_EUNSUPPORTED above);
+ * heights above 2^21 take one more pass over the data and scratch of the
+ * trace's size per call. */
 P3G_API int p3g_coset_lde(p3g_ctx *ctx, int field, const void *d_in, uint32_t log_h, uint32_t width,
                   uint32_t log_blowup, uint64_t shift, int bitrev_out, void *d_out, void *stream);
 
@@ -123,7 +125,7 @@ P3G_API int p3g_coset_lde(p3g_ctx *ctx, int field, const void *d_in, uint32_t lo
  * and, if bitrev_out, reverse_matrix_index_bits of the result.  Replaces
  * NttCuda's dft_batch / idft_batch / coset_dft_batch / coset_idft_batch
  * (ntt_cuda.hpp:310-356).  in, out: (1 << log_h) x width, natural order
- * unless bitrev_out; in and out must not overlap.  Supports log_h <= 21. */
+ * unless bitrev_out; in and out must not overlap.  Supports log_h <= 26. */
 enum p3g_dft_kind {
     P3G_DFT = 0,
     P3G_IDFT = 1,

@@ -498,7 +498,7 @@ int p3g_commit_traces_host(p3g_ctx* ctx, int field, const p3g_trace* traces, siz
         P3G_REQUIRE(tr.width == 0 || tr.d_trace, "commit_traces_host: null trace");
         P3G_REQUIRE(tr.shift < (field == P3G_BABYBEAR ? uint64_t(p3g::bb::P) : p3g::gl::P),
                     "commit_traces_host: shift must be canonical");
-        P3G_REQUIRE(tr.log_h <= 21, "commit_traces_host: log_h > 21 is not supported");
+        if (tr.log_h > 26) throw p3g::Error(P3G_EUNSUPPORTED, "commit_traces_host: log_h > 26 is not supported");
     }
     // Column chunks.  512-byte chunk rows keep the strided copies at the
     // contiguous copy's bandwidth (narrower rows lose 15% at 256 bytes, half

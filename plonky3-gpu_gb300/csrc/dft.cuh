@@ -22,6 +22,8 @@
 //   pass B: size-N2 DIF over each contiguous N2-row block, outputs scaled by
 //           alpha^(N1 m2), rows in bit-reversed order (in place) or
 //           scattered to natural order.
+// 2^21 < h <= 2^26: those two passes as the inner transforms of one more
+// split, plus an outer pass (big_run below).
 #pragma once
 #include "lde.cuh"
 
@@ -294,6 +296,146 @@ static void dft_run(const typename F::T* in, int log_h, int w, uint64_t sigma, u
     for (void* b : bufs) ctx->release(b, st);
 }
 
+// ------------------------------------------------------------ h > 2^21
+// Above the two-pass limit the transform splits once more, h = A * B with
+// A = 2^LDE_PASS_MAX and B = h / A <= 32 (h <= 2^LDE_BIG_MAX).  With input row
+// k = B*k1 + k2 and output m = m1 + A*m2 (omega_h^(A*B) = 1):
+//   out[m] = alpha^m * sum_k2 omega_B^(+-k2 m2) * (sigma * omega_h^(+-m1))^k2
+//            * Z_k2[m1],
+//   Z_k2[m1] = sum_k1 beta0 * (sigma^B)^k1 * x[B*k1 + k2] * omega_A^(+-k1 m1),
+// so the inner transforms are one dft_run of size A over the A x (B*w) view of
+// the matrix (row k1 holds rows B*k1 .. B*k1 + B - 1), and the outer step is,
+// per inner output row and column, a twist and a size-B DIF in registers
+// (position p holds m2 = bitrev_B(p)).
+//   Bit-reversed output: the inner transforms write `out` in bit-reversed row
+//   order, row j holding m1 = bitrev_A(j); output position B*j + p then holds
+//   m = m1 + A*bitrev_B(p) = bitrev_h(B*j + p), so the outer step runs in
+//   place on the B*w elements of row j.
+//   Natural output: the inner output goes to a scratch matrix in natural
+//   order (row j = m1) and the outer step writes output m to out row
+//   row0 + m * rs (rs > 1 interleaves several transforms, as the LDE's cosets).
+template <class F, int Q, int INV>
+__global__ void __launch_bounds__(256)
+k_big_outer(const typename F::T* z, typename F::T* out, int64_t w, int log_a, int log_h,
+            typename F::T sigma_c, int inplace, int64_t row0, int64_t rs, const typename F::T* __restrict__ a1,
+            const typename F::T* __restrict__ aB, RootTab<F> roots) {
+    using T = typename F::T;
+    constexpr int B = 1 << Q;
+    const int64_t A = int64_t(1) << log_a;
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= A * w) return;
+    const int64_t j = i / w, c = i - j * w;
+    const uint64_t m1 = inplace ? bitrev_dev(unsigned(j), log_a) : uint64_t(j);
+    const T* zp = z + j * B * w + c;
+    T v[B];
+    const T f = F::cmul(INV ? roots.omega_inv(log_h, m1) : roots.omega(log_h, m1), sigma_c);
+    T cur = f;
+    v[0] = zp[0];
+#pragma unroll
+    for (int k2 = 1; k2 < B; ++k2) {
+        v[k2] = F::mulc(zp[k2 * w], cur);
+        if (k2 + 1 < B) cur = F::cmul(cur, f);
+    }
+    reg_dif<F, Q, INV>(v);
+#pragma unroll
+    for (int p = 0; p < B; ++p) {
+        const int m2 = int(bitrev_ct(unsigned(p), Q));
+        T y = v[p];
+        if (a1) y = F::mulc(y, F::cmul(a1[m1], aB[m2]));
+        if (inplace)
+            out[(j * B + p) * w + c] = y;
+        else
+            out[(row0 + int64_t(m1 + uint64_t(A) * m2) * rs) * w + c] = y;
+    }
+}
+
+template <class F, int Q, int INV>
+static void launch_big_outer(const typename F::T* z, typename F::T* out, int64_t w, int log_a, int log_h,
+                             typename F::T sigma_c, int inplace, int64_t row0, int64_t rs, const typename F::T* a1,
+                             const typename F::T* aB, RootTab<F> roots, cudaStream_t st) {
+    const int64_t n = (int64_t(1) << log_a) * w;
+    k_big_outer<F, Q, INV><<<unsigned(ceil_div(n, 256)), 256, 0, st>>>(z, out, w, log_a, log_h, sigma_c, inplace,
+                                                                      row0, rs, a1, aB, roots);
+    P3G_LAUNCHED();
+    P3G_CUDA(cudaGetLastError());
+}
+
+// dft_run's transform for LDE_PASS_MAX < log_h <= LDE_BIG_MAX; natural-order
+// output goes to rows row0 + m * rs of `out` (bit-reversed output: row0 = 0,
+// rs = 1).  in and out must not overlap.
+template <class F, int INV>
+static void big_run(const typename F::T* in, int log_h, int w, uint64_t sigma, uint64_t beta0, uint64_t alpha,
+                    int bitrev_out, typename F::T* out, int64_t row0, int64_t rs, cudaStream_t st, RootTab<F> roots,
+                    const typename F::TW* dft_tw, p3g_ctx* ctx) {
+    using T = typename F::T;
+    const int la = LDE_PASS_MAX, q = log_h - la;
+    const int64_t A = int64_t(1) << la, B = int64_t(1) << q, h = int64_t(1) << log_h;
+    P3G_REQUIRE(w <= (1 << 17), "dft: width above 2^17 at log_h > 21");  // keeps A * w / 256 CTAs below 2^31
+    std::vector<void*> bufs;
+    auto take = [&](size_t bytes) {
+        bufs.push_back(ctx->alloc(bytes, st));
+        return bufs.back();
+    };
+    try {
+        T* z = bitrev_out ? out : static_cast<T*>(take(sizeof(T) * size_t(h) * size_t(w)));
+        dft_run<F, INV>(in, la, int(w * B), F::h_pow(sigma, uint64_t(B)), beta0, 1, bitrev_out, z, st, roots, dft_tw,
+                        ctx);
+        T* a1 = nullptr;
+        T* aB = nullptr;
+        if (alpha != 1) {
+            a1 = static_cast<T*>(take(sizeof(T) * size_t(A)));
+            aB = static_cast<T*>(take(sizeof(T) * size_t(B)));
+            pow_table<F>(a1, alpha, 1, int(A), st);
+            pow_table<F>(aB, F::h_pow(alpha, uint64_t(A)), 1, int(B), st);
+        }
+        const T sc = F::to_const(sigma);
+        switch (q) {
+#define C_(Q) case Q: launch_big_outer<F, Q, INV>(z, out, w, la, log_h, sc, bitrev_out, row0, rs, a1, aB, roots, st); break;
+            C_(1) C_(2) C_(3) C_(4) C_(5)
+#undef C_
+            default: throw Error(P3G_EUNSUPPORTED, "dft: outer split size");
+        }
+    } catch (...) {
+        for (void* b : bufs) ctx->release(b, st);
+        throw;
+    }
+    for (void* b : bufs) ctx->release(b, st);
+}
+
+// The coset LDE above the three-pass limit (LDE_PASS_MAX < log_h <=
+// LDE_BIG_MAX, arguments validated by lde_impl): the coefficients
+// (1/h) IDFT_h(e) into a scratch matrix, then per coset t the size-h
+// transform with sigma = g_t = shift * omega_H^(bitrev_b(t)):
+//   bit-reversed LDE: block t (rows t*h .. t*h + h - 1) in bit-reversed order,
+//   which is where the three-pass LDE puts coset t;
+//   natural LDE: coset t's output m is LDE row bitrev_b(t) + 2^b * m.
+template <class F>
+static void lde_big_run(p3g_ctx* ctx, const typename F::T* in, int log_h, int w, int log_b, uint64_t shift,
+                        int bitrev_out, typename F::T* out, cudaStream_t st, RootTab<F> roots,
+                        const typename F::TW* dft_tw) {
+    using T = typename F::T;
+    const int64_t h = int64_t(1) << log_h;
+    T* coeffs = static_cast<T*>(ctx->alloc(sizeof(T) * size_t(h) * size_t(w), st));
+    try {
+        big_run<F, 1>(in, log_h, w, 1, F::h_inv(uint64_t(h) % F::P), 1, 0, coeffs, 0, 1, st, roots, dft_tw, ctx);
+        const uint64_t wH = F::root(unsigned(log_h + log_b));
+        for (int t = 0; t < (1 << log_b); ++t) {
+            const unsigned u = bitrev_ct(unsigned(t), log_b);
+            const uint64_t g = F::h_mul(shift, F::h_pow(wH, u));
+            if (bitrev_out)
+                big_run<F, 0>(coeffs, log_h, w, g, 1, 1, 1, out + size_t(t) * size_t(h) * size_t(w), 0, 1, st, roots,
+                              dft_tw, ctx);
+            else
+                big_run<F, 0>(coeffs, log_h, w, g, 1, 1, 0, out, int64_t(u), int64_t(1) << log_b, st, roots, dft_tw,
+                              ctx);
+        }
+    } catch (...) {
+        ctx->release(coeffs, st);
+        throw;
+    }
+    ctx->release(coeffs, st);
+}
+
 // Context entry: validates and dispatches one of the four kinds.
 template <class F>
 static void dft_impl(p3g_ctx* ctx, int kind, const typename F::T* in, int log_h, int w, uint64_t shift,
@@ -301,7 +443,7 @@ static void dft_impl(p3g_ctx* ctx, int kind, const typename F::T* in, int log_h,
                      const typename F::TW* dft_tw) {
     P3G_REQUIRE(kind >= DFT_FWD && kind <= DFT_COSET_INV, "dft: unknown kind");
     P3G_REQUIRE(log_h >= 0 && log_h <= int(F::TWO_ADICITY), "dft: log_h exceeds two-adicity");
-    if (log_h > LDE_PASS_MAX) throw Error(P3G_EUNSUPPORTED, "dft: log_h > 21 is not supported");
+    if (log_h > LDE_BIG_MAX) throw Error(P3G_EUNSUPPORTED, "dft: log_h > 26 is not supported");
     const bool coset = kind == DFT_COSET || kind == DFT_COSET_INV;
     if (coset) P3G_REQUIRE(shift % F::P != 0, "dft: shift must be non-zero");
     if (w == 0) return;
@@ -314,10 +456,16 @@ static void dft_impl(p3g_ctx* ctx, int kind, const typename F::T* in, int log_h,
     const uint64_t sigma = kind == DFT_COSET ? shift % F::P : 1;
     const uint64_t beta0 = inv ? F::h_inv(uint64_t(h) % F::P) : 1;
     const uint64_t alpha = kind == DFT_COSET_INV ? F::h_inv(shift % F::P) : 1;
-    if (inv)
+    if (log_h > LDE_PASS_MAX) {
+        if (inv)
+            big_run<F, 1>(in, log_h, w, sigma, beta0, alpha, bitrev_out, out, 0, 1, st, roots, dft_tw, ctx);
+        else
+            big_run<F, 0>(in, log_h, w, sigma, beta0, alpha, bitrev_out, out, 0, 1, st, roots, dft_tw, ctx);
+    } else if (inv) {
         dft_run<F, 1>(in, log_h, w, sigma, beta0, alpha, bitrev_out, out, st, roots, dft_tw, ctx);
-    else
+    } else {
         dft_run<F, 0>(in, log_h, w, sigma, beta0, alpha, bitrev_out, out, st, roots, dft_tw, ctx);
+    }
 }
 
 }  // namespace p3g

@@ -168,6 +168,11 @@ void* make_dft_tw_bb();
 void* make_dft_tw_gl();
 void lde_gl(p3g_ctx* ctx, const uint64_t* in, int log_h, int w, int log_b, uint64_t shift,
             int bitrev_out, uint64_t* out, cudaStream_t st);
+// the coset LDE for 2^21 < h <= 2^26, called by lde_bb / lde_gl (dft_bb.cu, dft_gl.cu)
+void lde_big(p3g_ctx* ctx, const uint32_t* in, int log_h, int w, int log_b, uint64_t shift, int bitrev_out,
+             uint32_t* out, cudaStream_t st);
+void lde_big(p3g_ctx* ctx, const uint64_t* in, int log_h, int w, int log_b, uint64_t shift, int bitrev_out,
+             uint64_t* out, cudaStream_t st);
 // dft / idft / coset_dft / coset_idft (kind = P3G_DFT_*)
 void dft_bb(p3g_ctx* ctx, int kind, const uint32_t* in, int log_h, int w, uint32_t shift, int bitrev_out,
             uint32_t* out, cudaStream_t st);

@@ -24,6 +24,8 @@
 //           scale c_k * g_t^k, size-N1 forward DFT and twiddle
 //           g_t^(k2) w_h^(k2 m1), write out row t*h + bitrev(m1)*N2 + k2;
 //   pass 3: size-N2 forward DFT over contiguous N2-row blocks, in place.
+// 2^21 < h <= 2^26: the coefficients and each coset's transform through the
+// split transform of dft.cuh (lde_big_run), same output layout.
 // Every pass reads its tile straight from global memory into the registers
 // of the first radix-32 super-stage and writes the last super-stage's
 // registers straight back; shared memory only carries the exchange between
@@ -37,10 +39,16 @@ namespace p3g {
 
 template <class F>
 struct LdeCfg;
+#ifndef P3G_LDE_BB_C13
+#define P3G_LDE_BB_C13 16
+#endif
+#ifndef P3G_LDE_BB_C2
+#define P3G_LDE_BB_C2 8
+#endif
 template <>
 struct LdeCfg<FBB> {
-    static constexpr int C13 = 16;   // columns per tile, passes 1/3 and single (64-byte rows)
-    static constexpr int C2 = 8;     // pass 2 keeps two tiles: 32-byte rows, two CTAs per SM
+    static constexpr int C13 = P3G_LDE_BB_C13;  // columns per tile, passes 1/3 and single (64-byte rows)
+    static constexpr int C2 = P3G_LDE_BB_C2;    // pass 2 keeps two tiles: 32-byte rows, two CTAs per SM
     static constexpr int MAXT = 256;
     static constexpr uint32_t ONE_C = bb::R1;
 };
@@ -52,8 +60,20 @@ struct LdeCfg<FGL> {
     static constexpr uint64_t ONE_C = 1;
 };
 
+// Minimum resident CTAs per SM of passes 1/3 and of pass 2 (launch bounds;
+// settable at build time to compare register budgets).
+#ifndef P3G_LDE_MINB13
+#define P3G_LDE_MINB13 2
+#endif
+#ifndef P3G_LDE_MINB2
+#define P3G_LDE_MINB2 2
+#endif
+
 constexpr int LDE_SINGLE_MAX = 10;  // single-kernel LDE up to h = 2^10
 constexpr int LDE_PASS_MAX = 21;    // three-pass LDE up to h = 2^21
+// above it, one more split h = 2^21 * B with B <= 32 (dft.cuh, big_run; B is
+// bounded by the in-register roots, which go up to omega_32)
+constexpr int LDE_BIG_MAX = LDE_PASS_MAX + 5;
 
 // Prepared in-tile DFT twiddles (one table per context and field): for every
 // LOGN in 1..DFT_TW_MAXLOG the N = 2^LOGN powers omega_N^e, e < N, as F::TW;
@@ -285,7 +305,7 @@ k_lde_single(const typename F::T* __restrict__ in, typename F::T* __restrict__ o
 
 // ------------------------------------------------------------ pass 1 (LOGN = n2)
 template <class F, int LOGN>
-__global__ void __launch_bounds__(Tile<F, LOGN, LdeCfg<F>::C13>::THREADS, 2)
+__global__ void __launch_bounds__(Tile<F, LOGN, LdeCfg<F>::C13>::THREADS, P3G_LDE_MINB13)
 k_lde_pass1(const typename F::T* __restrict__ in, typename F::T* __restrict__ scratch, int w, int n1,
             RootTab<F> roots, const typename F::TW* __restrict__ gtwi) {
     constexpr int C = LdeCfg<F>::C13;
@@ -322,7 +342,7 @@ k_lde_pass1(const typename F::T* __restrict__ in, typename F::T* __restrict__ sc
 
 // ------------------------------------------------------------ pass 2 (LOGN = n1)
 template <class F, int LOGN>
-__global__ void __launch_bounds__(Tile<F, LOGN, LdeCfg<F>::C2>::THREADS, 2)
+__global__ void __launch_bounds__(Tile<F, LOGN, LdeCfg<F>::C2>::THREADS, P3G_LDE_MINB2)
 k_lde_pass2(const typename F::T* __restrict__ scratch, typename F::T* __restrict__ dst, int w, int n2,
             int log_b, const typename F::T* __restrict__ sp, const typename F::T* __restrict__ sq,
             RootTab<F> roots, const typename F::TW* __restrict__ gtwi, const typename F::TW* __restrict__ gtwf,
@@ -377,7 +397,7 @@ k_lde_pass2(const typename F::T* __restrict__ scratch, typename F::T* __restrict
 
 // ------------------------------------------------------------ pass 3 (LOGN = n2)
 template <class F, int LOGN>
-__global__ void __launch_bounds__(Tile<F, LOGN, LdeCfg<F>::C13>::THREADS, 2)
+__global__ void __launch_bounds__(Tile<F, LOGN, LdeCfg<F>::C13>::THREADS, P3G_LDE_MINB13)
 k_lde_pass3(const typename F::T* src, typename F::T* out, int w, int n1, int log_b, int bitrev_out,
             RootTab<F> roots, const typename F::TW* __restrict__ gtwf) {
     constexpr int C = LdeCfg<F>::C13;
@@ -587,10 +607,14 @@ static void lde_impl(p3g_ctx* ctx, const typename F::T* in, int log_h, int w, in
                      const typename F::TW* dft_tw) {
     P3G_REQUIRE(log_h >= 0 && log_b >= 0, "coset_lde: negative size");
     P3G_REQUIRE(log_h + log_b <= int(F::TWO_ADICITY), "coset_lde: log_h + log_blowup exceeds two-adicity");
-    if (log_h > LDE_PASS_MAX) throw Error(P3G_EUNSUPPORTED, "coset_lde: log_h > 21 is not supported");
+    if (log_h > LDE_BIG_MAX) throw Error(P3G_EUNSUPPORTED, "coset_lde: log_h > 26 is not supported");
     P3G_REQUIRE(shift % F::P != 0, "coset_lde: shift must be non-zero");
     if (w == 0) return;
     shift %= F::P;
+    if (log_h > LDE_PASS_MAX) {
+        lde_big(ctx, in, log_h, w, log_b, shift, bitrev_out, out, st);
+        return;
+    }
     const LdeScratch need = lde_scratch<F>(log_h, w, log_b, bitrev_out);
     void* buf[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
     auto release = [&] {

@@ -128,8 +128,16 @@ __device__ __forceinline__ void reg_dif(typename F::T* x) {
 // 4-byte elements and 4 for 8-byte ones: a radix-32 group of u64 values
 // takes 64 registers per thread before any temporaries, which held the
 // Goldilocks passes to a few warps per SM.
+// (Both limits can be set at build time, -DP3G_SS_MLR4= / -DP3G_SS_MLR8=, to
+// compare splits.)
+#ifndef P3G_SS_MLR4
+#define P3G_SS_MLR4 5
+#endif
+#ifndef P3G_SS_MLR8
+#define P3G_SS_MLR8 4
+#endif
 template <class T>
-__host__ __device__ constexpr int ss_max_lr() { return sizeof(T) == 8 ? 4 : 5; }
+__host__ __device__ constexpr int ss_max_lr() { return sizeof(T) == 8 ? P3G_SS_MLR8 : P3G_SS_MLR4; }
 __host__ __device__ constexpr int ss_count(int logn, int mlr) { return logn == 0 ? 0 : (logn + mlr - 1) / mlr; }
 __host__ __device__ constexpr int ss_radix(int logn, int j, int mlr) {
     // ceil-balanced split: the first (logn % cnt) parts get one more bit

@@ -45,6 +45,29 @@ def test_large_heights_vs_oracle(gpu_ctx, log_h, w, kind):
     assert np.array_equal(gpu_ctx.dft(KIND[kind], m, 7), O.bb_dft(kind, m, 7))
 
 
+@pytest.mark.parametrize("log_h,w", [(22, 2), (23, 1)])
+@pytest.mark.parametrize("kind", ["dft", "idft", "coset_dft", "coset_idft"])
+def test_split_transform_heights_vs_oracle(gpu_ctx, log_h, w, kind):
+    """Above 2^21 rows the transform splits once more (inner 2^21-point
+    transforms, outer 2- and 4-point steps): every kind, both orders."""
+    m = np.random.default_rng(log_h + w).integers(0, O.BB_P, size=(1 << log_h, w), dtype=np.uint32)
+    want = O.bb_dft(kind, m, 11)
+    assert np.array_equal(gpu_ctx.dft(KIND[kind], m, 11), want)
+    br = np.arange(1 << log_h, dtype=np.int64)
+    rev = np.zeros_like(br)
+    for b in range(log_h):
+        rev |= ((br >> b) & 1) << (log_h - 1 - b)
+    assert np.array_equal(gpu_ctx.dft(KIND[kind], m, 11, bitrev=True), want[rev])
+
+
+def test_goldilocks_split_transform_identities(gpu_ctx):
+    x = np.random.default_rng(22).integers(0, O.GL_P, size=(1 << 22, 2), dtype=np.uint64)
+    assert np.array_equal(gpu_ctx.dft(P.IDFT, gpu_ctx.dft(P.DFT, x)), x)
+    assert np.array_equal(gpu_ctx.dft(P.COSET_IDFT, gpu_ctx.dft(P.COSET_DFT, x, 7), 7), x)
+    lde = gpu_ctx.coset_lde(x, 0, 7, bitrev=False)
+    assert np.array_equal(lde, gpu_ctx.dft(P.COSET_DFT, gpu_ctx.dft(P.IDFT, x), 7))
+
+
 def _gl_pow(a, e):
     return pow(int(a), int(e), O.GL_P)
 
@@ -92,6 +115,8 @@ def test_bad_arguments(gpu_ctx):
     assert L.p3g_dft(gpu_ctx.handle, P.BABYBEAR, 4, d.ptr, 4, 4, 0, 0, d.ptr + 2048, None) == 1
     assert L.p3g_dft(gpu_ctx.handle, P.BABYBEAR, P.DFT, d.ptr, 4, 4, 0, 0, d.ptr, None) == 1  # in == out
     assert L.p3g_dft(gpu_ctx.handle, P.BABYBEAR, P.COSET_DFT, d.ptr, 2, 2, 0, 0, d.ptr + 64, None) == 1
-    assert L.p3g_dft(gpu_ctx.handle, P.BABYBEAR, P.DFT, d.ptr, 22, 1, 0, 0, d.ptr + 64, None) == 5
+    # 2^27 rows is within the field's two-adicity but above the split transform's 2^26
+    assert L.p3g_dft(gpu_ctx.handle, P.BABYBEAR, P.DFT, d.ptr, 27, 1, 0, 0, d.ptr + 64, None) == 5
+    assert L.p3g_dft(gpu_ctx.handle, P.BABYBEAR, P.DFT, d.ptr, 28, 1, 0, 0, d.ptr + 64, None) == 1
     assert L.p3g_dft(gpu_ctx.handle, 7, P.DFT, d.ptr, 2, 2, 0, 0, d.ptr + 64, None) == 1
     d.free()

@@ -94,3 +94,27 @@ def test_host_commit_staged_row_hashes(gpu_ctx, field, shapes):
     dev.free()
     for b in bufs:
         b.free()
+
+
+def test_commit_above_three_pass_height(gpu_ctx):
+    """A 2^22-row trace (LDE through the split transform) next to a short one:
+    the host-trace commit equals the device commit, and the device commit's
+    leaf digests equal the oracle's sponge over the oracle's LDE rows."""
+    rng = np.random.default_rng(22)
+    shapes = [(22, 9), (12, 8)]
+    traces = [rng.integers(0, O.BB_P, size=(1 << lh, w), dtype=np.uint32) for lh, w in shapes]
+    bufs = [gpu_ctx.to_device(t) for t in traces]
+    dev = gpu_ctx.commit_traces_device(P.BABYBEAR, [(b.ptr, lh, w, 1, 31) for b, (lh, w) in zip(bufs, shapes)], 0)
+    host = gpu_ctx.commit_traces_host(P.BABYBEAR, [(t.ctypes.data, lh, w, 1, 31)
+                                                   for t, (lh, w) in zip(traces, shapes)], 0)
+    for a, b in zip(host.layers(), dev.layers()):
+        assert np.array_equal(a, b)
+    lde = O.bb_coset_lde(traces[0], 1, 31, True, nthreads=8)
+    leaves = dev.layers()[0]
+    p = O.bb16_params()
+    for r in (0, 1, 12345, (1 << 23) - 1):
+        assert np.array_equal(leaves[r], O.hash_iter(p, lde[r])), r
+    host.free()
+    dev.free()
+    for b in bufs:
+        b.free()

@@ -106,7 +106,29 @@ def test_lde_largest_supported_heights(gpu_ctx, log_h, w, lb, field):
         assert np.array_equal(gpu_ctx.coset_lde(t, lb, shift, br), ref(br)), (log_h, w, lb, br)
 
 
+@pytest.mark.parametrize("log_h,w,lb,field", [(22, 3, 1, "bb"), (23, 1, 2, "bb"), (22, 2, 1, "gl")])
+def test_lde_split_transform_heights(gpu_ctx, log_h, w, lb, field):
+    """Above 2^21 rows the coefficients and each coset's evaluations go through
+    the split transform (2^21-point inner transforms, 2- or 4-point outer
+    steps): every element against the oracle, both orders."""
+    rng = np.random.default_rng(log_h * 11 + w)
+    if field == "bb":
+        t = rng.integers(0, O.BB_P, size=(1 << log_h, w), dtype=np.uint32)
+        ref = lambda br: O.bb_coset_lde(t, lb, 31, br, nthreads=os.cpu_count() or 1)
+        shift = 31
+    else:
+        t = rng.integers(0, O.GL_P, size=(1 << log_h, w), dtype=np.uint64)
+        ref = lambda br: O.gl_coset_lde(t, lb, 7, br, nthreads=os.cpu_count() or 1)
+        shift = 7
+    for br in (True, False):
+        assert np.array_equal(gpu_ctx.coset_lde(t, lb, shift, br), ref(br)), (log_h, w, lb, br)
+
+
 def test_lde_beyond_supported_height_is_reported(gpu_ctx):
     d = gpu_ctx.alloc(64)
-    assert P.load().p3g_coset_lde(gpu_ctx.handle, 0, d.ptr, 22, 1, 1, 31, 1, d.ptr, None) == 5  # unsupported
+    L = P.load()
+    # 2^27 rows: within BabyBear's two-adicity (no blowup) but above the split transform's 2^26
+    assert L.p3g_coset_lde(gpu_ctx.handle, 0, d.ptr, 27, 1, 0, 31, 1, d.ptr, None) == 5  # unsupported
+    assert L.p3g_coset_lde(gpu_ctx.handle, 1, d.ptr, 27, 1, 1, 7, 1, d.ptr, None) == 5
+    assert L.p3g_coset_lde(gpu_ctx.handle, 0, d.ptr, 27, 1, 1, 31, 1, d.ptr, None) == 1  # beyond two-adicity
     d.free()
