@@ -83,9 +83,12 @@ namespace {
 uint64_t footprint(const p3g_request& r) {
     const uint64_t h = uint64_t(1) << r.log_h, H = h << r.log_blowup;
     const uint64_t w = r.width;
-    // trace + LDE + LDE scratch (h*w) + digests (2H * 32 B) + descriptors
-    // + packed fold input (H * 16 B) + fold output (H/2 * 16 B) + slack
-    return 4 * h * w + 4 * H * w + 4 * h * w + 64 * H + 16 * H + 8 * H + (1u << 20);
+    // trace + LDE + LDE scratch (h*w; three times that above 2^21 rows: the
+    // coefficients, the inner transforms' output and their staging) + digests
+    // (2H * 32 B) + descriptors + packed fold input (H * 16 B) + fold output
+    // (H/2 * 16 B) + slack
+    const uint64_t scratch = (r.log_h > 21 ? 3 : 1) * 4 * h * w;
+    return 4 * h * w + 4 * H * w + scratch + 64 * H + 16 * H + 8 * H + (1u << 20);
 }
 
 void finish(p3g_server* s, const std::shared_ptr<Job>& j) {
@@ -257,7 +260,7 @@ int p3g_server_submit(p3g_server* s, const p3g_request* req) {
         P3G_REQUIRE(s && req, "server_submit: null argument");
         P3G_REQUIRE(req->width >= 4, "server_submit: width must be >= 4 (the fold reads four columns)");
         P3G_REQUIRE(req->h_trace != nullptr, "server_submit: null trace");
-        P3G_REQUIRE(req->log_h + req->log_blowup <= 27 && req->log_h <= 21 && req->log_h + req->log_blowup >= 1,
+        P3G_REQUIRE(req->log_h + req->log_blowup <= 27 && req->log_h <= 26 && req->log_h + req->log_blowup >= 1,
                     "server_submit: unsupported size");
         P3G_REQUIRE(req->shift % p3g::bb::P != 0 && req->shift < p3g::bb::P, "server_submit: bad shift");
         for (int k = 0; k < 4; ++k) P3G_REQUIRE(req->beta[k] < p3g::bb::P, "server_submit: beta must be canonical");
