@@ -415,6 +415,7 @@ static void lde_big_run(p3g_ctx* ctx, const typename F::T* in, int log_h, int w,
                         const typename F::TW* dft_tw) {
     using T = typename F::T;
     const int64_t h = int64_t(1) << log_h;
+    P3G_REQUIRE(w <= (1 << 17), "coset_lde: width above 2^17 at log_h > 21");  // big_run's limit, checked first
     T* coeffs = static_cast<T*>(ctx->alloc(sizeof(T) * size_t(h) * size_t(w), st));
     try {
         big_run<F, 1>(in, log_h, w, 1, F::h_inv(uint64_t(h) % F::P), 1, 0, coeffs, 0, 1, st, roots, dft_tw, ctx);

@@ -131,4 +131,7 @@ def test_lde_beyond_supported_height_is_reported(gpu_ctx):
     assert L.p3g_coset_lde(gpu_ctx.handle, 0, d.ptr, 27, 1, 0, 31, 1, d.ptr, None) == 5  # unsupported
     assert L.p3g_coset_lde(gpu_ctx.handle, 1, d.ptr, 27, 1, 1, 7, 1, d.ptr, None) == 5
     assert L.p3g_coset_lde(gpu_ctx.handle, 0, d.ptr, 27, 1, 1, 31, 1, d.ptr, None) == 1  # beyond two-adicity
+    # above 2^21 rows the width is limited to 2^17 (checked before anything is allocated or launched)
+    assert L.p3g_coset_lde(gpu_ctx.handle, 0, d.ptr, 22, (1 << 17) + 1, 1, 31, 1, d.ptr, None) == 1
+    assert L.p3g_dft(gpu_ctx.handle, 0, P.DFT, d.ptr, 22, (1 << 17) + 1, 0, 0, d.ptr + 32, None) == 1
     d.free()
