@@ -60,6 +60,32 @@ def test_split_transform_heights_vs_oracle(gpu_ctx, log_h, w, kind):
     assert np.array_equal(gpu_ctx.dft(KIND[kind], m, 11, bitrev=True), want[rev])
 
 
+def _bitrev_rows(log_h):
+    idx = np.arange(1 << log_h, dtype=np.int64)
+    rev = np.zeros_like(idx)
+    for b in range(log_h):
+        rev |= ((idx >> b) & 1) << (log_h - 1 - b)
+    return rev
+
+
+@pytest.mark.parametrize("log_h,kind", [(24, "coset_idft"), (25, "dft"), (26, "coset_dft")])
+def test_split_transform_outer_sizes_vs_oracle(gpu_ctx, log_h, kind):
+    """Outer steps of 8, 16 and 32 points (2^24 .. 2^26 rows, one column),
+    forward, inverse with the coset scaling, both orders."""
+    m = np.random.default_rng(log_h).integers(0, O.BB_P, size=(1 << log_h, 1), dtype=np.uint32)
+    want = O.bb_dft(kind, m, 31)
+    assert np.array_equal(gpu_ctx.dft(KIND[kind], m, 31), want)
+    assert np.array_equal(gpu_ctx.dft(KIND[kind], m, 31, bitrev=True), want[_bitrev_rows(log_h)])
+
+
+@pytest.mark.parametrize("log_h", [25, 26])
+def test_goldilocks_split_transform_outer_sizes(gpu_ctx, log_h):
+    x = np.random.default_rng(log_h).integers(0, O.GL_P, size=(1 << log_h, 1), dtype=np.uint64)
+    fwd = gpu_ctx.dft(P.COSET_DFT, x, 7)
+    assert np.array_equal(gpu_ctx.dft(P.COSET_IDFT, fwd, 7), x)
+    assert np.array_equal(gpu_ctx.dft(P.COSET_DFT, x, 7, bitrev=True), fwd[_bitrev_rows(log_h)])
+
+
 def test_goldilocks_split_transform_identities(gpu_ctx):
     x = np.random.default_rng(22).integers(0, O.GL_P, size=(1 << 22, 2), dtype=np.uint64)
     assert np.array_equal(gpu_ctx.dft(P.IDFT, gpu_ctx.dft(P.DFT, x)), x)

@@ -124,6 +124,19 @@ def test_lde_split_transform_heights(gpu_ctx, log_h, w, lb, field):
         assert np.array_equal(gpu_ctx.coset_lde(t, lb, shift, br), ref(br)), (log_h, w, lb, br)
 
 
+def test_lde_split_transform_eight_point_outer_step(gpu_ctx):
+    """2^24 rows: 2^21-point inner transforms and an 8-point outer step, both
+    orders, against the oracle."""
+    t = np.random.default_rng(24).integers(0, O.BB_P, size=(1 << 24, 2), dtype=np.uint32)
+    want = O.bb_coset_lde(t, 1, 31, False, nthreads=2)
+    assert np.array_equal(gpu_ctx.coset_lde(t, 1, 31, False), want)
+    idx = np.arange(1 << 25, dtype=np.int64)
+    rev = np.zeros_like(idx)
+    for b in range(25):
+        rev |= ((idx >> b) & 1) << (24 - b)
+    assert np.array_equal(gpu_ctx.coset_lde(t, 1, 31, True), want[rev])
+
+
 def test_lde_beyond_supported_height_is_reported(gpu_ctx):
     d = gpu_ctx.alloc(64)
     L = P.load()
