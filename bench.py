@@ -1,22 +1,29 @@
 #!/usr/bin/env python3
 """Benchmark of the trace-commitment hot path on GB300.
 
-Workload (default): the plain single-trace BabyBear commit -- a 2^20 x 256
-trace of uniform random elements, coset LDE with log_blowup 1 and shift 31
-(rows bit-reversed, 2^21 x 256 = 2 GiB of u32), then the Poseidon2-16
-(x^7, 8 full + 13 partial rounds, seeded constants) mixed-height MMCS commit
-to one root.  A step is one full commit of that trace.
+Headline workload (the metric's configuration): the batched commit of 64
+BabyBear traces -- log2 height uniform over {12..18}, width uniform in
+[8, 512], log_blowup 1, shift 31 -- as one mixed-height Poseidon2-16 (x^7,
+8 full + 13 partial rounds, seeded constants) MMCS, plus fold_matrix of a
+2^19-row BabyBear^4 quotient (log_arity 1, seeded beta), all captured in one
+CUDA graph (p3g_plan_commit).  A step is one launch of that graph.  The same
+work done as plain per-trace commits (one p3g_commit_traces call per trace,
+then the fold) is timed beside it.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-Prints one JSON line (rank 0).  `value` is committed LDE elements/s with the
-trace already resident in HBM (device-timed with CUDA events on the launching
-stream); `e2e` is the same metric through the C ABI with the trace in pinned
-host memory, the host->device copy and the root read-back inside the timed
-region.  `--impl reference` times the CPU restatement of the reference path
-(the oracle, built from oracle/) on the host cores, on a bounded sample of the
-same workload.  Inputs (1 GiB trace, 2 GiB LDE) are larger than L2 (129 MB),
-so no L2 flush is needed between steps.
+Prints one JSON line (rank 0).  `value` is committed LDE elements/s of the
+batched plan with the traces resident in HBM (CUDA events on the launching
+stream); `plain_per_trace` and `batched_over_plain` compare it with the
+per-trace commit.  `e2e` is the same metric through the host-input plan
+(p3g_plan_commit_host): the traces and the fold input in pinned host memory
+are copied in inside every step, and the root and the fold output are read
+back.  `config1` (a 2^20 x 256 single trace), `config2` (Goldilocks), the
+prover steps and `config4` (serving) are further workloads.  `--impl
+reference` times the CPU restatement of the reference path (the oracle,
+built from oracle/) on the host cores, on a bounded sample of the same
+workload.  The traces (4.2 GB) and LDEs (8.4 GB) exceed L2 (129 MB), so no
+flush is needed between steps.
 """
 from __future__ import annotations
 
@@ -37,8 +44,14 @@ sys.path.insert(0, os.path.join(REPO, "plonky3-gpu_gb300"))
 
 METRIC = "committed LDE elements/s on 1 GB300, batched vs plain per-trace; p50/p99 ms"
 UNIT = "elements/s"
-LOG_H, WIDTH, LOG_B, SHIFT = 20, 256, 1, 31
 BB_P = 0x78000001
+GL_P = 0xFFFFFFFF00000001
+SHIFT = 31
+C3_LOG_B = 1
+C3_FOLD_LOG = 19
+C1_LOG_H, C1_WIDTH, C1_LOG_B = 20, 256, 1
+# the SM count and SMSPs of a GB300 (the issue bound below)
+SMSPS = 152 * 4
 
 
 def peaks():
@@ -124,22 +137,61 @@ class ClockSampler:
                 "sm_max_mhz": max(mx) if mx else None, "reasons": reasons, "samples": len(rows)}
 
 
-def cpu_sample(nthreads: int, log_h: int = 14):
-    """The oracle's commit (restated Radix2Dit LDE + Poseidon2 MMCS) on a bounded
-    sample of the workload: same width, blowup and hash, height 2^log_h."""
+# ------------------------------------------------------------------ workloads
+def config3_shapes(seed: int = 3):
+    """64 BabyBear traces: (log2 height uniform over {12..18}, width uniform in [8, 512])."""
+    rng = np.random.default_rng(seed)
+    return [(int(rng.integers(12, 19)), int(rng.integers(8, 513))) for _ in range(64)]
+
+
+def config3_inputs(seed: int = 3, shrink: int = 0):
+    """The batched workload's inputs: the 64 traces (uniform canonical BabyBear
+    elements, trace i from default_rng([seed, i])), the 2^19 x 4 quotient
+    (default_rng([seed, 64])) and the folding challenge beta.  `shrink` divides
+    every height (and the quotient's) by 2^shrink: the bounded CPU samples."""
+    shapes = [(lh - shrink, w) for lh, w in config3_shapes(seed)]
+    traces = [np.random.default_rng([seed, i]).integers(0, BB_P, size=(1 << lh, w), dtype=np.uint32)
+              for i, (lh, w) in enumerate(shapes)]
+    fold_in = np.random.default_rng([seed, 64]).integers(0, BB_P, size=(1 << (C3_FOLD_LOG - shrink), 4),
+                                                         dtype=np.uint32)
+    beta = [int(x) for x in np.random.default_rng([seed, 65]).integers(0, BB_P, 4)]
+    return shapes, traces, fold_in, beta
+
+
+def lde_butterflies(shapes, log_b: int) -> float:
+    """Radix-2 butterflies of the coset LDEs: per column an inverse transform
+    of size h and 2^b forward ones, (h / 2) log2 h butterflies each."""
+    return float(sum(w * (1 + (1 << log_b)) * ((1 << lh) // 2) * lh for lh, w in shapes))
+
+
+def issue_bound_ms(butterflies: float, sm_mhz: float | None) -> float:
+    """The BabyBear LDE's instruction-issue bound: six ALU-pipe instructions per
+    butterfly (modular add, lazy difference, the Shoup product's correction),
+    16 lanes per SMSP per clock on the ALU pipe, 608 SMSPs."""
+    mhz = sm_mhz or 2070.0
+    return butterflies * 6 / (SMSPS * 16 * mhz * 1e6) * 1e3
+
+
+def cpu_sample(nthreads: int, shrink: int):
+    """The oracle's batched commit (restated Radix2Dit LDEs, one mixed-height
+    Poseidon2 MMCS, fold_matrix) on the config-3 traces with every height
+    divided by 2^shrink.  Returns (LDE elements/s, seconds, description)."""
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import oracle as O
 
     O.build()
-    rng = np.random.default_rng(5)
-    t = rng.integers(0, BB_P, size=(1 << log_h, WIDTH), dtype=np.uint32)
+    shapes, traces, fold_in, beta = config3_inputs(3, shrink)
     p = O.bb16_params()
     t0 = time.perf_counter()
-    lde = O.bb_coset_lde(t, LOG_B, SHIFT, True, nthreads=nthreads)
-    O.mmcs_commit(p, [lde], 0, nthreads=nthreads)
+    ldes = [O.bb_coset_lde(t, C3_LOG_B, SHIFT, True, nthreads=nthreads) for t in traces]
+    O.mmcs_commit(p, ldes, 0, nthreads=nthreads)
+    O.fold_matrix_bb4(fold_in, C3_FOLD_LOG - shrink, 1, beta, nthreads=nthreads)
     dt = time.perf_counter() - t0
-    elems = (1 << (log_h + LOG_B)) * WIDTH
-    return elems / dt, dt, f"2^{log_h} x {WIDTH} BabyBear trace, log_blowup 1, LDE + Poseidon2-16 MMCS root"
+    elems = sum((1 << (lh + C3_LOG_B)) * w for lh, w in shapes)
+    desc = (f"the 64 config-3 traces with every height divided by 2^{shrink} (log2 h in "
+            f"{{{12 - shrink}..{18 - shrink}}}, {elems / 1e6:.0f} M LDE elements), one mixed-height Poseidon2-16 "
+            f"MMCS, fold of a 2^{C3_FOLD_LOG - shrink} BabyBear^4 quotient")
+    return elems / dt, dt, desc
 
 
 def run_reference(args):
@@ -148,11 +200,11 @@ def run_reference(args):
         return 0
     nthreads = os.cpu_count() or 1
     for _ in range(args.warmup):
-        cpu_sample(nthreads, 12)
+        cpu_sample(nthreads, 9)
     vals, times = [], []
     desc = ""
     for _ in range(args.steps):
-        v, dt, desc = cpu_sample(nthreads)
+        v, dt, desc = cpu_sample(nthreads, args.ref_shrink)
         vals.append(v)
         times.append(dt * 1e3)
     value = statistics.mean(vals)
@@ -161,7 +213,7 @@ def run_reference(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": statistics.mean(times),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32 (BabyBear)",
         "data": "synthetic",
-        "config": {"workload": "plain single-trace BabyBear commit, 2^20 x 256, log_blowup 1 (bounded CPU sample)",
+        "config": {"workload": "batched commit of the 64 config-3 BabyBear traces + fold (bounded CPU sample)",
                    "sample": desc},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port", "sample": desc},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -170,7 +222,185 @@ def run_reference(args):
     return 0
 
 
-GL_P = 0xFFFFFFFF00000001
+def events_timed(torch, dev, stream, fn, n):
+    """Per-call durations (ms) of n calls of fn, CUDA events on `stream`."""
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(n + 1)]
+    torch.cuda.synchronize(dev)
+    with torch.cuda.stream(stream):
+        for i in range(n):
+            evs[i].record(stream)
+            fn()
+        evs[-1].record(stream)
+    torch.cuda.synchronize(dev)
+    return [evs[i].elapsed_time(evs[i + 1]) for i in range(n)]
+
+
+def pinned_copy(torch, a: np.ndarray):
+    """A page-locked host copy of a uint32 / uint64 array (a torch tensor that keeps it alive)."""
+    dt = torch.int32 if a.dtype == np.uint32 else torch.int64
+    t = torch.empty(a.size, dtype=dt, pin_memory=True)
+    t.numpy().view(a.dtype)[:] = a.reshape(-1)
+    return t
+
+
+def traffic_of(key: str):
+    tpath = os.path.join(REPO, "profiles", "traffic.json")
+    if os.path.exists(tpath):
+        with open(tpath) as f:
+            return json.load(f).get(key)
+    return None
+
+
+# ------------------------------------------------------------------ further workloads
+def run_config1(P, torch, ctx, dev, stream, steps: int, warmup: int, log_h: int, width: int, perm_peak: float):
+    """Config 1: the plain single-trace BabyBear commit of a 2^20 x 256 trace
+    (LDE 2^21 x 256 = 2 GiB), device-timed with the trace resident, its LDE
+    alone for the HBM roofline, and end to end through p3g_commit_traces_host
+    (pinned host trace, root read back)."""
+    sptr = stream.cuda_stream
+    h, H = 1 << log_h, 1 << (log_h + C1_LOG_B)
+    elems = H * width
+    trace = np.random.default_rng(1234).integers(0, BB_P, size=(h, width), dtype=np.uint32)
+    d_trace = ctx.to_device(trace)
+    ctx.sync()
+
+    def step():
+        ctx.commit_traces_device(P.BABYBEAR, [(d_trace.ptr, log_h, width, C1_LOG_B, SHIFT)], 0, stream=sptr).free(sptr)
+
+    for _ in range(max(warmup, 1)):
+        step()
+    st = events_timed(torch, dev, stream, step, steps)
+    ms = statistics.mean(st)
+    d_lde = ctx.alloc(elems * 4, sptr)
+    lde = lambda: ctx.coset_lde_device(P.BABYBEAR, d_trace.ptr, log_h, width, C1_LOG_B, SHIFT, True, d_lde.ptr, sptr)
+    for _ in range(2):
+        lde()
+    lde_ms = statistics.mean(events_timed(torch, dev, stream, lde, 10))
+    d_lde.free(sptr)
+    torch.cuda.synchronize(dev)
+
+    pinned = pinned_copy(torch, trace)
+    cap = np.zeros((1, 8), np.uint32)
+    e2e_ms = []
+    for i in range(warmup + steps):
+        t0 = time.perf_counter()
+        ctx.commit_traces_host(P.BABYBEAR, [(pinned.data_ptr(), log_h, width, C1_LOG_B, SHIFT)], 0,
+                               stream=sptr, cap_out=cap).free(sptr)
+        if i >= warmup:
+            e2e_ms.append((time.perf_counter() - t0) * 1e3)
+    torch.cuda.synchronize(dev)
+    d_trace.free()
+    hbm, src = peaks()
+    lde_bytes = 4 * width * (h + H)
+    lde_gbs = lde_bytes / (lde_ms / 1e3) / 1e9
+    perms = H * ((width + 7) // 8) + (H - 1)
+    hash_ms = ms - lde_ms
+    bfly = lde_butterflies([(log_h, width)], C1_LOG_B)
+    return {
+        "workload": f"plain single-trace BabyBear commit: 2^{log_h} x {width} trace, log_blowup {C1_LOG_B}, shift "
+                    f"{SHIFT}, bit-reversed LDE 2^{log_h + C1_LOG_B} x {width}, Poseidon2-16 (x^7, 8+13) MMCS, "
+                    "cap_height 0",
+        "value": elems / (ms / 1e3), "unit": UNIT, "ms_per_step": ms,
+        "p50_ms": float(np.percentile(st, 50)), "p99_ms": float(np.percentile(st, 99)),
+        "e2e": {"value": elems / (statistics.mean(e2e_ms) / 1e3), "unit": UNIT,
+                "h2d_bytes_per_step": h * width * 4, "d2h_bytes_per_step": 32,
+                "p50_ms": float(np.percentile(e2e_ms, 50)), "p99_ms": float(np.percentile(e2e_ms, 99)),
+                "samples_ms": [round(x, 3) for x in e2e_ms],
+                "call": "p3g_commit_traces_host (pinned host trace, root read back)"},
+        "roofline": {"kernel": f"coset LDE 2^{log_h} x {width} (k_lde_pass1/2/3)", "bound": "hbm",
+                     "achieved": lde_gbs, "peak": hbm, "unit": "GB/s", "frac": lde_gbs / hbm,
+                     "traffic": traffic_of(f"lde_bb_2p{log_h}x{width}_b{C1_LOG_B}_bytes"), "peak_source": src,
+                     "algorithmic_bytes": lde_bytes, "ms": lde_ms},
+        "issue_bound_ms": issue_bound_ms(bfly, None),
+        "stages": {"lde_ms": lde_ms, "merkle_ms": hash_ms, "perms": perms,
+                   "perms_per_s": perms / (hash_ms / 1e3) if hash_ms > 0 else None},
+        "hash_roofline": {"kernel": "Merkle stage (k_hash_groups leaf sponge + compress levels)",
+                          "bound": "integer multiply pipe (permutation issue)",
+                          "achieved": perms / (hash_ms / 1e3) if hash_ms > 0 else None, "unit": "perms/s",
+                          "peak": perm_peak, "peak_source": "isolated Poseidon2-16 permutation throughput, same run",
+                          "frac": perms / (hash_ms / 1e3) / perm_peak if hash_ms > 0 else None},
+    }
+
+
+def run_prover(P, torch, ctx, dev, stream, perm_peak: float):
+    """The prover steps after the commit on a resident 2^21 x 256 bit-reversed
+    LDE: PCS open's two passes, prove_fri on the reduced opening, FRI folds and
+    the proof-of-work search."""
+    sptr = stream.cuda_stream
+    rng = np.random.default_rng(77)
+    log_h, width = C1_LOG_H, C1_WIDTH
+    log_n = log_h + C1_LOG_B
+    H = 1 << log_n
+    elems = H * width
+    d_trace = ctx.to_device(rng.integers(0, BB_P, size=(1 << log_h, width), dtype=np.uint32))
+    tree = ctx.commit_traces_device(P.BABYBEAR, [(d_trace.ptr, log_h, width, C1_LOG_B, SHIFT)], 0, stream=sptr)
+    pts = rng.integers(0, BB_P, size=(2, 4), dtype=np.uint32)
+    alpha = rng.integers(0, BB_P, size=4, dtype=np.uint32)
+    d_q = ctx.alloc(H * 16, sptr)
+    ov = ctx.pcs_open_values_device(tree.leaf_ptr(0), log_n, width, True, SHIFT, pts, stream=sptr)
+    ctx.pcs_reduce_device(tree.leaf_ptr(0), log_n, width, True, SHIFT, pts, ov, alpha, 0, True, d_q.ptr, sptr)
+    open_ms = statistics.mean(events_timed(
+        torch, dev, stream, lambda: ctx.pcs_open_values_device(tree.leaf_ptr(0), log_n, width, True, SHIFT, pts,
+                                                              stream=sptr), 5))
+    reduce_ms = statistics.mean(events_timed(
+        torch, dev, stream, lambda: ctx.pcs_reduce_device(tree.leaf_ptr(0), log_n, width, True, SHIFT, pts, ov, alpha,
+                                                         0, True, d_q.ptr, sptr), 5))
+    fri_params = dict(log_blowup=C1_LOG_B, log_final_poly_len=0, max_log_arity=1, num_queries=100,
+                      commit_proof_of_work_bits=0, query_proof_of_work_bits=16)
+    st0 = rng.integers(0, BB_P, size=16, dtype=np.uint32)
+    ctx.fri_prove_device([(d_q.ptr, log_n)], fri_params, st0, [], [], stream=sptr)
+    fri_ms = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        fri_res = ctx.fri_prove_device([(d_q.ptr, log_n)], fri_params, st0, [], [], stream=sptr)
+        fri_ms.append((time.perf_counter() - t0) * 1e3)
+    d_q.free(sptr)
+    tree.free(sptr)
+    d_trace.free(sptr)
+    torch.cuda.synchronize(dev)
+
+    fold = {}
+    for log_f in (19, 25):
+        d_in = ctx.to_device(rng.integers(0, BB_P, size=(1 << log_f, 4), dtype=np.uint32))
+        d_out = ctx.alloc((1 << log_f) * 16 // 2, sptr)
+        beta_f = rng.integers(0, BB_P, size=4, dtype=np.uint32)
+        for la in (1, 2, 3):
+            f = lambda: ctx.fold_matrix_bb4_device(d_in.ptr, log_f, la, beta_f, d_out.ptr, sptr)
+            f()
+            ms = statistics.mean(events_timed(torch, dev, stream, f, 10))
+            nbytes = 16 * ((1 << log_f) + ((1 << log_f) >> la))
+            fold[f"2^{log_f}_arity{1 << la}"] = {"ms": ms, "algorithmic_bytes": nbytes,
+                                                 "gbs": nbytes / (ms / 1e3) / 1e9}
+        d_out.free(sptr)
+        d_in.free()
+    torch.cuda.synchronize(dev)
+
+    grind_bits, grind_cand, grind_s = 26, 0, 0.0
+    ctx.grind(P.BABYBEAR, np.zeros(16, np.uint32), [], 8, stream=sptr)
+    for k in range(4):
+        st = rng.integers(0, BB_P, size=16, dtype=np.uint32)
+        t0 = time.perf_counter()
+        w = ctx.grind(P.BABYBEAR, st, [int(x) for x in st[:k]], grind_bits, stream=sptr)
+        grind_s += time.perf_counter() - t0
+        grind_cand += w + 1
+    return {
+        "pcs_open": {"workload": f"TwoAdicFriPcs::open passes on the resident bit-reversed LDE 2^{log_n} x "
+                                 f"{width}, 2 BabyBear^4 points",
+                     "open_values_ms": open_ms, "reduce_ms": reduce_ms, "lde_bytes": elems * 4,
+                     "open_values_gbs": elems * 4 / (open_ms / 1e3) / 1e9,
+                     "reduce_gbs": elems * 4 / (reduce_ms / 1e3) / 1e9},
+        "fri_prove": {"workload": f"prove_fri over the 2^{log_n} BabyBear^4 reduced opening above: "
+                                  f"{len(fri_res['log_arities'])} rounds of arity 2, final polynomial of 1, "
+                                  "16-bit query proof of work, 100 queries with openings; transcript on the device",
+                      "ms": statistics.median(fri_ms), "samples_ms": [round(x, 3) for x in fri_ms]},
+        "fold": {"workload": "fold_matrix over BabyBear^4 (p3g_fold_matrix_bb4), arities 2/4/8: 2^19 values "
+                             "(config 3's quotient, L2-resident) and 2^25 values (512 MiB, HBM)",
+                 **fold, "hbm_frac_2^25_arity2": fold["2^25_arity2"]["gbs"] / peaks()[0]},
+        "pow_grind": {"workload": f"DuplexChallenger::grind, {grind_bits} bits, 4 challenger states "
+                                  "(0-3 pending inputs), Poseidon2-16",
+                      "candidates": grind_cand, "ms": grind_s * 1e3, "perms_per_s": grind_cand / grind_s,
+                      "frac_of_perm_peak": grind_cand / grind_s / perm_peak},
+    }
 
 
 def run_goldilocks(P, torch, ctx, dev, stream, steps: int, warmup: int, log_h: int = 18, width: int = 128,
@@ -182,8 +412,7 @@ def run_goldilocks(P, torch, ctx, dev, stream, steps: int, warmup: int, log_h: i
     LDE alone is timed beside it for its HBM roofline."""
     sptr = stream.cuda_stream
     h, H = 1 << log_h, 1 << (log_h + log_b)
-    rng = np.random.default_rng(2)
-    trace = rng.integers(0, GL_P, size=(h, width), dtype=np.uint64)
+    trace = np.random.default_rng(2).integers(0, GL_P, size=(h, width), dtype=np.uint64)
     d_trace = ctx.to_device(trace)
     ctx.sync()
 
@@ -191,30 +420,16 @@ def run_goldilocks(P, torch, ctx, dev, stream, steps: int, warmup: int, log_h: i
         ctx.commit_traces_device(P.GOLDILOCKS, [(d_trace.ptr, log_h, width, log_b, shift)], 0,
                                  stream=sptr).free(sptr)
 
-    def timed(fn, n):
-        evs = [torch.cuda.Event(enable_timing=True) for _ in range(n + 1)]
-        torch.cuda.synchronize(dev)
-        with torch.cuda.stream(stream):
-            for i in range(n):
-                evs[i].record(stream)
-                fn()
-            evs[-1].record(stream)
-        torch.cuda.synchronize(dev)
-        return [evs[i].elapsed_time(evs[i + 1]) for i in range(n)]
-
     for _ in range(warmup):
         step()
     l0 = P.kernel_launches()
-    st = timed(step, steps)
+    st = events_timed(torch, dev, stream, step, steps)
     launches = (P.kernel_launches() - l0) // max(steps, 1)
     d_lde = ctx.alloc(H * width * 8, sptr)
-
-    def lde():
-        ctx.coset_lde_device(P.GOLDILOCKS, d_trace.ptr, log_h, width, log_b, shift, True, d_lde.ptr, sptr)
-
+    lde = lambda: ctx.coset_lde_device(P.GOLDILOCKS, d_trace.ptr, log_h, width, log_b, shift, True, d_lde.ptr, sptr)
     for _ in range(2):
         lde()
-    lt = timed(lde, 10)
+    lt = events_timed(torch, dev, stream, lde, 10)
     d_lde.free(sptr)
     torch.cuda.synchronize(dev)
     d_trace.free()
@@ -222,11 +437,6 @@ def run_goldilocks(P, torch, ctx, dev, stream, steps: int, warmup: int, log_h: i
     lde_bytes = 8 * width * (h + H)
     hbm, src = peaks()
     perms = H * ((width + 3) // 4) + (H - 1)
-    traffic = None
-    tpath = os.path.join(REPO, "profiles", "traffic.json")
-    if os.path.exists(tpath):
-        with open(tpath) as f:
-            traffic = json.load(f).get(f"lde_gl_2p{log_h}x{width}_b{log_b}_bytes")
     return {
         "workload": f"plain single-trace Goldilocks commit: 2^{log_h} x {width} trace, log_blowup {log_b}, "
                     f"shift {shift}, bit-reversed LDE 2^{log_h + log_b} x {width}, Poseidon2-8 (x^7, 8+22) MMCS, "
@@ -236,107 +446,33 @@ def run_goldilocks(P, torch, ctx, dev, stream, steps: int, warmup: int, log_h: i
         "kernels_per_step": int(launches),
         "lde": {"ms": lde_ms, "algorithmic_bytes": lde_bytes, "achieved_gbs": lde_bytes / (lde_ms / 1e3) / 1e9,
                 "peak_gbs": hbm, "frac": lde_bytes / (lde_ms / 1e3) / 1e9 / hbm, "peak_source": src,
-                "traffic": traffic},
+                "traffic": traffic_of(f"lde_gl_2p{log_h}x{width}_b{log_b}_bytes")},
         "merkle": {"ms": ms - lde_ms, "perms": perms, "perms_per_s": perms / ((ms - lde_ms) / 1e3)},
     }
 
 
-def config3_shapes(seed: int = 3):
-    """64 BabyBear traces: log2 height uniform over {12..18}, width uniform in [8, 512]."""
-    rng = np.random.default_rng(seed)
-    return [(int(rng.integers(12, 19)), int(rng.integers(8, 513))) for _ in range(64)]
-
-
-def run_batched(P, torch, ctx, dev, stream, steps: int, warmup: int):
-    """Config 3: the 64-trace batch committed as one graph-captured plan (one
-    mixed-height MMCS) plus a fold of a 2^19-row BabyBear^4 quotient, against
-    the same work done per trace (one p3g_commit_traces per trace, then the
-    fold) on one stream.  Traces are generated on the device (seeded)."""
-    sptr = stream.cuda_stream
-    shapes = config3_shapes()
-    gen = torch.Generator(device=dev)
-    gen.manual_seed(3)
-    bufs = [torch.randint(0, BB_P, ((1 << lh) * w,), device=dev, dtype=torch.int64, generator=gen).to(torch.int32)
-            for lh, w in shapes]
-    fin = torch.randint(0, BB_P, ((1 << 19) * 4,), device=dev, dtype=torch.int64, generator=gen).to(torch.int32)
-    fout = torch.empty((1 << 18) * 4, device=dev, dtype=torch.int32)
-    beta = [int(x) for x in np.random.default_rng(4).integers(0, BB_P, 4)]
-    traces = [(b.data_ptr(), lh, w, 1, SHIFT) for b, (lh, w) in zip(bufs, shapes)]
-    elems = sum((1 << (lh + 1)) * w for lh, w in shapes)
-    torch.cuda.synchronize(dev)
-    t0 = time.perf_counter()
-    plan = P.Plan(ctx, P.BABYBEAR, traces, 0, fold=(fin.data_ptr(), fout.data_ptr(), 19, 1, beta), n_streams=0)
-    plan_s = time.perf_counter() - t0
-
-    def timed(fn, n):
-        evs = [torch.cuda.Event(enable_timing=True) for _ in range(n + 1)]
-        torch.cuda.synchronize(dev)
-        with torch.cuda.stream(stream):
-            for i in range(n):
-                evs[i].record(stream)
-                fn()
-            evs[-1].record(stream)
-        torch.cuda.synchronize(dev)
-        return [evs[i].elapsed_time(evs[i + 1]) for i in range(n)]
-
-    for _ in range(warmup):
-        plan.launch(sptr)
-    l0 = P.kernel_launches()
-    bt = timed(lambda: plan.launch(sptr), steps)
-    b_launches = (P.kernel_launches() - l0) // max(steps, 1)
-
-    def plain():
-        for tr in traces:
-            ctx.commit_traces_device(P.BABYBEAR, [tr], 0, stream=sptr).free(sptr)
-        ctx.fold_matrix_bb4_device(fin.data_ptr(), 19, 1, beta, fout.data_ptr(), stream=sptr)
-
-    for _ in range(warmup):
-        plain()
-    l0 = P.kernel_launches()
-    pt = timed(plain, steps)
-    p_launches = (P.kernel_launches() - l0) // max(steps, 1)
-    bms, pms = statistics.mean(bt), statistics.mean(pt)
-    out = {
-        "workload": "64 BabyBear traces, log2 h uniform in {12..18}, width uniform in [8, 512], log_blowup 1, "
-                    "one mixed-height Poseidon2-16 MMCS, plus fold_matrix of a 2^19-row BabyBear^4 quotient "
-                    "(log_arity 1, seeded beta)",
-        "lde_elements": elems,
-        "batched": {"value": elems / (bms / 1e3), "unit": UNIT, "ms_per_step": bms,
-                    "p50_ms": float(np.percentile(bt, 50)), "p99_ms": float(np.percentile(bt, 99)),
-                    "graph_launches_per_step": 1, "kernels_per_step": int(b_launches),
-                    "streams": plan.n_streams, "plan_seconds": plan_s},
-        "plain_per_trace": {"value": elems / (pms / 1e3), "unit": UNIT, "ms_per_step": pms,
-                            "p50_ms": float(np.percentile(pt, 50)), "p99_ms": float(np.percentile(pt, 99)),
-                            "kernels_per_step": int(p_launches)},
-        "batched_over_plain": pms / bms,
-    }
-    plan.destroy()
-    del bufs
-    return out
-
-
-def run_serving(P, torch, ctx, rates, per_rate: int, slots: int = 8):
+def run_serving(P, torch, ctx, rates, total: int, slots: int = 8):
     """Config 4: Poisson arrivals of commit+fold requests (log2 h uniform in
     {10..20}, width uniform in [4, 256], log_blowup in {1, 2, 3}) into the
     continuous-batching server; each completed request gets a 32-query
-    opening on its resident LDE/tree and is then released.  Latency is from
-    the scheduled arrival to the result; elements/s counts committed LDE
-    elements over the run.  Request payloads are prefixes of one pinned host
-    buffer of random BabyBear elements."""
-    import ctypes as C
-
+    opening on its resident LDE/tree and is then released.  `total` requests
+    are split evenly over the arrival rates.  Latency is from the scheduled
+    arrival to the result; elements/s counts committed LDE elements over the
+    run.  Request payloads are prefixes of one pinned host buffer of random
+    BabyBear elements."""
     max_elems = (1 << 20) * 256
     host = torch.randint(0, BB_P, (max_elems,), dtype=torch.int64).to(torch.int32).pin_memory()
     hptr = host.data_ptr()
     server = P.Server(ctx, max_slots=slots)
     out = []
     rid = 0
+    per = [total // len(rates) + (1 if k < total % len(rates) else 0) for k in range(len(rates))]
     try:
-        for lam in rates:
+        for lam, n_req in zip(rates, per):
             rng = np.random.default_rng(int(lam))
             reqs = []
             t = 0.0
-            for _ in range(per_rate):
+            for _ in range(n_req):
                 t += rng.exponential(1.0 / lam)
                 lh, w, lb = int(rng.integers(10, 21)), int(rng.integers(4, 257)), int(rng.integers(1, 4))
                 beta = [int(x) for x in rng.integers(0, BB_P, 4)]
@@ -380,12 +516,51 @@ def run_serving(P, torch, ctx, rates, per_rate: int, slots: int = 8):
     return {"workload": "Poisson commit+fold requests: log2 h uniform in {10..20}, width uniform in [4, 256], "
                         "log_blowup uniform in {1, 2, 3}; fold of the LDE's first four columns as BabyBear^4; "
                         "32-query opening on the resident tree, then release",
-            "slots": slots, "points": out}
+            "slots": slots, "requests": sum(per), "completed": sum(p["completed"] for p in out), "points": out}
 
 
+def run_case(args):
+    """One kernel sequence on its own, for profiling: `--case
+    lde|commit:bb|gl:LOG_H:WIDTH:LOG_B` runs the coset LDE (bit-reversed rows)
+    or the whole commit of one seeded trace, `warmup` untimed and `steps` timed
+    calls (CUDA events), and prints their mean."""
+    import torch
+    import p3g_gb300 as P
+
+    kind, field, log_h, width, log_b = args.case.split(":")
+    log_h, width, log_b = int(log_h), int(width), int(log_b)
+    gl = field == "gl"
+    fid, shift = (P.GOLDILOCKS, 7) if gl else (P.BABYBEAR, SHIFT)
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(0)
+    stream = torch.cuda.Stream(device=dev)
+    sptr = stream.cuda_stream
+    ctx = P.Context(0)
+    ctx.set_default_poseidon2()
+    rng = np.random.default_rng(11)
+    t = rng.integers(0, GL_P if gl else BB_P, size=(1 << log_h, width), dtype=np.uint64 if gl else np.uint32)
+    d_t = ctx.to_device(t)
+    H = 1 << (log_h + log_b)
+    d_out = ctx.alloc(H * width * t.itemsize)
+    ctx.sync()
+    if kind == "lde":
+        fn = lambda: ctx.coset_lde_device(fid, d_t.ptr, log_h, width, log_b, shift, True, d_out.ptr, sptr)
+    else:
+        fn = lambda: ctx.commit_traces_device(fid, [(d_t.ptr, log_h, width, log_b, shift)], 0, stream=sptr).free(sptr)
+    for _ in range(args.warmup):
+        fn()
+    ms = statistics.mean(events_timed(torch, dev, stream, fn, args.steps))
+    nbytes = t.itemsize * width * ((1 << log_h) + H)
+    print(json.dumps({"case": args.case, "ms": ms, "lde_elements_per_s": H * width / (ms / 1e3),
+                      "algorithmic_gbs": nbytes / (ms / 1e3) / 1e9 if kind == "lde" else None}))
+    d_out.free()
+    d_t.free()
+    ctx.close()
+    return 0
+
+
+# ------------------------------------------------------------------ headline
 def run_ours(args):
-    import ctypes as C
-
     import torch
     import p3g_gb300 as P
 
@@ -397,27 +572,28 @@ def run_ours(args):
     dev = torch.device("cuda", local)
     stream = torch.cuda.Stream(device=dev)
     sptr = stream.cuda_stream
-
     ctx = P.Context(local)
     ctx.set_default_poseidon2()
-    LOG_H, WIDTH = args.log_h, args.width
-    h, H = 1 << LOG_H, 1 << (LOG_H + LOG_B)
-    elems = H * WIDTH
-    rng = np.random.default_rng(1234 + rank)
-    trace = rng.integers(0, BB_P, size=(h, WIDTH), dtype=np.uint32)
-    d_trace = ctx.to_device(trace)
-    ctx.sync()
 
-    def step(cap_out=None):
-        tree = ctx.commit_traces_device(P.BABYBEAR, [(d_trace.ptr, LOG_H, WIDTH, LOG_B, SHIFT)], 0,
-                                        stream=sptr, cap_out=cap_out)
-        tree.free(sptr)
+    # ---- config 3 inputs (host, seeded), device copies for the resident-trace runs
+    shapes, traces, fold_in, beta = config3_inputs(3, args.c3_shrink)
+    fold_log = C3_FOLD_LOG - args.c3_shrink
+    elems = sum((1 << (lh + C3_LOG_B)) * w for lh, w in shapes)
+    trace_bytes = sum(t.nbytes for t in traces)
+    d_traces = [ctx.to_device(t) for t in traces]
+    d_fin = ctx.to_device(fold_in)
+    d_fout = ctx.alloc((1 << (fold_log - 1)) * 16)
+    ctx.sync()
+    dtr = [(b.ptr, lh, w, C3_LOG_B, SHIFT) for b, (lh, w) in zip(d_traces, shapes)]
+    t0 = time.perf_counter()
+    plan = P.Plan(ctx, P.BABYBEAR, dtr, 0, fold=(d_fin.ptr, d_fout.ptr, fold_log, 1, beta), n_streams=0)
+    plan_s = time.perf_counter() - t0
 
     for _ in range(max(args.warmup, 1)):
-        step()
+        plan.launch(sptr)
     torch.cuda.synchronize(dev)
 
-    # ---- device-timed region (trace resident in HBM)
+    # ---- device-timed region: K launches of the batched plan
     evs = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
     if ws > 1:
         torch.distributed.barrier()
@@ -429,7 +605,7 @@ def run_ours(args):
         with torch.cuda.stream(stream):
             for i in range(args.steps):
                 evs[i].record(stream)
-                step()
+                plan.launch(sptr)
             evs[-1].record(stream)
         torch.cuda.synchronize(dev)
     gc.enable()
@@ -438,219 +614,147 @@ def run_ours(args):
     total_ms = evs[0].elapsed_time(evs[-1])
     value, total_ms = job_throughput(float(elems) * args.steps, total_ms, dev)
     ms_per_step = total_ms / args.steps
+    clocks = clk.summary()
 
-    # ---- stage breakdown: the LDE alone (roofline) -- same stream, CUDA events
-    d_lde = ctx.alloc(elems * 4, sptr)
-    reps = 10
-    for _ in range(2):
-        ctx.coset_lde_device(P.BABYBEAR, d_trace.ptr, LOG_H, WIDTH, LOG_B, SHIFT, True, d_lde.ptr, sptr)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize(dev)
-    e0.record(stream)
-    for _ in range(reps):
-        ctx.coset_lde_device(P.BABYBEAR, d_trace.ptr, LOG_H, WIDTH, LOG_B, SHIFT, True, d_lde.ptr, sptr)
-    e1.record(stream)
-    torch.cuda.synchronize(dev)
-    lde_ms = e0.elapsed_time(e1) / reps
-    d_lde.free(sptr)
-    torch.cuda.synchronize(dev)
+    # ---- the same work as plain per-trace commits (one call per trace, then the fold)
+    plain = None
+    if not args.no_plain:
+        def plain_step():
+            for tr in dtr:
+                ctx.commit_traces_device(P.BABYBEAR, [tr], 0, stream=sptr).free(sptr)
+            ctx.fold_matrix_bb4_device(d_fin.ptr, fold_log, 1, beta, d_fout.ptr, stream=sptr)
 
-    # ---- end to end through the C ABI with the trace in pinned host memory:
-    # p3g_commit_traces_host copies column chunks on a second stream while the
-    # earlier chunks' LDEs and row hashes run; the root read-back synchronises
-    # the stream
-    pinned = torch.empty(h * WIDTH, dtype=torch.int32, pin_memory=True)
-    pinned.numpy().view(np.uint32)[:] = trace.reshape(-1)
-    cap = np.zeros((1, 8), np.uint32)
+        for _ in range(max(args.warmup, 1)):
+            plain_step()
+        l1 = P.kernel_launches()
+        pt = events_timed(torch, dev, stream, plain_step, args.steps)
+        p_launches = (P.kernel_launches() - l1) // max(args.steps, 1)
+        pms = statistics.mean(pt)
+        plain = {"value": elems / (pms / 1e3), "unit": UNIT, "ms_per_step": pms,
+                 "p50_ms": float(np.percentile(pt, 50)), "p99_ms": float(np.percentile(pt, 99)),
+                 "kernels_per_step": int(p_launches),
+                 "call": "p3g_commit_traces once per trace, then p3g_fold_matrix_bb4, one stream"}
+
+    # ---- LDE stage of the headline workload alone (roofline): the 64 LDEs on
+    # one stream into the plan's own LDE buffers, CUDA events
+    def ldes():
+        for i, (lh, w) in enumerate(shapes):
+            ctx.coset_lde_device(P.BABYBEAR, d_traces[i].ptr, lh, w, C3_LOG_B, SHIFT, True, plan.tree.leaf_ptr(i), sptr)
+
+    ldes()
+    lde_ms = statistics.mean(events_timed(torch, dev, stream, ldes, 5))
+    # restore the plan's commitment inputs (the same values) and check the root is unchanged
+    root_dev = plan.tree.layers()[-1].copy()
+
+    # ---- end to end: the host-input plan, traces and quotient in pinned host memory
+    pinned = [pinned_copy(torch, t) for t in traces]
+    pin_fold = pinned_copy(torch, fold_in)
+    htr = [(pt_.data_ptr(), lh, w, C3_LOG_B, SHIFT) for pt_, (lh, w) in zip(pinned, shapes)]
+    plan_h = P.Plan(ctx, P.BABYBEAR, htr, 0, fold=(pin_fold.data_ptr(), d_fout.ptr, fold_log, 1, beta),
+                    n_streams=0, host=True)
+    nlayers = len(plan_h.tree.info()[0])
+    root_ptr = plan_h.tree.layer_ptr(nlayers - 1)
+    root = np.zeros(8, np.uint32)
+    fold_out = np.zeros((1 << (fold_log - 1), 4), np.uint32)
+    lib = P.load()
     e2e_ms = []
     gc.collect()
     gc.disable()  # the interpreter's collector paused in the timed loop, as the timeit module does
     for i in range(args.warmup + args.steps):
         t0 = time.perf_counter()
-        tree = ctx.commit_traces_host(P.BABYBEAR, [(pinned.data_ptr(), LOG_H, WIDTH, LOG_B, SHIFT)], 0,
-                                      stream=sptr, cap_out=cap)
-        tree.free(sptr)
-        dt = (time.perf_counter() - t0) * 1e3
+        plan_h.launch(sptr)
+        P.check(lib.p3g_memcpy_d2h(ctx.handle, root.ctypes.data, root_ptr, 32, sptr))
+        P.check(lib.p3g_memcpy_d2h(ctx.handle, fold_out.ctypes.data, d_fout.ptr, fold_out.nbytes, sptr))
         if i >= args.warmup:
-            e2e_ms.append(dt)
+            e2e_ms.append((time.perf_counter() - t0) * 1e3)
     gc.enable()
     torch.cuda.synchronize(dev)
+    assert np.array_equal(root, root_dev[0]), "host-input plan and device plan commit differently"
     e2e_value, e2e_mean = job_throughput(float(elems), statistics.mean(e2e_ms), dev)
-
-    prover = {}
-    if not args.no_prover:
-        # ---- PCS open on the commit's resident bit-reversed LDE (2^21 x 256):
-        # opened values at 2 points and the reduced opening into a q vector
-        tree = ctx.commit_traces_device(P.BABYBEAR, [(d_trace.ptr, LOG_H, WIDTH, LOG_B, SHIFT)], 0, stream=sptr)
-        log_n = LOG_H + LOG_B
-        pts = rng.integers(0, BB_P, size=(2, 4), dtype=np.uint32)
-        alpha = rng.integers(0, BB_P, size=4, dtype=np.uint32)
-        d_q = ctx.alloc(H * 16, sptr)
-        ov = ctx.pcs_open_values_device(tree.leaf_ptr(0), log_n, WIDTH, True, SHIFT, pts, stream=sptr)
-        ctx.pcs_reduce_device(tree.leaf_ptr(0), log_n, WIDTH, True, SHIFT, pts, ov, alpha, 0, True, d_q.ptr, sptr)
-        torch.cuda.synchronize(dev)
-        open_reps = 5
-        e0.record(stream)
-        for _ in range(open_reps):
-            ctx.pcs_open_values_device(tree.leaf_ptr(0), log_n, WIDTH, True, SHIFT, pts, stream=sptr)
-        e1.record(stream)
-        torch.cuda.synchronize(dev)
-        open_ms = e0.elapsed_time(e1) / open_reps
-        e0.record(stream)
-        for _ in range(open_reps):
-            ctx.pcs_reduce_device(tree.leaf_ptr(0), log_n, WIDTH, True, SHIFT, pts, ov, alpha, 0, True, d_q.ptr, sptr)
-        e1.record(stream)
-        torch.cuda.synchronize(dev)
-        reduce_ms = e0.elapsed_time(e1) / open_reps
-        # ---- prove_fri on that reduced opening (2^21 BabyBear^4), transcript on the
-        # device: commit-phase rounds, final polynomial, 16-bit query proof of work,
-        # 100 query indices and every round's openings (host clock; the call synchronises)
-        fri_params = dict(log_blowup=LOG_B, log_final_poly_len=0, max_log_arity=1, num_queries=100,
-                          commit_proof_of_work_bits=0, query_proof_of_work_bits=16)
-        st0 = rng.integers(0, BB_P, size=16, dtype=np.uint32)
-        ctx.fri_prove_device([(d_q.ptr, log_n)], fri_params, st0, [], [], stream=sptr)
-        fri_ms = []
-        for _ in range(3):
-            t0 = time.perf_counter()
-            fri_res = ctx.fri_prove_device([(d_q.ptr, log_n)], fri_params, st0, [], [], stream=sptr)
-            fri_ms.append((time.perf_counter() - t0) * 1e3)
-        d_q.free(sptr)
-        tree.free(sptr)
-        torch.cuda.synchronize(dev)
-
-        # ---- FRI fold (p3g_fold_matrix_bb4): the config-3 quotient size (2^19
-        # BabyBear^4, L2-resident) and a 2^25-value vector (512 MiB in, larger
-        # than L2) for the HBM roofline; CUDA events on the stream
-        fold = {}
-        for log_f in (19, 25):
-            d_in = ctx.to_device(rng.integers(0, BB_P, size=(1 << log_f, 4), dtype=np.uint32))
-            d_out = ctx.alloc((1 << log_f) * 16 // 2, sptr)
-            beta_f = rng.integers(0, BB_P, size=4, dtype=np.uint32)
-            for la in (1, 2, 3):
-                ctx.fold_matrix_bb4_device(d_in.ptr, log_f, la, beta_f, d_out.ptr, sptr)
-                torch.cuda.synchronize(dev)
-                e0.record(stream)
-                for _ in range(reps):
-                    ctx.fold_matrix_bb4_device(d_in.ptr, log_f, la, beta_f, d_out.ptr, sptr)
-                e1.record(stream)
-                torch.cuda.synchronize(dev)
-                ms = e0.elapsed_time(e1) / reps
-                nbytes = 16 * ((1 << log_f) + ((1 << log_f) >> la))
-                fold[f"2^{log_f}_arity{1 << la}"] = {"ms": ms, "algorithmic_bytes": nbytes,
-                                                     "gbs": nbytes / (ms / 1e3) / 1e9}
-            d_out.free(sptr)
-            d_in.free()
-        torch.cuda.synchronize(dev)
+    e2e_streams = plan_h.n_streams
+    plan_h.destroy()
+    del pinned, pin_fold
+    kernels_per_step = plan.kernels_per_launch
+    n_streams = plan.n_streams
+    plan.destroy()
+    for b in d_traces:
+        b.free()
+    d_fin.free()
+    d_fout.free()
+    torch.cuda.synchronize(dev)
 
     # ---- permutation ceiling: the same Poseidon2-16 on 2^22 register-resident
     # states (p3g_poseidon2_permute), no sponge or tree around it
+    rng = np.random.default_rng(9)
     n_states = 1 << 22
     d_states = ctx.to_device(rng.integers(0, BB_P, size=(n_states, 16), dtype=np.uint32))
     perm_once = lambda: P.check(P.load().p3g_poseidon2_permute(ctx.handle, P.BABYBEAR, d_states.ptr, n_states, sptr))
-    for _ in range(2):
-        perm_once()
-    torch.cuda.synchronize(dev)
-    e0.record(stream)
-    for _ in range(reps):
-        perm_once()
-    e1.record(stream)
-    torch.cuda.synchronize(dev)
-    perm_peak = n_states / (e0.elapsed_time(e1) / reps / 1e3)
+    perm_once()
+    perm_peak = n_states / (statistics.mean(events_timed(torch, dev, stream, perm_once, 10)) / 1e3)
     d_states.free()
 
-    if not args.no_prover:
-        # ---- proof-of-work search (DuplexChallenger::grind, p3g_grind) at 26 bits
-        # from 4 random challenger states: candidates searched per second, host
-        # clock around each call (the call synchronises)
-        grind_bits, grind_cand, grind_s = 26, 0, 0.0
-        ctx.grind(P.BABYBEAR, np.zeros(16, np.uint32), [], 8, stream=sptr)
-        for k in range(4):
-            st = rng.integers(0, BB_P, size=16, dtype=np.uint32)
-            t0 = time.perf_counter()
-            w = ctx.grind(P.BABYBEAR, st, [int(x) for x in st[:k]], grind_bits, stream=sptr)
-            grind_s += time.perf_counter() - t0
-            grind_cand += w + 1
-
-    if not args.no_prover:
-        prover = {
-            "pcs_open": {"workload": f"TwoAdicFriPcs::open passes on the resident bit-reversed LDE 2^{LOG_H + LOG_B} x "
-                                     f"{WIDTH}, 2 BabyBear^4 points",
-                         "open_values_ms": open_ms, "reduce_ms": reduce_ms,
-                         "lde_bytes": elems * 4,
-                         "open_values_gbs": elems * 4 / (open_ms / 1e3) / 1e9,
-                         "reduce_gbs": elems * 4 / (reduce_ms / 1e3) / 1e9},
-            "fri_prove": {"workload": f"prove_fri over the 2^{log_n} BabyBear^4 reduced opening above: "
-                                      f"{len(fri_res['log_arities'])} rounds of arity 2, final polynomial of 1, "
-                                      "16-bit query proof of work, 100 queries with openings; transcript on the device",
-                          "ms": statistics.median(fri_ms), "samples_ms": [round(x, 3) for x in fri_ms]},
-            "fold": {"workload": "fold_matrix over BabyBear^4 (p3g_fold_matrix_bb4), arities 2/4/8: 2^19 values "
-                                 "(config 3's quotient, L2-resident) and 2^25 values (512 MiB, HBM)",
-                     **fold, "hbm_frac_2^25_arity2": fold["2^25_arity2"]["gbs"] / peaks()[0]},
-            "pow_grind": {"workload": f"DuplexChallenger::grind, {grind_bits} bits, 4 challenger states "
-                                      "(0-3 pending inputs), Poseidon2-16",
-                          "candidates": grind_cand, "ms": grind_s * 1e3,
-                          "perms_per_s": grind_cand / grind_s,
-                          "frac_of_perm_peak": grind_cand / grind_s / perm_peak},
-        }
     hbm, src = peaks()
-    lde_bytes = 4 * WIDTH * (h + H)
+    lde_bytes = sum(4 * w * ((1 << lh) + (1 << (lh + C3_LOG_B))) for lh, w in shapes)
     lde_gbs = lde_bytes / (lde_ms / 1e3) / 1e9
-    traffic = None
-    tpath = os.path.join(REPO, "profiles", "traffic.json")
-    if os.path.exists(tpath):
-        with open(tpath) as f:
-            traffic = json.load(f).get(f"lde_bb_2p{LOG_H}x{WIDTH}_b{LOG_B}_bytes")
-    perms = H * ((WIDTH + 7) // 8) + (H - 1)
-    hash_ms = ms_per_step - lde_ms
+    bfly = lde_butterflies(shapes, C3_LOG_B)
+    perms = sum((1 << (lh + C3_LOG_B)) * ((w + 7) // 8) for lh, w in shapes)
     result = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step,
         "p50_ms": float(np.percentile(step_ms, 50)), "p99_ms": float(np.percentile(step_ms, 99)),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32 (BabyBear)",
         "data": "synthetic",
-        "config": {"workload": f"plain single-trace BabyBear commit: 2^{LOG_H} x {WIDTH} trace, log_blowup {LOG_B}, "
-                               f"shift {SHIFT}, bit-reversed LDE 2^{LOG_H + LOG_B} x {WIDTH}, Poseidon2-16 "
-                               "(x^7, 8+13) MMCS, cap_height 0",
-                   "trace_rows": h, "trace_cols": WIDTH, "lde_rows": H, "field": "BabyBear",
-                   "l2": (f"inputs larger than L2 ({h * WIDTH * 4 / 2**20:.0f} MiB trace, "
-                          f"{elems * 4 / 2**20:.0f} MiB LDE); no flush") if h * WIDTH * 4 > 129e6
+        "config": {"workload": "config 3: batched commit of 64 BabyBear traces (log2 h uniform in {12..18}, width "
+                               "uniform in [8, 512], log_blowup 1, shift 31, seeded) as one mixed-height "
+                               "Poseidon2-16 (x^7, 8+13) MMCS, plus fold_matrix of a 2^19-row BabyBear^4 quotient "
+                               "(log_arity 1, seeded beta), one CUDA graph launch per step",
+                   "traces": 64, "lde_elements": elems, "trace_bytes": trace_bytes,
+                   "height_shrink": args.c3_shrink,
+                   "l2": (f"inputs larger than L2 ({trace_bytes / 2**20:.0f} MiB of traces, "
+                          f"{elems * 4 / 2**20:.0f} MiB of LDEs); no flush") if trace_bytes > 129e6
                          else "inputs smaller than L2 (profiling case)",
                    "parallelism": f"replicas x{ws}"},
+        "batched": {"graph_launches_per_step": 1, "kernels_per_step": int(kernels_per_step), "streams": n_streams,
+                    "plan_seconds": plan_s},
+        "plain_per_trace": plain,
+        "batched_over_plain": (plain["ms_per_step"] / ms_per_step) if plain else None,
+        "batched_over_plain_target": 2.0,
         "python_gc": "collected before, paused during the timed loops (as the timeit module does)",
         "e2e": {"value": e2e_value, "unit": UNIT,
-                "h2d_bytes_per_step": h * WIDTH * 4, "d2h_bytes_per_step": 32,
+                "h2d_bytes_per_step": trace_bytes + fold_in.nbytes, "d2h_bytes_per_step": 32 + fold_out.nbytes,
                 "p50_ms": float(np.percentile(e2e_ms, 50)), "p99_ms": float(np.percentile(e2e_ms, 99)),
-                "samples_ms": [round(x, 3) for x in e2e_ms],
-                "call": "p3g_commit_traces_host (pinned host trace, root read back)"},
+                "samples_ms": [round(x, 3) for x in e2e_ms], "streams": e2e_streams,
+                "call": "p3g_plan_launch of a p3g_plan_commit_host plan (64 pinned host traces and the quotient "
+                        "copied in by the graph), root and fold output read back"},
         "gpu_launches": int(launches),
-        "clocks": clk.summary(),
-        "roofline": {"kernel": "coset LDE (3 passes, k_lde_pass1/2/3)", "bound": "hbm", "achieved": lde_gbs,
-                     "peak": hbm, "unit": "GB/s", "frac": lde_gbs / hbm, "traffic": traffic,
-                     "peak_source": src, "algorithmic_bytes": lde_bytes, "ms": lde_ms},
-        "stages": {"lde_ms": lde_ms, "merkle_ms": hash_ms, "perms": perms,
-                   "perms_per_s": perms / (hash_ms / 1e3) if hash_ms > 0 else None},
-        "hash_roofline": {"kernel": "Merkle stage (k_hash_groups leaf sponge + k_compress_level)",
-                          "bound": "integer multiply pipe (permutation issue)",
-                          "achieved": perms / (hash_ms / 1e3) if hash_ms > 0 else None, "unit": "perms/s",
-                          "peak": perm_peak,
-                          "peak_source": "isolated Poseidon2-16 permutation throughput, same run",
-                          "frac": perms / (hash_ms / 1e3) / perm_peak if hash_ms > 0 else None},
+        "clocks": clocks,
+        "roofline": {"kernel": "coset LDE stage of the 64 traces (k_lde_pass1/2/3, one stream)", "bound": "hbm",
+                     "achieved": lde_gbs, "peak": hbm, "unit": "GB/s", "frac": lde_gbs / hbm,
+                     "traffic": traffic_of("lde_bb_config3_bytes"), "peak_source": src,
+                     "algorithmic_bytes": lde_bytes, "ms": lde_ms},
+        "issue_bound_ms": {"lde": issue_bound_ms(bfly, clocks.get("sm_mhz")), "butterflies": bfly,
+                           "basis": "6 ALU-pipe instructions per radix-2 butterfly, 16 lanes per SMSP per clock, "
+                                    "608 SMSPs at the sampled SM clock"},
+        "stages": {"lde_ms": lde_ms, "leaf_perms": perms, "perm_peak_per_s": perm_peak,
+                   "leaf_hash_ms_at_perm_peak": perms / perm_peak * 1e3},
     }
-    result.update(prover)
+    if not args.no_config1:
+        result["config1"] = run_config1(P, torch, ctx, dev, stream, max(3, args.steps // 2), args.warmup,
+                                        args.log_h, args.width, perm_peak)
+    if not args.no_prover:
+        result.update(run_prover(P, torch, ctx, dev, stream, perm_peak))
     if not args.no_goldilocks:
         result["config2"] = run_goldilocks(P, torch, ctx, dev, stream, max(3, args.steps // 2), args.warmup)
-    if not args.no_batched:
-        result["config3"] = run_batched(P, torch, ctx, dev, stream, max(3, args.steps // 2), args.warmup)
     if not args.no_serving:
         result["config4"] = run_serving(P, torch, ctx, [50, 100, 200, 500, 1000, 2000], args.serving_requests)
     if rank == 0 and not args.no_cpu:
-        v, dt, desc = cpu_sample(os.cpu_count() or 1)
-        v1, dt1, desc1 = cpu_sample(1, 12)
-        result["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
-                                  "sample": desc, "seconds": dt,
+        nt = os.cpu_count() or 1
+        v, dt, desc = cpu_sample(nt, args.ref_shrink - 1)
+        v1, dt1, desc1 = cpu_sample(1, 8)
+        result["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": nt, "kind": "port", "sample": desc,
+                                  "seconds": dt,
                                   "single_thread": {"value": v1, "cores": 1, "sample": desc1, "seconds": dt1,
                                                     "note": "the reference's own CPU path is single-threaded"}}
-    d_trace.free()
     ctx.close()
     if rank == 0:
         print(json.dumps(result))
@@ -666,17 +770,26 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-plain", action="store_true", help="skip the per-trace comparison of the batched workload")
+    ap.add_argument("--no-config1", action="store_true", help="skip the 2^20 x 256 single-trace commit")
     ap.add_argument("--no-goldilocks", action="store_true", help="skip the Goldilocks 2^18 x 128 commit")
-    ap.add_argument("--no-batched", action="store_true", help="skip the 64-trace batched comparison")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop latency sweep")
     ap.add_argument("--no-prover", action="store_true",
                     help="skip the PCS-open, FRI and proof-of-work measurements (profiling the commit alone)")
-    ap.add_argument("--serving-requests", type=int, default=200, help="requests per arrival rate")
-    ap.add_argument("--log-h", type=int, default=LOG_H, help="trace log2 height (profiling cases)")
-    ap.add_argument("--width", type=int, default=WIDTH, help="trace width (profiling cases)")
+    ap.add_argument("--serving-requests", type=int, default=10000, help="requests over the whole rate sweep")
+    ap.add_argument("--c3-shrink", type=int, default=0,
+                    help="divide every config-3 height by 2^k (profiling cases)")
+    ap.add_argument("--ref-shrink", type=int, default=4,
+                    help="the reference arm's CPU sample: config-3 heights divided by 2^k (the all-core "
+                         "baseline of the GPU arm uses 2^(k-1))")
+    ap.add_argument("--log-h", type=int, default=C1_LOG_H, help="config-1 trace log2 height (profiling cases)")
+    ap.add_argument("--width", type=int, default=C1_WIDTH, help="config-1 trace width (profiling cases)")
+    ap.add_argument("--case", default="", help="profiling: lde|commit:bb|gl:LOG_H:WIDTH:LOG_B alone")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.case:
+        return run_case(args)
     return run_ours(args)
 
 

@@ -147,7 +147,9 @@ P3G_API int p3g_dft(p3g_ctx *ctx, int field, int kind, const void *d_in, uint32_
  * about (1 << log_h) * width <= 4M elements).  The first call on a device
  * sets the arrays up (address lookup, synchronous table copy) with that
  * device current: make it before any stream capture.  All calls share the
- * array, so calls that overlap on the GPU race; serialise them. */
+ * array, so calls that overlap on the GPU race; serialise them.  Arguments
+ * as for p3g_coset_lde: shift canonical (below p) and non-zero, width up to
+ * 2^24, log_h up to 21. */
 P3G_API int p3g_coset_lde_bb_noalloc(const void *d_in, uint32_t log_h, uint32_t width,
                                      uint32_t log_blowup, uint32_t shift, int bitrev_out,
                                      void *d_out, void *stream);
@@ -251,6 +253,17 @@ typedef struct {
 P3G_API int p3g_plan_commit(p3g_ctx *ctx, int field, const p3g_trace *traces, size_t n_traces,
                             uint32_t cap_height, const p3g_fold_job *fold, uint32_t n_streams,
                             p3g_plan **plan_out);
+/* p3g_plan_commit with every input in pinned HOST memory: each trace's
+ * d_trace and the fold's d_in are page-locked host pointers (cudaMallocHost or
+ * cudaHostRegister; P3G_EINVAL otherwise), read on every launch.  The graph
+ * copies them into device buffers the plan owns, on a copy stream, in the
+ * order the LDE streams take the traces, and each LDE waits only for its own
+ * trace, so the copies overlap the LDEs of the traces copied before.  The
+ * fold's d_out stays a device pointer.  The end-to-end form of the batched
+ * commit: host data in, commitment (p3g_plan_info's tree) out. */
+P3G_API int p3g_plan_commit_host(p3g_ctx *ctx, int field, const p3g_trace *traces, size_t n_traces,
+                                 uint32_t cap_height, const p3g_fold_job *fold, uint32_t n_streams,
+                                 p3g_plan **plan_out);
 /* Replays the plan's graph on `stream` (one cudaGraphLaunch). */
 P3G_API int p3g_plan_launch(p3g_ctx *ctx, p3g_plan *plan, void *stream);
 /* The plan's tree (use with p3g_tree_info/_layer_ptr/_leaf_ptr/p3g_mmcs_open_batch;
@@ -291,9 +304,9 @@ typedef struct {
  * arrive while others run overlap on the device.  Each request: host->device
  * copy, coset LDE (bit-reversed rows), Poseidon2 MMCS commit, and fold_matrix
  * (log_arity 1) of the LDE's first four columns read as BabyBear^4 values.  The
- * LDE and tree stay resident (and count against the budget) until
- * p3g_server_release; p3g_server_open serves MerkleTreeMmcs::open_batch
- * queries on them.  The reference has no serving layer; this mirrors its
+ * LDE, tree and folded vector stay resident (and count against the budget)
+ * until p3g_server_release; p3g_server_open serves MerkleTreeMmcs::open_batch
+ * queries on them and p3g_server_read_fold copies the folded vector out.  The reference has no serving layer; this mirrors its
  * commit (merkle_tree_mmcs.hpp:100-107), open_batch (:120-152) and
  * fold_matrix (fri_folding.hpp:200) per request. */
 P3G_API int p3g_server_create(p3g_ctx *ctx, uint32_t max_slots, uint64_t mem_budget_bytes,
@@ -305,6 +318,10 @@ P3G_API int p3g_server_pending(p3g_server *server, uint64_t *queued, uint64_t *i
                                uint64_t *resident, uint64_t *bytes_used);
 P3G_API int p3g_server_open(p3g_server *server, uint64_t id, const uint64_t *h_indices,
                             size_t n_queries, void *h_rows, void *h_proof);
+/* The resident fold output of a completed request: n_values = H / 2 BabyBear^4
+ * values (4 canonical u32 each, H = 2^(log_h + log_blowup)) into h_out, in
+ * fold_matrix's output order.  Synchronous. */
+P3G_API int p3g_server_read_fold(p3g_server *server, uint64_t id, void *h_out, uint64_t n_values);
 P3G_API int p3g_server_release(p3g_server *server, uint64_t id);
 /* Stops the worker; queued requests are dropped, in-flight ones are waited for. */
 P3G_API int p3g_server_destroy(p3g_server *server);

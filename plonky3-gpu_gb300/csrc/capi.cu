@@ -457,27 +457,36 @@ int p3g_commit_traces(p3g_ctx* ctx, int field, const p3g_trace* traces, size_t n
     auto t = std::make_unique<p3g_tree>();
     t->field = field;
     const size_t esz = field == P3G_BABYBEAR ? 4 : 8;
+    // traces of one shape run as one batch (one launch per LDE pass)
+    std::vector<p3g::LdeGroup> groups;
     try {
+        std::vector<const void*> in(n_traces);
         for (size_t i = 0; i < n_traces; ++i) {
             const p3g_trace& tr = traces[i];
             P3G_REQUIRE(tr.width == 0 || tr.d_trace, "commit_traces: null trace");
+            P3G_REQUIRE(tr.shift < (field == P3G_BABYBEAR ? uint64_t(p3g::bb::P) : p3g::gl::P),
+                        "commit_traces: shift must be canonical");
+            P3G_REQUIRE(tr.log_h + tr.log_blowup <= (field == P3G_BABYBEAR ? 27u : 32u),
+                        "commit_traces: log_h + log_blowup exceeds two-adicity");
+            if (tr.log_h > 26) throw p3g::Error(P3G_EUNSUPPORTED, "commit_traces: log_h > 26 is not supported");
+            P3G_REQUIRE(tr.shift % (field == P3G_BABYBEAR ? uint64_t(p3g::bb::P) : p3g::gl::P) != 0,
+                        "commit_traces: shift must be non-zero");
             const uint64_t H = uint64_t(1) << (tr.log_h + tr.log_blowup);
             void* lde = ctx->alloc(esz * H * tr.width, st);
             t->owned.push_back(lde);
-            if (field == P3G_BABYBEAR) {
-                P3G_REQUIRE(tr.shift < p3g::bb::P, "commit_traces: shift must be canonical");
-                p3g::lde_bb(ctx, static_cast<const uint32_t*>(tr.d_trace), int(tr.log_h), int(tr.width),
-                            int(tr.log_blowup), uint32_t(tr.shift), 1, static_cast<uint32_t*>(lde), st);
-            } else {
-                P3G_REQUIRE(tr.shift < p3g::gl::P, "commit_traces: shift must be canonical");
-                p3g::lde_gl(ctx, static_cast<const uint64_t*>(tr.d_trace), int(tr.log_h), int(tr.width),
-                            int(tr.log_blowup), tr.shift, 1, static_cast<uint64_t*>(lde), st);
-            }
             t->mats.push_back(p3g_matrix{lde, H, tr.width, 0});
+            in[i] = tr.d_trace;
+        }
+        groups = p3g::lde_groups(traces, n_traces);
+        for (auto& gr : groups) {
+            p3g::lde_group_prepare(ctx, field, gr, traces, st);
+            p3g::lde_group_run(ctx, field, gr, traces, in.data(), t->owned.data(), st);
+            p3g::lde_group_release(ctx, gr, st);
         }
         p3g::mmcs_build(ctx, t.get(), cap_height, st);
         copy_cap(t.get(), h_cap_out, st);
     } catch (...) {
+        for (auto& gr : groups) p3g::lde_group_release(ctx, gr, st);
         p3g::tree_release(ctx, t.get(), st);
         throw;
     }

@@ -108,7 +108,7 @@ k_dft_single(const typename F::T* __restrict__ in, typename F::T* __restrict__ o
     TW* pre = tw + N;
     TW* post = pre + N;
     const int tid = threadIdx.x, c = tid % C, t = tid / C;
-    const int col = blockIdx.y * C + c;
+    const int col = tile_coord<C>(w).ct * C + c;
     const bool ok = col < w;
     for (int e = tid; e < N; e += NT) {
         tw[e] = gtw ? gtw[e] : F::tw_from_const(INV ? roots.omega_inv(LOGN, e) : roots.omega(LOGN, e));
@@ -138,9 +138,10 @@ k_dft_pass_a(const typename F::T* __restrict__ in, typename F::T* __restrict__ m
     TW* pre = tw + N;
     TW* post = pre + N;
     const int tid = threadIdx.x, c = tid % C, t = tid / C;
-    const int col = blockIdx.y * C + c;
+    const TileCoord tc_ = tile_coord<C>(w);
+    const int col = tc_.ct * C + c;
     const bool ok = col < w;
-    const int64_t k2 = blockIdx.x;
+    const int64_t k2 = tc_.blk;
     const int64_t N2 = int64_t(1) << n2;
     const int n = LOGN + n2;
     const T sk2 = sq[k2];
@@ -174,9 +175,10 @@ k_dft_pass_b(const typename F::T* src, typename F::T* out, int w, int n1, int bi
     TW* tw = reinterpret_cast<TW*>(A + SH::TILE);
     TW* post = tw + N;
     const int tid = threadIdx.x, c = tid % C, t = tid / C;
-    const int col = blockIdx.y * C + c;
+    const TileCoord tc_ = tile_coord<C>(w);
+    const int col = tc_.ct * C + c;
     const bool ok = col < w;
-    const int64_t base = int64_t(blockIdx.x) * N;
+    const int64_t base = tc_.blk * N;
     for (int e = tid; e < N; e += NT) {
         tw[e] = gtw ? gtw[e] : F::tw_from_const(INV ? roots.omega_inv(LOGN, e) : roots.omega(LOGN, e));
         if (gpost) post[e] = gpost[e];
@@ -196,7 +198,7 @@ static void launch_dft_single(const typename F::T* in, typename F::T* out, int w
     const size_t smem = SH::TILE * sizeof(typename F::T) + 3 * SH::N * sizeof(typename F::TW);
     auto k = k_dft_single<F, LOGN, INV>;
     set_smem(k, smem);
-    dim3 grid(1, ceil_div(w, LdeCfg<F>::C13));
+    const dim3 grid = tile_grid(1, w, LdeCfg<F>::C13);
     k<<<grid, SH::THREADS, smem, st>>>(in, out, w, br, pre, post, tw_table<F>(dft_tw, LOGN, INV != 0), roots);
     P3G_LAUNCHED();
     P3G_CUDA(cudaGetLastError());
@@ -209,7 +211,7 @@ static void launch_dft_pass_a(const typename F::T* in, typename F::T* mid, int w
     const size_t smem = SH::TILE * sizeof(typename F::T) + 3 * SH::N * sizeof(typename F::TW);
     auto k = k_dft_pass_a<F, LOGN, INV>;
     set_smem(k, smem);
-    dim3 grid(1u << n2, ceil_div(w, LdeCfg<F>::C13));
+    const dim3 grid = tile_grid(int64_t(1) << n2, w, LdeCfg<F>::C13);
     k<<<grid, SH::THREADS, smem, st>>>(in, mid, w, n2, pre, sq, a1, tw_table<F>(dft_tw, LOGN, INV != 0), roots);
     P3G_LAUNCHED();
     P3G_CUDA(cudaGetLastError());
@@ -222,7 +224,7 @@ static void launch_dft_pass_b(const typename F::T* mid, typename F::T* out, int 
     const size_t smem = SH::TILE * sizeof(typename F::T) + 2 * SH::N * sizeof(typename F::TW);
     auto k = k_dft_pass_b<F, LOGN, INV>;
     set_smem(k, smem);
-    dim3 grid(1u << n1, ceil_div(w, LdeCfg<F>::C13));
+    const dim3 grid = tile_grid(int64_t(1) << n1, w, LdeCfg<F>::C13);
     k<<<grid, SH::THREADS, smem, st>>>(mid, out, w, n1, br, post, tw_table<F>(dft_tw, LOGN, INV != 0), roots);
     P3G_LAUNCHED();
     P3G_CUDA(cudaGetLastError());

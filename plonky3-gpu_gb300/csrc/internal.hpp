@@ -138,6 +138,10 @@ struct p3g_tree {
     size_t desc_ents_off = 0;         // byte offset of the entries in d_desc
     std::vector<void*> stage_bufs;    // sponge states between parts (staged builds)
     bool in_plan = false;             // owned by a plan; p3g_tree_free refuses it
+    // Merkle-layer fusion (0 = the defaults of merkle.cu): levels of at most
+    // tail_max nodes at the top of the tree run in one CTA, one after the
+    // other; BabyBear levels of at most coop_max nodes use 16 lanes per node.
+    uint64_t tail_max = 0, coop_max = 0;
 };
 
 namespace p3g {
@@ -163,6 +167,41 @@ void fri_prove(p3g_ctx* ctx, const void* const* d_inputs, const uint32_t* log_he
 // (d_a: a in device memory instead, canonical)
 void bb4_axpy(p3g_ctx* ctx, uint32_t* y, const uint32_t* x, uint64_t n, const uint32_t* a, cudaStream_t st,
               const uint32_t* d_a = nullptr);
+// Batched LDEs (lde.cuh): traces that share (log_h, log_b, shift),
+// 1 <= log_h <= 21, with bit-reversed rows, in one launch per pass.  The
+// shape's three tables (sizes by lde_group_table_bytes_*, k = 0..2; 0 =
+// unused) are filled once by lde_group_tables_*; each trace needs
+// lde_group_scr_bytes_* of pass-1 scratch (0: none).
+size_t lde_group_table_bytes_bb(int log_h, int log_b, int k);
+size_t lde_group_table_bytes_gl(int log_h, int log_b, int k);
+size_t lde_group_scr_bytes_bb(int log_h, int w);
+size_t lde_group_scr_bytes_gl(int log_h, int w);
+void lde_group_tables_bb(p3g_ctx* ctx, int log_h, int log_b, uint64_t shift, void* const* tab, cudaStream_t st);
+void lde_group_tables_gl(p3g_ctx* ctx, int log_h, int log_b, uint64_t shift, void* const* tab, cudaStream_t st);
+void lde_group_bb(p3g_ctx* ctx, int log_h, int log_b, const void* const* in, void* const* scr, void* const* out,
+                  const uint32_t* w, size_t n, void* const* tab, cudaStream_t st);
+void lde_group_gl(p3g_ctx* ctx, int log_h, int log_b, const void* const* in, void* const* scr, void* const* out,
+                  const uint32_t* w, size_t n, void* const* tab, cudaStream_t st);
+// The LDE stage of a batched commit (plan.cu): traces grouped by shape.
+// Traces that share (log_h, log_b, shift) with 1 <= log_h <= 21 form one
+// group, run as one batch; every other trace (log_h 0 or above 21) is a group
+// of its own, run by lde_bb / lde_gl.
+struct LdeGroup {
+    int log_h = 0, log_b = 0;
+    uint64_t shift = 0;
+    bool batched = false;
+    std::vector<size_t> idx;     // trace indices
+    void* tab[3] = {nullptr, nullptr, nullptr};
+    std::vector<void*> scr;      // per trace of idx
+    uint64_t work = 0;           // LDE elements
+};
+std::vector<LdeGroup> lde_groups(const p3g_trace* traces, size_t n);
+// Allocates a batched group's tables and scratch from the pool and fills the tables.
+void lde_group_prepare(p3g_ctx* ctx, int field, LdeGroup& g, const p3g_trace* traces, cudaStream_t st);
+// Enqueues the group's LDEs (bit-reversed rows): trace i reads in[i] and writes lde[i].
+void lde_group_run(p3g_ctx* ctx, int field, const LdeGroup& g, const p3g_trace* traces, const void* const* in,
+                   void* const* lde, cudaStream_t st);
+void lde_group_release(p3g_ctx* ctx, LdeGroup& g, cudaStream_t st);
 // device copies of the prepared DFT twiddle tables (cudaMalloc'd; the context frees them)
 void* make_dft_tw_bb();
 void* make_dft_tw_gl();

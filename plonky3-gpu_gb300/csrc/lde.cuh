@@ -32,6 +32,9 @@
 // super-stages (and, in pass 2, the coefficients between the inverse and the
 // forward transforms).
 #pragma once
+#include <array>
+#include <vector>
+
 #include "internal.hpp"
 #include "ntt.cuh"
 
@@ -141,6 +144,26 @@ __global__ void k_broadcast_row(const typename F::T* in, typename F::T* out, int
 
 template <class F, int LOGN, int C>
 struct Tile : DftShape<typename F::T, LOGN, C, LdeCfg<F>::MAXT> {};
+
+// Grids of row blocks x column tiles are one-dimensional, the column tile
+// varying fastest: the CTAs in flight together cover whole row spans, so
+// every 128-byte line they touch is read or written in full while it is in
+// L2, and the column-tile count has no 65535 limit (grid.y).
+struct TileCoord {
+    int64_t blk;  // row block
+    int ct;       // column tile
+};
+template <int C>
+__device__ __forceinline__ TileCoord tile_coord(int w) {
+    const unsigned nct = unsigned(w + C - 1) / unsigned(C);
+    const unsigned b = blockIdx.x;
+    return {int64_t(b / nct), int(b % nct)};
+}
+inline dim3 tile_grid(int64_t nblk, int w, int C) {
+    const int64_t n = nblk * ((int64_t(w) + C - 1) / C);
+    if (n >= (int64_t(1) << 31)) throw Error(P3G_EUNSUPPORTED, "transform: grid of 2^31 or more CTAs");
+    return dim3(unsigned(n));
+}
 
 // ---- group loads (first super-stage) and stores (last super-stage)
 // Global rows i -> p0[i * s] (p0 already offset to this thread's column).
@@ -258,12 +281,47 @@ struct OutStore {
     }
 };
 
+// ------------------------------------------------------------ batches
+// Every launch runs a batch of LDEs of one shape (log_h, log_b, shift): one
+// trace for a single call, a whole height group for a batched commit.  The
+// grids of the traces are laid end to end; a CTA finds its trace from the
+// first CTA of each trace in the pass.  The batch is a kernel parameter
+// (constant bank); larger batches take several launches.
+constexpr int LDE_MAXJ = 64;
+template <class T>
+struct LdeJob {
+    const T* in;  // h x w trace
+    T* scr;       // pass-1 output, tiled by pass-2 column tiles (unused by the single kernel)
+    T* mid;       // pass-2 output (the LDE itself when rows are bit-reversed)
+    T* out;       // H x w LDE
+    uint32_t w;
+    uint32_t cta0[3];  // first CTA of this trace in pass 1 (or the single kernel), 2 and 3
+};
+template <class T>
+struct LdeJobs {
+    int n;
+    LdeJob<T> job[LDE_MAXJ];
+};
+// This CTA's trace in pass `ps`, and the CTA's index within that trace's grid.
+template <class T>
+__device__ __forceinline__ const LdeJob<T>& lde_job(const LdeJobs<T>& J, int ps, unsigned& local) {
+    int j = 0;
+#pragma unroll 1
+    while (j + 1 < J.n && J.job[j + 1].cta0[ps] <= blockIdx.x) ++j;
+    local = blockIdx.x - J.job[j].cta0[ps];
+    return J.job[j];
+}
+template <int C>
+__device__ __forceinline__ TileCoord local_tile(unsigned local, int w) {
+    const unsigned nct = unsigned(w + C - 1) / unsigned(C);
+    return {int64_t(local / nct), int(local % nct)};
+}
+
 // ------------------------------------------------------------ single kernel
 template <class F, int LOGN>
 __global__ void __launch_bounds__(Tile<F, LOGN, LdeCfg<F>::C13>::THREADS)
-k_lde_single(const typename F::T* __restrict__ in, typename F::T* __restrict__ out, int w,
-             int log_b, int bitrev_out, const typename F::T* __restrict__ sq, RootTab<F> roots,
-             const typename F::TW* __restrict__ gtwi, const typename F::TW* __restrict__ gtwf,
+k_lde_single(const LdeJobs<typename F::T> J, int log_b, int bitrev_out, const typename F::T* __restrict__ sq,
+             RootTab<F> roots, const typename F::TW* __restrict__ gtwi, const typename F::TW* __restrict__ gtwf,
              const typename F::TW* __restrict__ gpre) {
     constexpr int C = LdeCfg<F>::C13;
     using SH = Tile<F, LOGN, C>;
@@ -276,8 +334,11 @@ k_lde_single(const typename F::T* __restrict__ in, typename F::T* __restrict__ o
     TW* twi = reinterpret_cast<TW*>(B + SH::TILE);
     TW* twf = twi + N;
     TW* pre = twf + N;
+    unsigned local;
+    const LdeJob<T>& jb = lde_job(J, 0, local);
+    const int w = int(jb.w);
     const int tid = threadIdx.x, c = tid % C, t = tid / C;
-    const int col = blockIdx.y * C + c;
+    const int col = int(local) * C + c;
     const bool ok = col < w;
     const int logH = LOGN + log_b;
 
@@ -287,7 +348,7 @@ k_lde_single(const typename F::T* __restrict__ in, typename F::T* __restrict__ o
     }
     __syncthreads();
     {
-        GLoad<T> ld{in + col, w, ok};
+        GLoad<T> ld{jb.in + col, w, ok};
         TileStore<T, SH> st{A, c};
         cta_dif<F, SH, LOGN, C, 1>(A, twi, t, c, ld, st);
     }
@@ -297,7 +358,7 @@ k_lde_single(const typename F::T* __restrict__ in, typename F::T* __restrict__ o
             pre[k] = gpre ? gpre[tc * N + k] : F::tw_from_const(F::cmul(sq[k], roots.omega(logH, u * k)));
         __syncthreads();  // pre ready; A complete (first round) or B free (later rounds)
         PermLoad<F, SH, LOGN> ld{A, pre, c};
-        OutStore<T> st{out + col, w, int64_t(tc) * N, logH, bitrev_out != 0, ok};
+        OutStore<T> st{jb.out + col, w, int64_t(tc) * N, logH, bitrev_out != 0, ok};
         cta_dif<F, SH, LOGN, C, 0>(B, twf, t, c, ld, st);
         __syncthreads();  // pre and B reused by the next coset
     }
@@ -306,8 +367,7 @@ k_lde_single(const typename F::T* __restrict__ in, typename F::T* __restrict__ o
 // ------------------------------------------------------------ pass 1 (LOGN = n2)
 template <class F, int LOGN>
 __global__ void __launch_bounds__(Tile<F, LOGN, LdeCfg<F>::C13>::THREADS, P3G_LDE_MINB13)
-k_lde_pass1(const typename F::T* __restrict__ in, typename F::T* __restrict__ scratch, int w, int n1,
-            RootTab<F> roots, const typename F::TW* __restrict__ gtwi) {
+k_lde_pass1(const LdeJobs<typename F::T> J, int n1, RootTab<F> roots, const typename F::TW* __restrict__ gtwi) {
     constexpr int C = LdeCfg<F>::C13;
     using SH = Tile<F, LOGN, C>;
     using T = typename F::T;
@@ -317,10 +377,14 @@ k_lde_pass1(const typename F::T* __restrict__ in, typename F::T* __restrict__ sc
     T* A = reinterpret_cast<T*>(smem_raw);
     TW* tw = reinterpret_cast<TW*>(A + SH::TILE);
     TW* post = tw + N;
+    unsigned local;
+    const LdeJob<T>& jb = lde_job(J, 0, local);
+    const int w = int(jb.w);
     const int tid = threadIdx.x, c = tid % C, t = tid / C;
-    const int col = blockIdx.y * C + c;
+    const TileCoord tc_ = local_tile<C>(local, w);
+    const int col = tc_.ct * C + c;
     const bool ok = col < w;
-    const int64_t i1 = blockIdx.x;
+    const int64_t i1 = tc_.blk;
     const int64_t N1 = int64_t(1) << n1;
     const int n = n1 + LOGN;
 
@@ -334,8 +398,8 @@ k_lde_pass1(const typename F::T* __restrict__ in, typename F::T* __restrict__ sc
     // one contiguous block
     constexpr int C2 = LdeCfg<F>::C2;
     const int64_t h = int64_t(1) << n;
-    T* dst = ok ? scratch + ((int64_t(col / C2) * h + i1) * C2 + col % C2) : scratch;
-    GLoad<T> ld{in + i1 * w + col, N1 * w, ok};
+    T* dst = ok ? jb.scr + ((int64_t(col / C2) * h + i1) * C2 + col % C2) : jb.scr;
+    GLoad<T> ld{jb.in + i1 * w + col, N1 * w, ok};
     BitrevStore<F, LOGN> st{dst, N1 * C2, post, ok};
     cta_dif<F, SH, LOGN, C, 1>(A, tw, t, c, ld, st);
 }
@@ -343,10 +407,9 @@ k_lde_pass1(const typename F::T* __restrict__ in, typename F::T* __restrict__ sc
 // ------------------------------------------------------------ pass 2 (LOGN = n1)
 template <class F, int LOGN>
 __global__ void __launch_bounds__(Tile<F, LOGN, LdeCfg<F>::C2>::THREADS, P3G_LDE_MINB2)
-k_lde_pass2(const typename F::T* __restrict__ scratch, typename F::T* __restrict__ dst, int w, int n2,
-            int log_b, const typename F::T* __restrict__ sp, const typename F::T* __restrict__ sq,
-            RootTab<F> roots, const typename F::TW* __restrict__ gtwi, const typename F::TW* __restrict__ gtwf,
-            const typename F::TW* __restrict__ gpre) {
+k_lde_pass2(const LdeJobs<typename F::T> J, int n2, int log_b, const typename F::T* __restrict__ sp,
+            const typename F::T* __restrict__ sq, RootTab<F> roots, const typename F::TW* __restrict__ gtwi,
+            const typename F::TW* __restrict__ gtwf, const typename F::TW* __restrict__ gpre) {
     constexpr int C = LdeCfg<F>::C2;
     using SH = Tile<F, LOGN, C>;
     using T = typename F::T;
@@ -359,10 +422,14 @@ k_lde_pass2(const typename F::T* __restrict__ scratch, typename F::T* __restrict
     TW* twf = twi + N;
     TW* pre = twf + N;
     TW* post = pre + N;
+    unsigned local;
+    const LdeJob<T>& jb = lde_job(J, 1, local);
+    const int w = int(jb.w);
     const int tid = threadIdx.x, c = tid % C, t = tid / C;
-    const int col = blockIdx.y * C + c;
+    const TileCoord tc_ = local_tile<C>(local, w);
+    const int col = tc_.ct * C + c;
     const bool ok = col < w;
-    const int64_t k2 = blockIdx.x;
+    const int64_t k2 = tc_.blk;
     const int64_t N2 = int64_t(1) << n2;
     const int n = LOGN + n2;
     const int64_t h = int64_t(1) << n;
@@ -374,7 +441,7 @@ k_lde_pass2(const typename F::T* __restrict__ scratch, typename F::T* __restrict
     }
     __syncthreads();
     {
-        GLoad<T> ld{scratch + (int64_t(blockIdx.y) * h + int64_t(N) * k2) * C + c, C, ok};
+        GLoad<T> ld{jb.scr + (int64_t(tc_.ct) * h + int64_t(N) * k2) * C + c, C, ok};
         TileStore<T, SH> st{A, c};
         cta_dif<F, SH, LOGN, C, 1>(A, twi, t, c, ld, st);
     }
@@ -389,7 +456,7 @@ k_lde_pass2(const typename F::T* __restrict__ scratch, typename F::T* __restrict
         }
         __syncthreads();
         PermLoad<F, SH, LOGN> ld{A, pre, c};
-        GStore<F, true> st{dst + (tc * h + k2) * w + col, N2 * w, post, ok};
+        GStore<F, true> st{jb.mid + (tc * h + k2) * w + col, N2 * w, post, ok};
         cta_dif<F, SH, LOGN, C, 0>(B, twf, t, c, ld, st);
         __syncthreads();
     }
@@ -398,8 +465,8 @@ k_lde_pass2(const typename F::T* __restrict__ scratch, typename F::T* __restrict
 // ------------------------------------------------------------ pass 3 (LOGN = n2)
 template <class F, int LOGN>
 __global__ void __launch_bounds__(Tile<F, LOGN, LdeCfg<F>::C13>::THREADS, P3G_LDE_MINB13)
-k_lde_pass3(const typename F::T* src, typename F::T* out, int w, int n1, int log_b, int bitrev_out,
-            RootTab<F> roots, const typename F::TW* __restrict__ gtwf) {
+k_lde_pass3(const LdeJobs<typename F::T> J, int n1, int log_b, int bitrev_out, RootTab<F> roots,
+            const typename F::TW* __restrict__ gtwf) {
     constexpr int C = LdeCfg<F>::C13;
     using SH = Tile<F, LOGN, C>;
     using T = typename F::T;
@@ -408,18 +475,22 @@ k_lde_pass3(const typename F::T* src, typename F::T* out, int w, int n1, int log
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* A = reinterpret_cast<T*>(smem_raw);
     TW* tw = reinterpret_cast<TW*>(A + SH::TILE);
+    unsigned local;
+    const LdeJob<T>& jb = lde_job(J, 2, local);
+    const int w = int(jb.w);
     const int tid = threadIdx.x, c = tid % C, t = tid / C;
-    const int col = blockIdx.y * C + c;
+    const TileCoord tc_ = local_tile<C>(local, w);
+    const int col = tc_.ct * C + c;
     const bool ok = col < w;
-    const int64_t blk = blockIdx.x;
+    const int64_t blk = tc_.blk;
     const int n = n1 + LOGN;
     const int logH = n + log_b;
     const int64_t base = blk * N;  // = t*h + s1*N2
 
     for (int e = tid; e < N; e += NT) tw[e] = gtwf ? gtwf[e] : F::tw_from_const(roots.omega(LOGN, e));
     __syncthreads();
-    GLoad<T> ld{src + base * w + col, w, ok};
-    OutStore<T> st{out + col, w, base, logH, bitrev_out != 0, ok};
+    GLoad<T> ld{jb.mid + base * w + col, w, ok};
+    OutStore<T> st{jb.out + col, w, base, logH, bitrev_out != 0, ok};
     cta_dif<F, SH, LOGN, C, 0>(A, tw, t, c, ld, st);
 }
 
@@ -437,54 +508,50 @@ static const typename F::TW* tw_table(const typename F::TW* dft_tw, int logn, bo
 }
 
 template <class F, int LOGN>
-static void launch_single(const typename F::T* in, typename F::T* out, int w, int log_b, int br,
-                          const typename F::T* sq, const typename F::TW* pre, RootTab<F> roots,
-                          const typename F::TW* dft_tw, cudaStream_t st) {
+static void launch_single(const LdeJobs<typename F::T>& J, unsigned ctas, int log_b, int br, const typename F::T* sq,
+                          const typename F::TW* pre, RootTab<F> roots, const typename F::TW* dft_tw,
+                          cudaStream_t st) {
     using SH = Tile<F, LOGN, LdeCfg<F>::C13>;
     size_t smem = 2 * SH::TILE * sizeof(typename F::T) + 3 * SH::N * sizeof(typename F::TW);
     auto k = k_lde_single<F, LOGN>;
     set_smem(k, smem);
-    dim3 grid(1, ceil_div(w, LdeCfg<F>::C13));
-    k<<<grid, SH::THREADS, smem, st>>>(in, out, w, log_b, br, sq, roots, tw_table<F>(dft_tw, LOGN, true),
+    k<<<ctas, SH::THREADS, smem, st>>>(J, log_b, br, sq, roots, tw_table<F>(dft_tw, LOGN, true),
                                        tw_table<F>(dft_tw, LOGN, false), pre);
     P3G_LAUNCHED();
     P3G_CUDA(cudaGetLastError());
 }
 template <class F, int LOGN>
-static void launch_pass1(const typename F::T* in, typename F::T* scr, int w, int n1, RootTab<F> roots,
+static void launch_pass1(const LdeJobs<typename F::T>& J, unsigned ctas, int n1, RootTab<F> roots,
                          const typename F::TW* dft_tw, cudaStream_t st) {
     using SH = Tile<F, LOGN, LdeCfg<F>::C13>;
     size_t smem = SH::TILE * sizeof(typename F::T) + 2 * SH::N * sizeof(typename F::TW);
     auto k = k_lde_pass1<F, LOGN>;
     set_smem(k, smem);
-    dim3 grid(1u << n1, ceil_div(w, LdeCfg<F>::C13));
-    k<<<grid, SH::THREADS, smem, st>>>(in, scr, w, n1, roots, tw_table<F>(dft_tw, LOGN, true));
+    k<<<ctas, SH::THREADS, smem, st>>>(J, n1, roots, tw_table<F>(dft_tw, LOGN, true));
     P3G_LAUNCHED();
     P3G_CUDA(cudaGetLastError());
 }
 template <class F, int LOGN>
-static void launch_pass2(const typename F::T* scr, typename F::T* dst, int w, int n2, int log_b,
-                         const typename F::T* sp, const typename F::T* sq, const typename F::TW* pre,
-                         RootTab<F> roots, const typename F::TW* dft_tw, cudaStream_t st) {
+static void launch_pass2(const LdeJobs<typename F::T>& J, unsigned ctas, int n2, int log_b, const typename F::T* sp,
+                         const typename F::T* sq, const typename F::TW* pre, RootTab<F> roots,
+                         const typename F::TW* dft_tw, cudaStream_t st) {
     using SH = Tile<F, LOGN, LdeCfg<F>::C2>;
     size_t smem = 2 * SH::TILE * sizeof(typename F::T) + 4 * SH::N * sizeof(typename F::TW);
     auto k = k_lde_pass2<F, LOGN>;
     set_smem(k, smem);
-    dim3 grid(1u << n2, ceil_div(w, LdeCfg<F>::C2));
-    k<<<grid, SH::THREADS, smem, st>>>(scr, dst, w, n2, log_b, sp, sq, roots, tw_table<F>(dft_tw, LOGN, true),
+    k<<<ctas, SH::THREADS, smem, st>>>(J, n2, log_b, sp, sq, roots, tw_table<F>(dft_tw, LOGN, true),
                                        tw_table<F>(dft_tw, LOGN, false), pre);
     P3G_LAUNCHED();
     P3G_CUDA(cudaGetLastError());
 }
 template <class F, int LOGN>
-static void launch_pass3(const typename F::T* src, typename F::T* out, int w, int n1, int log_b, int br,
-                         RootTab<F> roots, const typename F::TW* dft_tw, cudaStream_t st) {
+static void launch_pass3(const LdeJobs<typename F::T>& J, unsigned ctas, int n1, int log_b, int br, RootTab<F> roots,
+                         const typename F::TW* dft_tw, cudaStream_t st) {
     using SH = Tile<F, LOGN, LdeCfg<F>::C13>;
     size_t smem = SH::TILE * sizeof(typename F::T) + SH::N * sizeof(typename F::TW);
     auto k = k_lde_pass3<F, LOGN>;
     set_smem(k, smem);
-    dim3 grid(1u << (n1 + log_b), ceil_div(w, LdeCfg<F>::C13));
-    k<<<grid, SH::THREADS, smem, st>>>(src, out, w, n1, log_b, br, roots, tw_table<F>(dft_tw, LOGN, false));
+    k<<<ctas, SH::THREADS, smem, st>>>(J, n1, log_b, br, roots, tw_table<F>(dft_tw, LOGN, false));
     P3G_LAUNCHED();
     P3G_CUDA(cudaGetLastError());
 }
@@ -506,6 +573,113 @@ static void pre_table(typename F::TW* out, const typename F::T* s, int logn, int
     P3G_CUDA(cudaGetLastError());
 }
 
+// The four-step split of the three-pass LDE: h = 2^n1 * 2^n2.
+inline int lde_n2(int log_h) { return (log_h + 1) / 2; }
+
+// Tables of one LDE shape (log_h, log_b, shift), shared by every trace of
+// that shape: [0] the first power table, [1] the second, [2] the prepared
+// coset twists.  Sizes in bytes (0 = unused).
+template <class F>
+std::array<size_t, 3> lde_table_bytes(int log_h, int log_b) {
+    using T = typename F::T;
+    using TW = typename F::TW;
+    if (log_h == 0) return {0, 0, 0};
+    if (log_h <= LDE_SINGLE_MAX) return {sizeof(T) << log_h, 0, sizeof(TW) << (log_h + log_b)};
+    const int n2 = lde_n2(log_h), n1 = log_h - n2;
+    return {sizeof(T) << n1, sizeof(T) << n2, sizeof(TW) << (n1 + log_b)};
+}
+// Fills the shape's tables (three small kernels on `st`).
+template <class F>
+void lde_tables(int log_h, int log_b, uint64_t shift, void* const* tab, RootTab<F> roots, cudaStream_t st) {
+    using T = typename F::T;
+    using TW = typename F::TW;
+    if (log_h == 0) return;
+    const int64_t h = int64_t(1) << log_h;
+    const uint64_t inv_h = F::h_inv(uint64_t(h) % F::P);
+    if (log_h <= LDE_SINGLE_MAX) {
+        pow_table<F>(static_cast<T*>(tab[0]), shift, inv_h, int(h), st);
+        pre_table<F>(static_cast<TW*>(tab[2]), static_cast<const T*>(tab[0]), log_h, log_b, log_h + log_b, 1, roots,
+                     st);
+        return;
+    }
+    const int n2 = lde_n2(log_h), n1 = log_h - n2;
+    const int64_t N2 = int64_t(1) << n2;
+    pow_table<F>(static_cast<T*>(tab[0]), F::h_pow(shift, uint64_t(N2)), inv_h, int(int64_t(1) << n1), st);
+    pow_table<F>(static_cast<T*>(tab[1]), shift, 1, int(N2), st);
+    pre_table<F>(static_cast<TW*>(tab[2]), static_cast<const T*>(tab[0]), n1, log_b, log_h + log_b, uint64_t(N2),
+                 roots, st);
+}
+// Pass-1 scratch of one trace of the three-pass LDE (elements).
+template <class F>
+size_t lde_scr_elems(int log_h, int w) {
+    if (log_h <= LDE_SINGLE_MAX || w == 0) return 0;
+    constexpr int C2 = LdeCfg<F>::C2;
+    return size_t(ceil_div(w, C2)) * C2 << log_h;
+}
+
+// Launches the LDEs of a batch of traces of one shape (2^1 <= h <= 2^21)
+// whose tables are filled: jobs[i] gives trace i's input, pass-1 scratch,
+// pass-2 output (the output itself with bit-reversed rows) and output.  Every
+// pass covers the whole batch (in launches of at most LDE_MAXJ traces).
+template <class F>
+void lde_batch(const std::vector<LdeJob<typename F::T>>& jobs, int log_h, int log_b, int bitrev_out,
+               void* const* tab, RootTab<F> roots, const typename F::TW* dft_tw, cudaStream_t st) {
+    using T = typename F::T;
+    using TW = typename F::TW;
+    const bool single = log_h <= LDE_SINGLE_MAX;
+    const int n2 = lde_n2(log_h), n1 = log_h - n2;
+    for (size_t j0 = 0; j0 < jobs.size(); j0 += LDE_MAXJ) {
+        LdeJobs<T> J{};
+        int64_t ctas[3] = {0, 0, 0};
+        for (size_t j = j0; j < jobs.size() && j < j0 + LDE_MAXJ; ++j) {
+            if (jobs[j].w == 0) continue;
+            LdeJob<T> jb = jobs[j];
+            const int64_t per[3] = {
+                single ? ceil_div(jb.w, LdeCfg<F>::C13) : int64_t(tile_grid(int64_t(1) << n1, int(jb.w), LdeCfg<F>::C13).x),
+                single ? 0 : int64_t(tile_grid(int64_t(1) << n2, int(jb.w), LdeCfg<F>::C2).x),
+                single ? 0 : int64_t(tile_grid(int64_t(1) << (n1 + log_b), int(jb.w), LdeCfg<F>::C13).x)};
+            for (int q = 0; q < 3; ++q) {
+                jb.cta0[q] = uint32_t(ctas[q]);
+                ctas[q] += per[q];
+                if (ctas[q] >= (int64_t(1) << 31)) throw Error(P3G_EUNSUPPORTED, "coset_lde: batch grid too large");
+            }
+            J.job[J.n++] = jb;
+        }
+        if (J.n == 0) continue;
+        if (single) {
+            const T* sq = static_cast<const T*>(tab[0]);
+            const TW* pre = static_cast<const TW*>(tab[2]);
+            switch (log_h) {
+#define C_(L) case L: launch_single<F, L>(J, unsigned(ctas[0]), log_b, bitrev_out, sq, pre, roots, dft_tw, st); break;
+                C_(1) C_(2) C_(3) C_(4) C_(5) C_(6) C_(7) C_(8) C_(9) C_(10)
+#undef C_
+            }
+            continue;
+        }
+        const T* sp = static_cast<const T*>(tab[0]);
+        const T* sq = static_cast<const T*>(tab[1]);
+        const TW* pre = static_cast<const TW*>(tab[2]);
+        switch (n2) {
+#define C_(L) case L: launch_pass1<F, L>(J, unsigned(ctas[0]), n1, roots, dft_tw, st); break;
+            P3G_CASES_1_11(C_)
+#undef C_
+            default: throw Error(P3G_EUNSUPPORTED, "coset_lde: pass-1 size");
+        }
+        switch (n1) {
+#define C_(L) case L: launch_pass2<F, L>(J, unsigned(ctas[1]), n2, log_b, sp, sq, pre, roots, dft_tw, st); break;
+            P3G_CASES_1_11(C_)
+#undef C_
+            default: throw Error(P3G_EUNSUPPORTED, "coset_lde: pass-2 size");
+        }
+        switch (n2) {
+#define C_(L) case L: launch_pass3<F, L>(J, unsigned(ctas[2]), n1, log_b, bitrev_out, roots, dft_tw, st); break;
+            P3G_CASES_1_11(C_)
+#undef C_
+            default: throw Error(P3G_EUNSUPPORTED, "coset_lde: pass-3 size");
+        }
+    }
+}
+
 // Scratch buffers of one LDE call: [0] first power table, [1] second power
 // table, [2] prepared coset twists, [3] pass-1 output (tiled by pass-2
 // column tiles), [4] natural-order staging.  Sizes in bytes (0 = unused).
@@ -521,35 +695,24 @@ struct LdeScratch {
 template <class F>
 LdeScratch lde_scratch(int log_h, int w, int log_b, int bitrev_out) {
     using T = typename F::T;
-    using TW = typename F::TW;
     LdeScratch s;
     if (log_h == 0 || w == 0) return s;
-    const size_t h = size_t(1) << log_h;
-    if (log_h <= LDE_SINGLE_MAX) {
-        s.bytes[0] = sizeof(T) * h;
-        s.bytes[2] = sizeof(TW) * (h << log_b);
-        return s;
-    }
-    const int n2 = (log_h + 1) / 2, n1 = log_h - n2;
-    constexpr int C2 = LdeCfg<F>::C2;
-    s.bytes[0] = sizeof(T) << n1;
-    s.bytes[1] = sizeof(T) << n2;
-    s.bytes[2] = sizeof(TW) << (n1 + log_b);
-    s.bytes[3] = sizeof(T) * size_t(ceil_div(w, C2)) * C2 * h;
-    s.bytes[4] = bitrev_out ? 0 : sizeof(T) * (h << log_b) * size_t(w);
+    const auto tb = lde_table_bytes<F>(log_h, log_b);
+    for (int i = 0; i < 3; ++i) s.bytes[i] = tb[i];
+    if (log_h <= LDE_SINGLE_MAX) return s;
+    s.bytes[3] = sizeof(T) * lde_scr_elems<F>(log_h, w);
+    s.bytes[4] = bitrev_out ? 0 : sizeof(T) * (size_t(w) << (log_h + log_b));
     return s;
 }
 
-// The LDE proper, on validated arguments (log_h <= LDE_PASS_MAX, shift
+// The LDE of one trace, on validated arguments (log_h <= LDE_PASS_MAX, shift
 // canonical and non-zero) and scratch buffers sized by lde_scratch.
 template <class F>
 void lde_run(const typename F::T* in, int log_h, int w, int log_b, uint64_t shift, int bitrev_out,
              typename F::T* out, cudaStream_t st, RootTab<F> roots, const typename F::TW* dft_tw,
              void* const* buf) {
     using T = typename F::T;
-    using TW = typename F::TW;
     if (w == 0) return;
-    const int64_t h = int64_t(1) << log_h;
     if (log_h == 0) {
         int64_t total = (int64_t(1) << log_b) * w;
         k_broadcast_row<F><<<ceil_div(total, 256), 256, 0, st>>>(in, out, w, int(1 << log_b));
@@ -557,47 +720,25 @@ void lde_run(const typename F::T* in, int log_h, int w, int log_b, uint64_t shif
         P3G_CUDA(cudaGetLastError());
         return;
     }
-    const uint64_t inv_h = F::h_inv(uint64_t(h) % F::P);
-    if (log_h <= LDE_SINGLE_MAX) {
-        T* sq = static_cast<T*>(buf[0]);
-        TW* pre = static_cast<TW*>(buf[2]);
-        pow_table<F>(sq, shift, inv_h, int(h), st);
-        pre_table<F>(pre, sq, log_h, log_b, log_h + log_b, 1, roots, st);
-        switch (log_h) {
-#define C_(L) case L: launch_single<F, L>(in, out, w, log_b, bitrev_out, sq, pre, roots, dft_tw, st); break;
-            C_(1) C_(2) C_(3) C_(4) C_(5) C_(6) C_(7) C_(8) C_(9) C_(10)
-#undef C_
-        }
-        return;
-    }
-    const int n2 = (log_h + 1) / 2, n1 = log_h - n2;
-    const int64_t N2 = int64_t(1) << n2;
-    T* sp = static_cast<T*>(buf[0]);
-    T* sq = static_cast<T*>(buf[1]);
-    TW* pre = static_cast<TW*>(buf[2]);
-    T* scr = static_cast<T*>(buf[3]);
-    T* mid = bitrev_out ? out : static_cast<T*>(buf[4]);
-    pow_table<F>(sp, F::h_pow(shift, uint64_t(N2)), inv_h, int(int64_t(1) << n1), st);
-    pow_table<F>(sq, shift, 1, int(N2), st);
-    pre_table<F>(pre, sp, n1, log_b, log_h + log_b, uint64_t(N2), roots, st);
-    switch (n2) {
-#define C_(L) case L: launch_pass1<F, L>(in, scr, w, n1, roots, dft_tw, st); break;
-        P3G_CASES_1_11(C_)
-#undef C_
-        default: throw Error(P3G_EUNSUPPORTED, "coset_lde: pass-1 size");
-    }
-    switch (n1) {
-#define C_(L) case L: launch_pass2<F, L>(scr, mid, w, n2, log_b, sp, sq, pre, roots, dft_tw, st); break;
-        P3G_CASES_1_11(C_)
-#undef C_
-        default: throw Error(P3G_EUNSUPPORTED, "coset_lde: pass-2 size");
-    }
-    switch (n2) {
-#define C_(L) case L: launch_pass3<F, L>(mid, out, w, n1, log_b, bitrev_out, roots, dft_tw, st); break;
-        P3G_CASES_1_11(C_)
-#undef C_
-        default: throw Error(P3G_EUNSUPPORTED, "coset_lde: pass-3 size");
-    }
+    lde_tables<F>(log_h, log_b, shift, buf, roots, st);
+    T* mid = bitrev_out || log_h <= LDE_SINGLE_MAX ? out : static_cast<T*>(buf[4]);
+    const std::vector<LdeJob<T>> jobs{LdeJob<T>{in, static_cast<T*>(buf[3]), mid, out, uint32_t(w), {0, 0, 0}}};
+    lde_batch<F>(jobs, log_h, log_b, bitrev_out, buf, roots, dft_tw, st);
+}
+
+// Bit-reversed LDEs of n traces of one shape (1 <= log_h <= 21) as one batch,
+// with the shape's tables already filled (lde_tables) and each trace's pass-1
+// scratch given (lde_scr_elems elements; null for the single kernel).
+template <class F>
+void lde_group_t(int log_h, int log_b, const void* const* in, void* const* scr, void* const* out, const uint32_t* w,
+                 size_t n, void* const* tab, RootTab<F> roots, const typename F::TW* dft_tw, cudaStream_t st) {
+    using T = typename F::T;
+    std::vector<LdeJob<T>> jobs;
+    jobs.reserve(n);
+    for (size_t i = 0; i < n; ++i)
+        jobs.push_back(LdeJob<T>{static_cast<const T*>(in[i]), static_cast<T*>(scr[i]), static_cast<T*>(out[i]),
+                                 static_cast<T*>(out[i]), w[i], {0, 0, 0}});
+    lde_batch<F>(jobs, log_h, log_b, 1, tab, roots, dft_tw, st);
 }
 
 // Context entry: validates, takes the scratch from the context's pool.

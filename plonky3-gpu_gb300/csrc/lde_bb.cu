@@ -9,6 +9,17 @@ void lde_bb(p3g_ctx* ctx, const uint32_t* in, int log_h, int w, int log_b, uint3
                   static_cast<const FBB::TW*>(ctx->bb_dft_tw));
 }
 
+size_t lde_group_table_bytes_bb(int log_h, int log_b, int k) { return lde_table_bytes<FBB>(log_h, log_b)[k]; }
+size_t lde_group_scr_bytes_bb(int log_h, int w) { return sizeof(uint32_t) * lde_scr_elems<FBB>(log_h, w); }
+void lde_group_tables_bb(p3g_ctx* ctx, int log_h, int log_b, uint64_t shift, void* const* tab, cudaStream_t st) {
+    lde_tables<FBB>(log_h, log_b, shift % FBB::P, tab, ctx->bb_roots(), st);
+}
+void lde_group_bb(p3g_ctx* ctx, int log_h, int log_b, const void* const* in, void* const* scr, void* const* out,
+                  const uint32_t* w, size_t n, void* const* tab, cudaStream_t st) {
+    lde_group_t<FBB>(log_h, log_b, in, scr, out, w, n, tab, ctx->bb_roots(),
+                    static_cast<const FBB::TW*>(ctx->bb_dft_tw), st);
+}
+
 void* make_dft_tw_bb() {
     const auto v = build_dft_tw<FBB>();
     void* d = nullptr;

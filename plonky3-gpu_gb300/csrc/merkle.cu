@@ -274,14 +274,18 @@ static void hash_stages(p3g_ctx* ctx, p3g_tree* tree, const typename H::Params& 
 // levels are latency-bound: BabyBear runs them with one 16-lane group per
 // node (a launch per level up to COOP_MAX_NODES nodes, then one CTA for every
 // level of at most COOP_TAIL_NODES), Goldilocks with one CTA for every level
-// of at most TAIL_NODES.
+// of at most TAIL_NODES.  A tree's tail_max / coop_max override the two
+// thresholds (the batched commit's autotuner sets them).
 template <class H>
 static void levels(p3g_ctx* ctx, p3g_tree* tree, const typename H::Params& p, cudaStream_t st) {
     using T = typename H::T;
     constexpr bool BB = std::is_same<H, HBB>::value;
     T* dig = static_cast<T*>(tree->d_digests);
     const size_t nl = tree->layer_size.size();
-    const uint64_t tail_max = BB ? COOP_TAIL_NODES : uint64_t(TAIL_NODES);
+    // the Goldilocks tail kernel covers at most TAIL_NODES nodes per level
+    const uint64_t tail_max = tree->tail_max ? (BB ? tree->tail_max : std::min<uint64_t>(tree->tail_max, TAIL_NODES))
+                                             : (BB ? COOP_TAIL_NODES : uint64_t(TAIL_NODES));
+    const uint64_t coop_max = tree->coop_max ? tree->coop_max : COOP_MAX_NODES;
     size_t first_tail = nl;
     while (first_tail > 1 && tree->layer_size[first_tail - 1] <= tail_max &&
            nl - (first_tail - 1) <= size_t(TAIL_MAX_LEVELS))
@@ -296,7 +300,7 @@ static void levels(p3g_ctx* ctx, p3g_tree* tree, const typename H::Params& p, cu
     };
     for (size_t l = 1; l < first_tail; ++l) {
         const uint64_t np = tree->layer_size[l];
-        if (BB && np <= COOP_MAX_NODES) {
+        if (BB && np <= coop_max) {
             TailLevels<T> t{};
             t.lev[t.n++] = level(l);
             run(CoopFn<H>{&p, &t, unsigned((np * 16 + COOP_THREADS - 1) / COOP_THREADS), st});

@@ -376,12 +376,14 @@ void Launch<H, D, RF, RP>::hash_groups(const typename H::Params& p, unsigned lon
                                        const HashGroup<T>* groups, int ngroups, const HashEntry<T>* ents,
                                        uint64_t total_units, int sm_count, cudaStream_t st) {
     if (total_units == 0) return;
-    static int occ = 0;  // resident CTAs per SM (same for every device of one architecture)
-    if (occ == 0) {
+    // resident CTAs per SM (same for every device of one architecture); a
+    // function-local static is initialised once even when several host
+    // threads get here together
+    static const int occ = [] {
         int o = 0;
         P3G_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_hash_groups<H, D, RF, RP>, HASH_ROWS, 0));
-        occ = o > 0 ? o : 1;
-    }
+        return o > 0 ? o : 1;
+    }();
     const int grid = occ * sm_count;
     P3G_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned long long), st));
     const int blocks = int(std::min<uint64_t>(uint64_t(grid), total_units));
@@ -401,12 +403,11 @@ template <class H, int D, int RF, int RP>
 void Launch<H, D, RF, RP>::grind(const typename H::Params& p, const GrindArgs<T, H::W>* d_args, uint64_t base,
                                  uint64_t count, unsigned long long* found, int sm_count, cudaStream_t st) {
     if (count == 0) return;
-    static int occ = 0;
-    if (occ == 0) {
+    static const int occ = [] {
         int o = 0;
         P3G_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_grind<H, D, RF, RP>, 128, 0));
-        occ = o > 0 ? o : 1;
-    }
+        return o > 0 ? o : 1;
+    }();
     const uint64_t blocks = std::min<uint64_t>(uint64_t(occ) * sm_count, (count + 127) / 128);
     k_grind<H, D, RF, RP><<<unsigned(blocks), 128, 0, st>>>(p, d_args, base, count, found);
     P3G_LAUNCHED();

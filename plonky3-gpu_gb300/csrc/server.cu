@@ -10,9 +10,10 @@
 // the Poseidon2 MMCS commit (merkle_tree_mmcs.hpp:100-107), and fold_matrix
 // (fri_folding.hpp:200) of the LDE's first four columns read as one
 // BabyBear^4 column (a stand-in quotient), then the root and the first
-// folded value are copied back.  The LDE and its tree stay resident for
-// follow-up openings (MerkleTreeMmcs::open_batch, merkle_tree_mmcs.hpp:120-152)
-// until the client releases the request.  Results carry submit / admit /
+// folded value are copied back.  The LDE, its tree and the folded vector (the
+// next FRI round's input) stay resident for follow-up openings
+// (MerkleTreeMmcs::open_batch, merkle_tree_mmcs.hpp:120-152) and reads of the
+// fold until the client releases the request.  Results carry submit / admit /
 // done timestamps for latency percentiles.
 //
 // All waits are bounded: the worker sleeps on a condition variable with a
@@ -105,12 +106,17 @@ void finish(p3g_server* s, const std::shared_ptr<Job>& j) {
     s->completed.push_back(res);
 }
 
-void free_job_device(p3g_server* s, Job& j, cudaStream_t st) {
+// The request's working buffers (trace copy, packed fold input); with
+// `all`, the resident fold output too.
+void free_job_device(p3g_server* s, Job& j, cudaStream_t st, bool all) {
     p3g_ctx* ctx = s->ctx;
     if (j.d_trace) ctx->release(j.d_trace, st);
     if (j.d_pack) ctx->release(j.d_pack, st);
-    if (j.d_fold) ctx->release(j.d_fold, st);
-    j.d_trace = j.d_pack = j.d_fold = nullptr;
+    j.d_trace = j.d_pack = nullptr;
+    if (all && j.d_fold) {
+        ctx->release(j.d_fold, st);
+        j.d_fold = nullptr;
+    }
 }
 
 // Enqueues the request's whole device work on its slot stream.
@@ -161,7 +167,7 @@ void worker_loop(p3g_server* s) {
                 j->status = P3G_ECUDA;
                 s->fatal = cudaGetErrorString(q);
             }
-            free_job_device(s, *j, s->streams[k]);
+            free_job_device(s, *j, s->streams[k], j->status != P3G_OK);
             finish(s, j);  // copies the root and fold head out of the slot's pinned words
             j->h_out = nullptr;
             if (j->status == P3G_OK) {
@@ -331,6 +337,28 @@ int p3g_server_open(p3g_server* s, uint64_t id, const uint64_t* h_indices, size_
     return P3G_OK;
 }
 
+int p3g_server_read_fold(p3g_server* s, uint64_t id, void* h_out, uint64_t n_values) {
+    try {
+        P3G_REQUIRE(s && h_out, "server_read_fold: null argument");
+        std::shared_ptr<Job> j;
+        {
+            std::lock_guard<std::mutex> lk(s->mu);
+            auto it = s->resident.find(id);
+            P3G_REQUIRE(it != s->resident.end(), "server_read_fold: no resident result with that id");
+            j = it->second;
+        }
+        const uint64_t half = (uint64_t(1) << (j->req.log_h + j->req.log_blowup)) / 2;
+        P3G_REQUIRE(n_values == half, "server_read_fold: n_values must be half the LDE height");
+        P3G_REQUIRE(j->d_fold, "server_read_fold: the fold output is not resident");
+        P3G_CUDA(cudaSetDevice(s->ctx->device));
+        P3G_CUDA(cudaMemcpy(h_out, j->d_fold, 16 * half, cudaMemcpyDeviceToHost));
+    } catch (const p3g::Error& e) {
+        p3g::set_last_error(e.what());
+        return e.status;
+    }
+    return P3G_OK;
+}
+
 int p3g_server_release(p3g_server* s, uint64_t id) {
     try {
         P3G_REQUIRE(s, "server_release: null server");
@@ -346,6 +374,7 @@ int p3g_server_release(p3g_server* s, uint64_t id) {
         p3g::tree_release(s->ctx, j->tree, nullptr);
         delete j->tree;
         j->tree = nullptr;
+        p3g::free_job_device(s, *j, nullptr, true);
         {
             std::lock_guard<std::mutex> lk(s->mu);
             s->used -= j->bytes;
@@ -368,10 +397,11 @@ int p3g_server_destroy(p3g_server* s) {
     for (auto& kv : s->resident) {
         p3g::tree_release(s->ctx, kv.second->tree, nullptr);
         delete kv.second->tree;
+        p3g::free_job_device(s, *kv.second, nullptr, true);
     }
     for (auto& j : s->slot_job)
         if (j) {
-            p3g::free_job_device(s, *j, nullptr);
+            p3g::free_job_device(s, *j, nullptr, true);
             if (j->tree) p3g::tree_release(s->ctx, j->tree, nullptr);
             delete j->tree;
         }

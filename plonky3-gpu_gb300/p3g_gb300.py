@@ -26,9 +26,9 @@ EXPORTS = [
     "p3g_set_poseidon2", "p3g_poseidon2_permute", "p3g_coset_lde", "p3g_dft", "p3g_mmcs_commit",
     "p3g_commit_matrix", "p3g_tree_info", "p3g_tree_layer_ptr", "p3g_tree_leaf_ptr",
     "p3g_mmcs_open_batch", "p3g_tree_free", "p3g_commit_traces", "p3g_commit_traces_host", "p3g_fold_matrix_bb4",
-    "p3g_coset_lde_bb_noalloc", "p3g_plan_commit", "p3g_plan_launch", "p3g_plan_info",
+    "p3g_coset_lde_bb_noalloc", "p3g_plan_commit", "p3g_plan_commit_host", "p3g_plan_launch", "p3g_plan_info",
     "p3g_plan_destroy", "p3g_server_create", "p3g_server_submit", "p3g_server_poll",
-    "p3g_server_pending", "p3g_server_open", "p3g_server_release", "p3g_server_destroy",
+    "p3g_server_pending", "p3g_server_open", "p3g_server_read_fold", "p3g_server_release", "p3g_server_destroy",
     "p3g_pcs_open_values", "p3g_pcs_reduce", "p3g_bb4_axpy", "p3g_grind", "p3g_fri_rounds", "p3g_fri_prove", "p3g_ctx_memory",
 ]
 
@@ -123,6 +123,7 @@ def load(path: str | None = None):
     L.p3g_fold_matrix_bb4.argtypes = [vp, vp, u32, u32, vp, vp, vp]
     L.p3g_coset_lde_bb_noalloc.argtypes = [vp, u32, u32, u32, u32, i32, vp, vp]
     L.p3g_plan_commit.argtypes = [vp, i32, C.POINTER(Trace), sz, u32, C.POINTER(FoldJob), u32, C.POINTER(vp)]
+    L.p3g_plan_commit_host.argtypes = L.p3g_plan_commit.argtypes
     L.p3g_plan_launch.argtypes = [vp, vp, vp]
     L.p3g_plan_info.argtypes = [vp, C.POINTER(vp), C.POINTER(u32), C.POINTER(u64)]
     L.p3g_plan_destroy.argtypes = [vp, vp]
@@ -131,6 +132,7 @@ def load(path: str | None = None):
     L.p3g_server_poll.argtypes = [vp, C.POINTER(Result), sz, C.POINTER(sz)]
     L.p3g_server_pending.argtypes = [vp, C.POINTER(u64), C.POINTER(u64), C.POINTER(u64), C.POINTER(u64)]
     L.p3g_server_open.argtypes = [vp, u64, vp, sz, vp, vp]
+    L.p3g_server_read_fold.argtypes = [vp, u64, vp, u64]
     L.p3g_server_release.argtypes = [vp, u64]
     L.p3g_server_destroy.argtypes = [vp]
     L.p3g_pcs_open_values.argtypes = [vp, vp, u32, u32, i32, u32, vp, u32, vp, vp]
@@ -281,6 +283,12 @@ class Tree:
             out.append(arr)
         return out
 
+    def layer_ptr(self, i: int) -> int:
+        """Device pointer of digest layer i (0 = leaves; the last is the cap)."""
+        p = C.c_void_p()
+        check(load().p3g_tree_layer_ptr(self.handle, i, C.byref(p)))
+        return p.value
+
     def leaf_ptr(self, i: int) -> int:
         p = C.c_void_p()
         check(load().p3g_tree_leaf_ptr(self.handle, i, C.byref(p)))
@@ -303,10 +311,12 @@ class Tree:
 
 
 class Plan:
-    """A batched commit captured as one CUDA graph (p3g_plan_*)."""
+    """A batched commit captured as one CUDA graph (p3g_plan_*).  With
+    host=True the trace pointers and the fold input are pinned host memory
+    (p3g_plan_commit_host): every launch copies them in."""
 
     def __init__(self, ctx: "Context", field: int, traces, cap_height: int = 0, fold=None,
-                 n_streams: int = 0):
+                 n_streams: int = 0, host: bool = False):
         self.ctx, self.field = ctx, field
         arr = (Trace * len(traces))(*[Trace(p, lh, w, lb, 0, s) for (p, lh, w, lb, s) in traces])
         fj = None
@@ -314,8 +324,9 @@ class Plan:
             d_in, d_out, lh, la, beta = fold
             fj = FoldJob(d_in, d_out, lh, la, (C.c_uint32 * 4)(*[int(b) for b in beta]))
         h = C.c_void_p()
-        check(load().p3g_plan_commit(ctx.handle, field, arr, len(traces), cap_height,
-                                     C.byref(fj) if fj is not None else None, n_streams, C.byref(h)))
+        fn = load().p3g_plan_commit_host if host else load().p3g_plan_commit
+        check(fn(ctx.handle, field, arr, len(traces), cap_height, C.byref(fj) if fj is not None else None,
+                 n_streams, C.byref(h)))
         self.handle = h.value
         t = C.c_void_p()
         ns = C.c_uint32()
@@ -365,6 +376,12 @@ class Server:
         proof = np.zeros((idx.size, max(nlayers - 1, 0), 8), np.uint32)
         check(load().p3g_server_open(self.handle, rid, _np_ptr(idx), idx.size, _np_ptr(rows), _np_ptr(proof)))
         return rows, proof
+
+    def read_fold(self, rid: int, lde_height: int) -> np.ndarray:
+        """The request's resident fold output: lde_height / 2 BabyBear^4 values."""
+        out = np.zeros((lde_height // 2, 4), np.uint32)
+        check(load().p3g_server_read_fold(self.handle, rid, _np_ptr(out), lde_height // 2))
+        return out
 
     def release(self, rid: int):
         check(load().p3g_server_release(self.handle, rid))

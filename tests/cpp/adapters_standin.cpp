@@ -15,6 +15,9 @@
 //   adapters_standin dft <bb|gl> <in> <out> <log_h> <width> <kind 0-3> <shift>
 //   adapters_standin challenger <out> <seed> <n_obs> <bits>...
 //   adapters_standin prove_fri <in> <out> <challenger> <nq> <log_blowup> <log_fpl> <max_la> <cpow> <qpow> <log_h>...
+//   adapters_standin pcs_commit <in> <out> <log_blowup> <shift> <log_h0> <w0> [<log_h1> <w1> ...]
+//       (TwoAdicFriPcs::commit's composition over GpuDft and GpuInputMmcs;
+//        <out> receives the root digest, then the flat committed matrix)
 //
 // <in> holds canonical little-endian words (u32 BabyBear, u64 Goldilocks;
 // for mmcs the matrices back to back; for fold 4 beta coefficients, then
@@ -397,6 +400,50 @@ static int run_build_tree(int argc, char** a) {
     return 0;
 }
 
+// TwoAdicFriPcs::commit (two_adic_fri_pcs.hpp:207-266) as the PCS chains its
+// members: GpuDft::coset_lde_batch per matrix (natural order, the domain's
+// shift), the rows of every LDE side by side with row r of a shorter LDE
+// taken as r mod its height, the width padded with zero columns to a power of
+// two, then GpuInputMmcs::commit_matrix of that flat matrix.
+static int run_pcs_commit(int argc, char** a) {
+    if (argc < 8 || (argc - 6) % 2) return 2;
+    auto in = read_file(a[2]);
+    const size_t log_blowup = std::strtoul(a[4], nullptr, 0);
+    const BabyBear shift(uint32_t(std::strtoul(a[5], nullptr, 0)));
+    p3g::GpuDft<Radix2Dit> dft;
+    std::vector<RowMajorMatrix<BabyBear>> ldes;
+    size_t off = 0;
+    for (int i = 6; i + 1 < argc; i += 2) {
+        const size_t h = size_t(1) << std::strtoul(a[i], nullptr, 0), w = std::strtoul(a[i + 1], nullptr, 0);
+        RowMajorMatrix<BabyBear> m(p3g::from_words<BabyBear>(in.data() + off, h * w), w);
+        off += 4 * h * w;
+        ldes.push_back(dft.coset_lde_batch(std::move(m), log_blowup, shift));
+    }
+    size_t max_h = 0, total_w = 0;
+    for (const auto& l : ldes) {
+        max_h = std::max(max_h, l.height());
+        total_w += l.width();
+    }
+    size_t padded_w = 1;
+    while (padded_w < total_w) padded_w <<= 1;
+    std::vector<BabyBear> flat;
+    flat.reserve(max_h * padded_w);
+    for (size_t r = 0; r < max_h; ++r) {
+        for (const auto& l : ldes) {
+            const size_t row = r % l.height();
+            flat.insert(flat.end(), l.values.begin() + row * l.width(), l.values.begin() + (row + 1) * l.width());
+        }
+        flat.resize(flat.size() + (padded_w - total_w), BabyBear(0));
+    }
+    p3g::GpuInputMmcs<FlatMmcs<BabyBear, 8>> mmcs{FlatMmcs<BabyBear, 8>{}};
+    auto [commitment, pd] = mmcs.commit_matrix(flat, padded_w);
+    if (commitment.size() != 1 || pd.height != max_h || pd.width != padded_w) return 3;
+    std::vector<BabyBear> out(commitment[0].begin(), commitment[0].end());
+    out.insert(out.end(), flat.begin(), flat.end());
+    write_file(a[3], p3g::to_words(out));
+    return 0;
+}
+
 int main(int argc, char** argv) {
     if (argc < 4) return 2;
     const std::string cmd = argv[1];
@@ -404,6 +451,7 @@ int main(int argc, char** argv) {
         set_constants();
         if (cmd == "challenger") return run_challenger(argc, argv);
         if (cmd == "prove_fri") return run_prove_fri(argc, argv);
+        if (cmd == "pcs_commit") return run_pcs_commit(argc, argv);
         if (cmd == "lde") return std::string(argv[2]) == "bb" ? run_lde<BabyBear>(argv) : run_lde<Goldilocks>(argv);
         if (cmd == "dft") {
             if (argc < 9) return 2;

@@ -8,7 +8,9 @@ import pytest
 
 from conftest import compile_cpp
 
-REF_INCLUDE = os.environ.get("P3G_REFERENCE_INCLUDE", "/root/reference/src/include")
+# the reference's src/include directory; the tests that need it are skipped
+# when the variable is unset
+REF_INCLUDE = os.environ.get("P3G_REFERENCE_INCLUDE", "")
 
 
 def test_standin_program_compiles_and_links(tmp_path):
@@ -17,14 +19,16 @@ def test_standin_program_compiles_and_links(tmp_path):
     assert "warning" not in log, log
 
 
-@pytest.mark.skipif(not os.path.isdir(REF_INCLUDE), reason="reference headers not present")
+@pytest.mark.skipif(not (REF_INCLUDE and os.path.isdir(REF_INCLUDE)),
+                    reason="P3G_REFERENCE_INCLUDE does not name the reference headers")
 def test_adapters_drop_into_reference_types(tmp_path):
     rc, log = compile_cpp("adapters_reference.cpp", str(tmp_path / "ref"), ["-I", REF_INCLUDE])
     assert rc == 0, log
     assert os.path.exists(tmp_path / "ref")
 
 
-@pytest.mark.skipif(not os.path.isdir(REF_INCLUDE), reason="reference headers not present")
+@pytest.mark.skipif(not (REF_INCLUDE and os.path.isdir(REF_INCLUDE)),
+                    reason="P3G_REFERENCE_INCLUDE does not name the reference headers")
 def test_proof_wire_format_round_trips_through_reference_verifier(tmp_path):
     """include/p3g_proof.hpp: a TwoAdicFriPcs proof and its opened values made by
     the reference's own prover survive encode/decode byte for byte, the

@@ -230,3 +230,23 @@ def test_adapter_reports_bad_dimensions_as_invalid_argument(prog, tmp_path):
     rc, err, _ = _run(prog, tmp_path, "commit_matrix", None, [0, 0], np.zeros(0, np.uint32))
     assert rc == 4, err
     assert "bad dimensions" in err
+
+
+def test_gpu_pcs_commit_composition_matches_reference_roots(prog, tmp_path, golden):
+    """TwoAdicFriPcs::commit (two_adic_fri_pcs.hpp:207-266) chained as the PCS
+    chains its members -- GpuDft::coset_lde_batch per matrix, rows joined with
+    r % height, zero columns up to a power-of-two width, GpuInputMmcs::commit_matrix
+    -- gives the reference's own commitment roots on the GPU, and the flat
+    matrix it commits equals the oracle's."""
+    p = O.bb16_params()
+    for case in golden["pcs_commit"]:
+        shapes = [tuple(int(v) for v in s.split("x")) for s in case["shapes"]]
+        traces = [O.bb_random_matrix(1 << lh, w, case["seed"] + i) for i, (lh, w) in enumerate(shapes)]
+        data = np.concatenate([t.reshape(-1) for t in traces])
+        rest = [case["log_blowup"], case["shift"]] + [x for lh_w in shapes for x in lh_w]
+        rc, err, fout = _run(prog, tmp_path, "pcs_commit", None, rest, data)
+        assert rc == 0, err
+        got = np.fromfile(fout, dtype=np.uint32)
+        assert got[:8].tolist() == case["root"]
+        root, flat = O.pcs_commit(p, traces, case["log_blowup"], case["shift"])
+        assert np.array_equal(got[8:].reshape(flat.shape), flat)

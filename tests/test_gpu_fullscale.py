@@ -1,9 +1,9 @@
-"""Full-size workloads checked through size-independent properties: every
-Merkle opening the GPU tree produces verifies under the oracle's restatement
-of MerkleTreeMmcs::verify_batch (merkle_tree_mmcs.hpp:168-254) against the
-GPU's root, and the LDEs of the smaller traces match the oracle element by
-element (the large ones are covered by the 2^20 x 256 LDE test); the Goldilocks
-2^18 x 128 workload is compared whole."""
+"""Full-size workloads against the oracle: config 1 (2^20 x 256) and config 3
+(the bench's own 64 traces and quotient) tree layer by tree layer and fold
+value by fold value, the Goldilocks 2^18 x 128 workload whole; and through
+size-independent properties: every Merkle opening the GPU tree produces
+verifies under the oracle's restatement of MerkleTreeMmcs::verify_batch
+(merkle_tree_mmcs.hpp:168-254) against the GPU's root."""
 import os
 
 import numpy as np
@@ -36,14 +36,50 @@ def _verify_openings(tree, heights, widths, n_queries, seed):
         assert not O.mmcs_verify_batch(p, cap, heights, widths, index, bad, list(proof[q]))
 
 
-def test_config1_commit_openings_verify(gpu_ctx):
+def test_config1_commit_every_layer_matches_oracle(gpu_ctx):
+    """Config 1 (2^20 x 256, log_blowup 1): every digest layer of the GPU tree,
+    leaves to root, equals the oracle's tree over the oracle's LDE, and
+    openings verify under the oracle's verify_batch."""
     rng = np.random.default_rng(21)
     t = rng.integers(0, O.BB_P, size=(1 << 20, 256), dtype=np.uint32)
     d = gpu_ctx.to_device(t)
     tree = gpu_ctx.commit_traces_device(P.BABYBEAR, [(d.ptr, 20, 256, 1, 31)], 0)
     _verify_openings(tree, [1 << 21], [256], 12, 1)
+    lde = O.bb_coset_lde(t, 1, 31, True, nthreads=NT)
+    want = O.mmcs_commit(O.bb16_params(), [lde], 0, nthreads=NT)
+    got = tree.layers()
+    assert len(got) == len(want) == 22
+    for g, w in zip(got, want):
+        assert np.array_equal(g, w)
     tree.free()
     d.free()
+
+
+def test_config3_bench_workload_root_and_fold_match_oracle(gpu_ctx):
+    """Config 3 exactly as the bench runs it (bench.config3_inputs: the same
+    seeded 64 traces, 2^19 quotient and beta; the autotuned plan): every digest
+    layer of the one mixed-height tree and the whole fold output equal the
+    oracle's."""
+    import bench
+    shapes, traces, fold_in, beta = bench.config3_inputs(3)
+    bufs = [gpu_ctx.to_device(t) for t in traces]
+    d_fin = gpu_ctx.to_device(fold_in)
+    d_fout = gpu_ctx.alloc((1 << 18) * 16)
+    plan = P.Plan(gpu_ctx, P.BABYBEAR, [(b.ptr, lh, w, 1, 31) for b, (lh, w) in zip(bufs, shapes)], 0,
+                  fold=(d_fin.ptr, d_fout.ptr, 19, 1, beta), n_streams=0)
+    plan.launch()
+    gpu_ctx.sync()
+    got = plan.tree.layers()
+    fold = d_fout.download(np.uint32, (1 << 18, 4))
+    plan.destroy()
+    for b in bufs + [d_fin, d_fout]:
+        b.free()
+    assert np.array_equal(fold, O.fold_matrix_bb4(fold_in, 19, 1, beta, nthreads=NT))
+    ldes = [O.bb_coset_lde(t, 1, 31, True, nthreads=NT) for t in traces]
+    want = O.mmcs_commit(O.bb16_params(), ldes, 0, nthreads=NT)
+    assert len(got) == len(want)
+    for g, w in zip(got, want):
+        assert np.array_equal(g, w)
 
 
 def test_config1_host_commit_equals_device_commit(gpu_ctx):

@@ -105,3 +105,50 @@ def test_plan_goldilocks(gpu_ctx):
     plan.destroy()
     for b in bufs:
         b.free()
+
+
+@pytest.mark.parametrize("n_streams", [1, 3])
+def test_host_input_plan_copies_and_commits(gpu_ctx, n_streams):
+    """p3g_plan_commit_host: traces and the fold input in pinned host memory,
+    copied in by the graph on every launch; the same tree and fold as the
+    oracle, and again after the host buffers are refilled."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(60 + n_streams)
+    traces = _batch(rng, 7, 3, 13, 30)
+    pinned = []
+    for t in traces:
+        pt = torch.empty(t.size, dtype=torch.int32, pin_memory=True)
+        pt.numpy().view(np.uint32)[:] = t.reshape(-1)
+        pinned.append(pt)
+    lh_fold = 11
+    fv = rng.integers(0, O.BB_P, size=(1 << lh_fold, 4), dtype=np.uint32)
+    pf = torch.empty(fv.size, dtype=torch.int32, pin_memory=True)
+    pf.numpy().view(np.uint32)[:] = fv.reshape(-1)
+    beta = rng.integers(0, O.BB_P, size=4, dtype=np.uint32)
+    d_fout = gpu_ctx.alloc((1 << (lh_fold - 1)) * 16)
+    plan = P.Plan(gpu_ctx, P.BABYBEAR, [(p.data_ptr(), t.shape[0].bit_length() - 1, t.shape[1], 1, 31)
+                                        for p, t in zip(pinned, traces)],
+                  fold=(pf.data_ptr(), d_fout.ptr, lh_fold, 1, beta), n_streams=n_streams, host=True)
+    for rep in range(2):
+        if rep == 1:  # new contents in the same host buffers
+            traces = [rng.integers(0, O.BB_P, size=t.shape, dtype=np.uint32) for t in traces]
+            for p, t in zip(pinned, traces):
+                p.numpy().view(np.uint32)[:] = t.reshape(-1)
+        plan.launch()
+        gpu_ctx.sync()
+        want, _ = _oracle_commit(traces, 0)
+        got = plan.tree.layers()
+        assert len(got) == len(want)
+        for g, w in zip(got, want):
+            assert np.array_equal(g, w)
+        assert np.array_equal(d_fout.download(np.uint32, ((1 << (lh_fold - 1)), 4)),
+                              O.fold_matrix_bb4(fv, lh_fold, 1, beta))
+    plan.destroy()
+    d_fout.free()
+
+
+def test_host_input_plan_rejects_pageable_memory(gpu_ctx):
+    t = np.ones((1 << 6, 8), np.uint32)  # numpy memory is pageable
+    with pytest.raises(P.P3GError) as e:
+        P.Plan(gpu_ctx, P.BABYBEAR, [(t.ctypes.data, 6, 8, 1, 31)], n_streams=1, host=True)
+    assert e.value.status == 1

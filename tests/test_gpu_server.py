@@ -1,7 +1,8 @@
 """The continuous-batching serving loop (p3g_server_*): every request's root,
-fold value and openings are identical when it runs alone and when it runs
-mixed with others on several slots, and match the oracle; resident data
-serves openings until released; host-side failure paths return statuses."""
+whole fold output and openings are identical when it runs alone and when it
+runs mixed with others on several slots, and match the oracle; resident data
+serves openings and fold reads until released; host-side failure paths
+return statuses."""
 import time
 
 import numpy as np
@@ -52,7 +53,7 @@ def _run(ctx, reqs, slots, together):
         for rid, t, lh, w, lb, sh, beta in reqs:
             H = 1 << (lh + lb)
             idx = np.array([0, H - 1, H // 3], np.uint64)
-            opens[rid] = server.open(rid, idx, w, lh + lb + 1)
+            opens[rid] = server.open(rid, idx, w, lh + lb + 1) + (server.read_fold(rid, H),)
             server.release(rid)
         assert server.pending()[2] == 0
     finally:
@@ -69,15 +70,17 @@ def test_alone_and_mixed_results_identical_and_match_oracle(gpu_ctx):
         a, m = alone[rid], mixed[rid]
         assert a.status == 0 and m.status == 0
         assert list(a.root) == list(m.root) and list(a.fold_head) == list(m.fold_head)
-        assert np.array_equal(open_a[rid][0], open_m[rid][0]) and np.array_equal(open_a[rid][1], open_m[rid][1])
+        for k in range(3):  # opened rows, Merkle paths, the whole fold output
+            assert np.array_equal(open_a[rid][k], open_m[rid][k])
         assert m.t_submit_ns <= m.t_admit_ns <= m.t_done_ns
-    for rid, t, lh, w, lb, sh, beta in reqs[:8]:
+    for rid, t, lh, w, lb, sh, beta in reqs:
         lde = O.bb_coset_lde(t, lb, sh, True)
         layers = O.mmcs_commit(p, [lde], 0)
         assert list(mixed[rid].root) == layers[-1][0].tolist()
         fold = O.fold_matrix_bb4(np.ascontiguousarray(lde[:, :4]), lh + lb, 1, beta)
         assert list(mixed[rid].fold_head) == fold[0].tolist()
-        rows, proof = open_m[rid]
+        assert np.array_equal(open_m[rid][2], fold)
+        rows, proof, _ = open_m[rid]
         H = 1 << (lh + lb)
         for q, index in enumerate([0, H - 1, H // 3]):
             assert np.array_equal(rows[q], lde[index])
@@ -105,6 +108,8 @@ def test_bad_requests_rejected_on_the_host(gpu_ctx):
             server.submit(2, t.ctypes.data, 4, 8, 1, 0, [0, 0, 0, 0])    # zero shift
         with pytest.raises(P.P3GError):
             server.open(99, [0], 8, 2)                                   # unknown id
+        with pytest.raises(P.P3GError):
+            server.read_fold(99, 16)                                     # unknown id
     finally:
         server.close()
 
