@@ -33,6 +33,7 @@
 // forward transforms).
 #pragma once
 #include <array>
+#include <type_traits>
 #include <vector>
 
 #include "internal.hpp"
@@ -210,13 +211,22 @@ struct TileStore {
         for (int k = 0; k < (1 << LR); ++k) A[SH::addr(base + k, c)] = x[k];
     }
 };
-// Global position p -> p0[p * s] (optionally times post[p]).
-template <class F, bool POST>
+// x * c for a prepared twiddle (F::TW) or a const-form value (F::T); for
+// Goldilocks both are the canonical value and the product is the same.
+template <class F, class P>
+__device__ __forceinline__ typename F::T post_mul(typename F::T x, P c) {
+    if constexpr (std::is_same<P, typename F::TW>::value) return F::mul_tw(x, c);
+    else return F::mulc(x, c);
+}
+
+// Global position p -> p0[p * s] (optionally times post[p]; post holds
+// prepared twiddles or, with P = F::T, const-form values).
+template <class F, bool POST, class P = typename F::TW>
 struct GStore {
     using T = typename F::T;
     T* p0;
     int64_t s;
-    const typename F::TW* post;
+    const P* post;
     bool ok;
     template <int LR>
     __device__ __forceinline__ void group(int base, const T* x) const {
@@ -224,20 +234,21 @@ struct GStore {
         T* q = p0 + base * s;
 #pragma unroll
         for (int k = 0; k < (1 << LR); ++k) {
-            *q = POST ? F::mul_tw(x[k], post[base + k]) : x[k];
+            *q = POST ? post_mul<F>(x[k], post[base + k]) : x[k];
             q += s;
         }
     }
 };
 // Global position p -> p0[bitrev_N(p) * s] * post[p] (pass 1: scratch rows
-// i1 + N1*k2).  With p = g*R + k, bitrev_N(p) = bitrev_r(k) * 2^(N-r) +
-// bitrev_(N-r)(g): walk k in bit-reversed order so the pointer only advances.
+// i1 + N1*k2; post in const form).  With p = g*R + k, bitrev_N(p) =
+// bitrev_r(k) * 2^(N-r) + bitrev_(N-r)(g): walk k in bit-reversed order so
+// the pointer only advances.
 template <class F, int LOGN>
 struct BitrevStore {
     using T = typename F::T;
     T* p0;
     int64_t s;
-    const typename F::TW* post;
+    const T* post;
     bool ok;
     template <int LR>
     __device__ __forceinline__ void group(int base, const T* x) const {
@@ -248,7 +259,7 @@ struct BitrevStore {
 #pragma unroll
         for (int j = 0; j < (1 << LR); ++j) {
             const int k = int(bitrev_ct(unsigned(j), LR));
-            *q = F::mul_tw(x[k], post[base + k]);
+            *q = F::mulc(x[k], post[base + k]);
             q += st;
         }
     }
@@ -376,7 +387,7 @@ k_lde_pass1(const LdeJobs<typename F::T> J, int n1, RootTab<F> roots, const type
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* A = reinterpret_cast<T*>(smem_raw);
     TW* tw = reinterpret_cast<TW*>(A + SH::TILE);
-    TW* post = tw + N;
+    T* post = reinterpret_cast<T*>(tw + N);  // const form
     unsigned local;
     const LdeJob<T>& jb = lde_job(J, 0, local);
     const int w = int(jb.w);
@@ -390,7 +401,7 @@ k_lde_pass1(const LdeJobs<typename F::T> J, int n1, RootTab<F> roots, const type
 
     for (int e = tid; e < N; e += NT) {
         tw[e] = gtwi ? gtwi[e] : F::tw_from_const(roots.omega_inv(LOGN, e));
-        post[e] = F::tw_from_const(roots.omega_inv(n, uint64_t(i1) * bitrev_dev(e, LOGN)));
+        post[e] = roots.omega_inv(n, uint64_t(i1) * bitrev_dev(e, LOGN));
     }
     __syncthreads();
     // scratch is tiled by pass 2's column tiles: element (row r, column col)
@@ -421,7 +432,7 @@ k_lde_pass2(const LdeJobs<typename F::T> J, int n2, int log_b, const typename F:
     TW* twi = reinterpret_cast<TW*>(B + SH::TILE);
     TW* twf = twi + N;
     TW* pre = twf + N;
-    TW* post = pre + N;
+    T* post = reinterpret_cast<T*>(pre + N);  // const form
     unsigned local;
     const LdeJob<T>& jb = lde_job(J, 1, local);
     const int w = int(jb.w);
@@ -451,12 +462,11 @@ k_lde_pass2(const LdeJobs<typename F::T> J, int n2, int log_b, const typename F:
         for (int k = tid; k < N; k += NT) {
             pre[k] = gpre ? gpre[tc * N + k]
                           : F::tw_from_const(F::cmul(sp[k], roots.omega(logH, u * uint64_t(N2) * k)));
-            post[k] = F::tw_from_const(
-                F::cmul(sqk2, roots.omega(logH, uint64_t(k2) * (u + (uint64_t(bitrev_dev(k, LOGN)) << log_b)))));
+            post[k] = F::cmul(sqk2, roots.omega(logH, uint64_t(k2) * (u + (uint64_t(bitrev_dev(k, LOGN)) << log_b))));
         }
         __syncthreads();
         PermLoad<F, SH, LOGN> ld{A, pre, c};
-        GStore<F, true> st{jb.mid + (tc * h + k2) * w + col, N2 * w, post, ok};
+        GStore<F, true, T> st{jb.mid + (tc * h + k2) * w + col, N2 * w, post, ok};
         cta_dif<F, SH, LOGN, C, 0>(B, twf, t, c, ld, st);
         __syncthreads();
     }
@@ -524,7 +534,7 @@ template <class F, int LOGN>
 static void launch_pass1(const LdeJobs<typename F::T>& J, unsigned ctas, int n1, RootTab<F> roots,
                          const typename F::TW* dft_tw, cudaStream_t st) {
     using SH = Tile<F, LOGN, LdeCfg<F>::C13>;
-    size_t smem = SH::TILE * sizeof(typename F::T) + 2 * SH::N * sizeof(typename F::TW);
+    size_t smem = SH::TILE * sizeof(typename F::T) + SH::N * (sizeof(typename F::TW) + sizeof(typename F::T));
     auto k = k_lde_pass1<F, LOGN>;
     set_smem(k, smem);
     k<<<ctas, SH::THREADS, smem, st>>>(J, n1, roots, tw_table<F>(dft_tw, LOGN, true));
@@ -536,7 +546,7 @@ static void launch_pass2(const LdeJobs<typename F::T>& J, unsigned ctas, int n2,
                          const typename F::T* sq, const typename F::TW* pre, RootTab<F> roots,
                          const typename F::TW* dft_tw, cudaStream_t st) {
     using SH = Tile<F, LOGN, LdeCfg<F>::C2>;
-    size_t smem = 2 * SH::TILE * sizeof(typename F::T) + 4 * SH::N * sizeof(typename F::TW);
+    size_t smem = 2 * SH::TILE * sizeof(typename F::T) + SH::N * (3 * sizeof(typename F::TW) + sizeof(typename F::T));
     auto k = k_lde_pass2<F, LOGN>;
     set_smem(k, smem);
     k<<<ctas, SH::THREADS, smem, st>>>(J, n2, log_b, sp, sq, roots, tw_table<F>(dft_tw, LOGN, true),

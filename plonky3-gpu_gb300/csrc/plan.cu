@@ -302,7 +302,16 @@ float time_launches(p3g_plan* plan, int reps) {
 // launch sequence per trace) with the default tree fusion, then the tree's
 // layer fusion (the node counts below which levels run cooperatively and
 // fuse into one tail CTA).  Leaves the plan captured with the best choice.
-void tune(p3g_ctx* ctx, p3g_plan* plan) {
+// When P3G_TUNE_LOG names a file, every candidate's time is appended to it.
+void tune(p3g_ctx* ctx, p3g_plan* plan, const std::string& key) {
+    const char* log_path = std::getenv("P3G_TUNE_LOG");
+    std::ofstream log;
+    if (log_path) log.open(log_path, std::ios::app);
+    auto note = [&](int k, bool g, uint64_t tail, uint64_t coop, float ms) {
+        if (log.is_open())
+            log << key << " streams=" << k << " grouped=" << g << " tail=" << tail << " coop=" << coop << " ms=" << ms
+                << "\n";
+    };
     const int nt = int(plan->traces.size());
     int best_k = 1;
     bool best_g = true;
@@ -312,6 +321,7 @@ void tune(p3g_ctx* ctx, p3g_plan* plan) {
             if (k > nt && k > 1) break;
             capture(ctx, plan, k, gr != 0);
             const float ms = time_launches(plan, 2);
+            note(k, gr != 0, 0, 0, ms);
             if (ms < best_ms) {
                 best_ms = ms;
                 best_k = k;
@@ -328,6 +338,7 @@ void tune(p3g_ctx* ctx, p3g_plan* plan) {
         plan->tree.coop_max = f.second;
         capture(ctx, plan, best_k, best_g);
         const float ms = time_launches(plan, 2);
+        note(best_k, best_g, f.first, f.second, ms);
         if (ms < best_ms) {
             best_ms = ms;
             best_t = f.first;
@@ -468,7 +479,7 @@ int plan_commit(p3g_ctx* ctx, int field, const p3g_trace* traces, size_t n_trace
                     plan->tree.coop_max = uint64_t(kc->second);
                     p3g::capture(ctx, plan.get(), ks->second, kg->second != 0);
                 } else {
-                    p3g::tune(ctx, plan.get());
+                    p3g::tune(ctx, plan.get(), key);
                     p3g::g_tune[key + "/streams"] = plan->nstreams;
                     p3g::g_tune[key + "/grouped"] = plan->grouped ? 1 : 0;
                     p3g::g_tune[key + "/tail"] = int(plan->tree.tail_max);

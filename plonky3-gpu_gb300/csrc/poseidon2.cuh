@@ -190,14 +190,15 @@ __device__ __forceinline__ uint32_t p2_bb16_coop(uint32_t x, const P2BB16& p, co
 }
 
 // ------------------------------------------------------------------ Goldilocks 8
-// x^d with the intermediate powers left below 2^64 but unreduced mod p
-// (a product accepts any u64 operands); only the result is canonical.
+// The state words are kept below 2^64 but not reduced mod p inside the
+// permutation (every product and linear layer accepts any u64 operands);
+// squeezing makes them canonical.  x^d with every product left unreduced.
 __device__ __forceinline__ uint64_t gl_sbox(uint64_t x, int d) {
     uint64_t x2 = gl::mul_lazy(x, x);
-    if (d == 3) return gl::mul(x2, x);
-    if (d == 5) return gl::mul(gl::mul_lazy(x2, x2), x);
+    if (d == 3) return gl::mul_lazy(x2, x);
+    if (d == 5) return gl::mul_lazy(gl::mul_lazy(x2, x2), x);
     uint64_t x3 = gl::mul_lazy(x2, x), x4 = gl::mul_lazy(x2, x2);
-    return gl::mul(x3, x4);
+    return gl::mul_lazy(x3, x4);
 }
 // Goldilocks linear layers on unreduced sums: a G2 is lo + hi * 2^64 with a
 // small hi (a carry count), added with one three-limb carry chain and
@@ -220,18 +221,19 @@ __device__ __forceinline__ G2 g2add(G2 a, G2 b) {
           "r"(uint32_t(b.lo >> 32)), "r"(b.hi));
     return {(uint64_t(l1) << 32) | l0, h};
 }
-// canonical value of a G2 (hi < 2^32)
+// a value below 2^64 congruent to a G2 (hi < 2^32)
 __device__ __forceinline__ uint64_t g2red(G2 a) {
     const uint64_t t = (uint64_t(a.hi) << 32) - a.hi;  // hi * (2^32 - 1) <= (2^32 - 1)^2
     uint64_t s = a.lo + t;
     if (s < t) s += gl::EPS;  // wrapped: + 2^64 = + EPS; s < t keeps this below 2^64
-    return s >= gl::P ? s - gl::P : s;
+    return s;
 }
 // x * 2^k as a G2, 1 <= k < 32
 __device__ __forceinline__ G2 g2shl(uint64_t x, int k) { return {x << k, uint32_t(x >> (64 - k))}; }
 
 // MDS-light for width 8 (external.hpp:67-77, 170-201): [2 3 1 1] on each
-// 4-chunk, then the column sums; every output is a sum of at most 21 inputs.
+// 4-chunk, then the column sums; every output is a sum of at most 21 inputs
+// below 2^64, so its carry count stays below 2^5.
 __device__ __forceinline__ void mds_light_gl8(uint64_t* s) {
     G2 y[8];
 #pragma unroll
@@ -252,8 +254,8 @@ __device__ __forceinline__ void mds_light_gl8(uint64_t* s) {
         s[k + 4] = g2red(g2add(y[k + 4], col));
     }
 }
-// s + c for canonical c; the result is below 2^64 but possibly >= p (an
-// S-box input: products accept any u64)
+// s + c for any s < 2^64 and canonical c; the result is below 2^64 but
+// possibly >= p (an S-box input: products accept any u64)
 __device__ __forceinline__ uint64_t gl_add_lazy(uint64_t a, uint64_t c) {
     uint64_t t = a + c;
     if (t < c) t += gl::EPS;  // a + c - 2^64 < 2^64 - 2^33 leaves room for EPS
@@ -273,10 +275,9 @@ __device__ __forceinline__ void p2_gl8(uint64_t* s, const P2GL8& p) {
     for (int r = 0; r < RP; ++r) {
         // internal layer (generic.hpp:148-175): s_i <- s_i * 2^i + sum(s)
         s[0] = gl_sbox(gl_add_lazy(s[0], p.internal[r]), D);
-        G2 acc = g2(s[0]);
+        G2 sum = g2(s[0]);  // carry count below 8, left unreduced
 #pragma unroll
-        for (int i = 1; i < 8; ++i) acc = g2add(acc, g2(s[i]));
-        const G2 sum = g2(g2red(acc));
+        for (int i = 1; i < 8; ++i) sum = g2add(sum, g2(s[i]));
         s[0] = g2red(g2add(g2(s[0]), sum));
 #pragma unroll
         for (int i = 1; i < 8; ++i) s[i] = g2red(g2add(g2shl(s[i], i), sum));
@@ -306,7 +307,8 @@ struct HGL {
     using Params = P2GL8;
     static constexpr int W = 8, RATE = 4, DIG = 4;
     static __host__ __device__ __forceinline__ T absorb(T canonical) { return canonical; }
-    static __device__ __forceinline__ T squeeze(T v) { return v; }
+    // the permutation leaves words below 2^64, not necessarily below p
+    static __device__ __forceinline__ T squeeze(T v) { return v >= gl::P ? v - gl::P : v; }
     static __device__ __forceinline__ T from_u32(uint32_t x) { return x; }  // goldilocks.hpp:34
     template <int D, int RF, int RP>
     static __device__ __forceinline__ void perm(T* s, const Params& p) { p2_gl8<D, RF, RP>(s, p); }

@@ -195,6 +195,33 @@ def test_commit_pipeline_batched_vs_oracle(gpu_ctx):
         b.free()
 
 
+@pytest.mark.parametrize("field", ["bb", "gl"])
+def test_commit_traces_same_shape_batches_vs_oracle(gpu_ctx, field):
+    """Traces sharing (log_h, log_blowup, shift) run as one LDE batch (one
+    launch per pass for the whole group, single-kernel and three-pass heights,
+    ragged widths, a zero-width trace among them): the same tree as the oracle."""
+    rng = np.random.default_rng(91 if field == "bb" else 92)
+    fid, p, dt, shift, params = ((P.BABYBEAR, O.BB_P, np.uint32, 31, O.bb16_params()) if field == "bb"
+                                 else (P.GOLDILOCKS, O.GL_P, np.uint64, 7, O.gl8_params()))
+    shapes = [(11, 5), (11, 40), (6, 3), (11, 17), (6, 30), (13, 9), (11, 1), (13, 24), (6, 0), (6, 16)]
+    traces = [rng.integers(0, p, size=(1 << lh, w), dtype=dt) for lh, w in shapes]
+    bufs = [gpu_ctx.to_device(t) if t.size else None for t in traces]
+    tree = gpu_ctx.commit_traces_device(fid, [(b.ptr if b else 0, lh, w, 2, shift)
+                                              for b, (lh, w) in zip(bufs, shapes)], 0)
+    lde = O.bb_coset_lde if field == "bb" else O.gl_coset_lde
+    ldes = [lde(t, 2, shift, True) if t.size else np.zeros((1 << (lh + 2), 0), dt)
+            for t, (lh, w) in zip(traces, shapes)]
+    want = O.mmcs_commit(params, ldes, 0, nthreads=NT)
+    got = tree.layers()
+    assert len(got) == len(want)
+    for g, w in zip(got, want):
+        assert np.array_equal(g, w)
+    tree.free()
+    for b in bufs:
+        if b:
+            b.free()
+
+
 def test_missing_poseidon2_is_an_error():
     ctx = P.Context(0)
     try:
