@@ -277,27 +277,35 @@ void capture(p3g_ctx* ctx, p3g_plan* plan, int k, bool grouped) {
     plan->grouped = grouped;
 }
 
+// The fastest of `reps` launches after a warm one (the minimum: host-input
+// plans see occasional host-to-device copy stalls that have nothing to do
+// with the candidate).
 float time_launches(p3g_plan* plan, int reps) {
     cudaStream_t st;
     P3G_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
-    cudaEvent_t a, b;
-    P3G_CUDA(cudaEventCreate(&a));
-    P3G_CUDA(cudaEventCreate(&b));
+    std::vector<cudaEvent_t> ev(reps + 1);
+    for (auto& e : ev) P3G_CUDA(cudaEventCreate(&e));
     P3G_CUDA(cudaGraphLaunch(plan->exec, st));  // warm
-    P3G_CUDA(cudaEventRecord(a, st));
-    for (int i = 0; i < reps; ++i) P3G_CUDA(cudaGraphLaunch(plan->exec, st));
-    P3G_CUDA(cudaEventRecord(b, st));
-    P3G_CUDA(cudaEventSynchronize(b));
-    float ms = 0;
-    P3G_CUDA(cudaEventElapsedTime(&ms, a, b));
-    cudaEventDestroy(a);
-    cudaEventDestroy(b);
+    P3G_CUDA(cudaEventRecord(ev[0], st));
+    for (int i = 0; i < reps; ++i) {
+        P3G_CUDA(cudaGraphLaunch(plan->exec, st));
+        P3G_CUDA(cudaEventRecord(ev[i + 1], st));
+    }
+    P3G_CUDA(cudaEventSynchronize(ev[reps]));
+    float best = 1e30f;
+    for (int i = 0; i < reps; ++i) {
+        float ms = 0;
+        P3G_CUDA(cudaEventElapsedTime(&ms, ev[i], ev[i + 1]));
+        best = std::min(best, ms);
+    }
+    for (auto e : ev) cudaEventDestroy(e);
     cudaStreamDestroy(st);
-    return ms / float(reps);
+    return best;
 }
 
 // --------------------------------------------------------------- autotuner
-// Coordinate search, each candidate captured and timed over two launches:
+// Coordinate search, each candidate captured and timed (the fastest of three
+// launches):
 // first the LDE stage (1, 2, 4 or 8 streams x shape-group batches or one
 // launch sequence per trace) with the default tree fusion, then the tree's
 // layer fusion (the node counts below which levels run cooperatively and
@@ -320,7 +328,7 @@ void tune(p3g_ctx* ctx, p3g_plan* plan, const std::string& key) {
         for (int k : {1, 2, 4, 8}) {
             if (k > nt && k > 1) break;
             capture(ctx, plan, k, gr != 0);
-            const float ms = time_launches(plan, 2);
+            const float ms = time_launches(plan, 3);
             note(k, gr != 0, 0, 0, ms);
             if (ms < best_ms) {
                 best_ms = ms;
@@ -337,7 +345,7 @@ void tune(p3g_ctx* ctx, p3g_plan* plan, const std::string& key) {
         plan->tree.tail_max = f.first;
         plan->tree.coop_max = f.second;
         capture(ctx, plan, best_k, best_g);
-        const float ms = time_launches(plan, 2);
+        const float ms = time_launches(plan, 3);
         note(best_k, best_g, f.first, f.second, ms);
         if (ms < best_ms) {
             best_ms = ms;
