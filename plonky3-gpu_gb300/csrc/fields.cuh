@@ -100,16 +100,53 @@ namespace gl {
 constexpr uint64_t P = 0xFFFFFFFF00000001ull;
 constexpr uint64_t EPS = 0xFFFFFFFFull;  // 2^64 mod p
 
-P3G_HD uint64_t add(uint64_t a, uint64_t b) {  // canonical in/out
+// Canonical in and out.  On the device both run as 32-bit carry chains: the
+// correction is applied by a carry or borrow mask instead of 64-bit
+// compares and selects.
+P3G_HD uint64_t add(uint64_t a, uint64_t b) {
+#ifdef __CUDA_ARCH__
+    // s = a + b with carry c; t = s - p with borrow; a + b >= p exactly when
+    // c is set or t did not borrow, and then a + b - p = t (mod 2^64)
+    uint32_t s0, s1, c, t0, t1, bw;
+    asm("{\n\t"
+        "add.cc.u32 %0, %6, %8;\n\t"
+        "addc.cc.u32 %1, %7, %9;\n\t"
+        "addc.u32 %2, 0, 0;\n\t"
+        "sub.cc.u32 %3, %0, 1;\n\t"
+        "subc.cc.u32 %4, %1, 0xffffffff;\n\t"
+        "subc.u32 %5, 0, 0;\n\t"
+        "}"
+        : "=&r"(s0), "=&r"(s1), "=&r"(c), "=&r"(t0), "=&r"(t1), "=&r"(bw)
+        : "r"(uint32_t(a)), "r"(uint32_t(a >> 32)), "r"(uint32_t(b)), "r"(uint32_t(b >> 32)));
+    const bool ge = c != 0 || bw == 0;
+    return ge ? (uint64_t(t1) << 32) | t0 : (uint64_t(s1) << 32) | s0;
+#else
     uint64_t s = a + b;
     if (s < a) s += EPS;          // wrapped: true sum = s + 2^64 = s + EPS (mod p), < p
     else if (s >= P) s -= P;
     return s;
+#endif
 }
 P3G_HD uint64_t sub(uint64_t a, uint64_t b) {
+#ifdef __CUDA_ARCH__
+    // d = a - b; a borrow wraps by 2^64 = EPS (mod p): subtract EPS, i.e.
+    // the borrow mask m = 0xffffffff from the low word
+    uint32_t d0, d1, m;
+    asm("{\n\t"
+        "sub.cc.u32 %0, %3, %5;\n\t"
+        "subc.cc.u32 %1, %4, %6;\n\t"
+        "subc.u32 %2, 0, 0;\n\t"
+        "sub.cc.u32 %0, %0, %2;\n\t"
+        "subc.u32 %1, %1, 0;\n\t"
+        "}"
+        : "=&r"(d0), "=&r"(d1), "=&r"(m)
+        : "r"(uint32_t(a)), "r"(uint32_t(a >> 32)), "r"(uint32_t(b)), "r"(uint32_t(b >> 32)));
+    return (uint64_t(d1) << 32) | d0;
+#else
     uint64_t d = a - b;
     if (a < b) d -= EPS;          // d + 2^64 - 2^64 + p = d - EPS
     return d;
+#endif
 }
 P3G_HD uint64_t reduce128(uint64_t lo, uint64_t hi) {
     uint64_t hh = hi >> 32, hl = hi & EPS;
@@ -159,7 +196,7 @@ __device__ __forceinline__ uint64_t mul_lazy(uint64_t a, uint64_t b) {
         "subc.cc.u32 %1, %4, 0;\n\t"
         "subc.u32 %2, 0, 0;\n\t"  // m = 0 or 0xffffffff (borrow)
         "}"
-        : "=r"(t0), "=r"(t1), "=r"(m)
+        : "=&r"(t0), "=&r"(t1), "=&r"(m)
         : "r"(r0), "r"(r1), "r"(r3));
     asm("{\n\t"
         "sub.cc.u32 %0, %0, %2;\n\t"  // t -= EPS & m: EPS = {0xffffffff, 0}
@@ -175,7 +212,7 @@ __device__ __forceinline__ uint64_t mul_lazy(uint64_t a, uint64_t b) {
         "addc.cc.u32 %1, %4, nhi;\n\t"
         "addc.u32 %2, 0, 0;\n\t"      // c = carry
         "}"
-        : "=r"(u0), "=r"(u1), "=r"(c)
+        : "=&r"(u0), "=&r"(u1), "=&r"(c)
         : "r"(t0), "r"(t1), "r"(r2));
     asm("{\n\t"
         ".reg .u32 mc;\n\t"

@@ -307,7 +307,8 @@ float time_launches(p3g_plan* plan, int reps) {
 // Coordinate search, each candidate captured and timed (the fastest of three
 // launches):
 // first the LDE stage (1, 2, 4 or 8 streams x shape-group batches or one
-// launch sequence per trace) with the default tree fusion, then the tree's
+// launch sequence per trace, which must be more than 1% faster to be taken)
+// with the default tree fusion, then the tree's
 // layer fusion (the node counts below which levels run cooperatively and
 // fuse into one tail CTA).  Leaves the plan captured with the best choice.
 // When P3G_TUNE_LOG names a file, every candidate's time is appended to it.
@@ -330,7 +331,9 @@ void tune(p3g_ctx* ctx, p3g_plan* plan, const std::string& key) {
             capture(ctx, plan, k, gr != 0);
             const float ms = time_launches(plan, 3);
             note(k, gr != 0, 0, 0, ms);
-            if (ms < best_ms) {
+            // per-trace launch sequences must win by more than 1%: otherwise
+            // the shape-group batches (far fewer graph nodes) are kept
+            if (ms < (gr ? 1.0f : 0.99f) * best_ms) {
                 best_ms = ms;
                 best_k = k;
                 best_g = gr != 0;

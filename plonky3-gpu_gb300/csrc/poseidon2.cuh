@@ -216,7 +216,7 @@ __device__ __forceinline__ G2 g2add(G2 a, G2 b) {
         "addc.cc.u32 %1, %4, %7;\n\t"
         "addc.u32 %2, %5, %8;\n\t"
         "}"
-        : "=r"(l0), "=r"(l1), "=r"(h)
+        : "=&r"(l0), "=&r"(l1), "=&r"(h)
         : "r"(uint32_t(a.lo)), "r"(uint32_t(a.lo >> 32)), "r"(a.hi), "r"(uint32_t(b.lo)),
           "r"(uint32_t(b.lo >> 32)), "r"(b.hi));
     return {(uint64_t(l1) << 32) | l0, h};
