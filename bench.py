@@ -523,10 +523,37 @@ def run_case(args):
     """One kernel sequence on its own, for profiling: `--case
     lde|commit:bb|gl:LOG_H:WIDTH:LOG_B` runs the coset LDE (bit-reversed rows)
     or the whole commit of one seeded trace, `warmup` untimed and `steps` timed
-    calls (CUDA events), and prints their mean."""
+    calls (CUDA events), and prints their mean; `--case c3lde` runs the
+    headline's LDE stage as the bench times it (the 64 config-3 LDEs, one
+    p3g_coset_lde call each, on one stream)."""
     import torch
     import p3g_gb300 as P
 
+    if args.case == "c3lde":
+        dev = torch.device("cuda", 0)
+        torch.cuda.set_device(0)
+        stream = torch.cuda.Stream(device=dev)
+        sptr = stream.cuda_stream
+        ctx = P.Context(0)
+        shapes, traces, _, _ = config3_inputs(3, args.c3_shrink)
+        d_in = [ctx.to_device(t) for t in traces]
+        d_out = [ctx.alloc(t.nbytes << C3_LOG_B) for t in traces]
+        ctx.sync()
+
+        def ldes():
+            for (lh, w), a, b in zip(shapes, d_in, d_out):
+                ctx.coset_lde_device(P.BABYBEAR, a.ptr, lh, w, C3_LOG_B, SHIFT, True, b.ptr, sptr)
+
+        for _ in range(args.warmup):
+            ldes()
+        ms = statistics.mean(events_timed(torch, dev, stream, ldes, args.steps))
+        nbytes = sum(4 * w * ((1 << lh) + (1 << (lh + C3_LOG_B))) for lh, w in shapes)
+        print(json.dumps({"case": args.case, "ms": ms, "algorithmic_bytes": nbytes,
+                          "algorithmic_gbs": nbytes / (ms / 1e3) / 1e9}))
+        for b in d_in + d_out:
+            b.free()
+        ctx.close()
+        return 0
     kind, field, log_h, width, log_b = args.case.split(":")
     log_h, width, log_b = int(log_h), int(width), int(log_b)
     gl = field == "gl"
@@ -832,7 +859,8 @@ def main():
                          "baseline of the GPU arm uses 2^(k-1))")
     ap.add_argument("--log-h", type=int, default=C1_LOG_H, help="config-1 trace log2 height (profiling cases)")
     ap.add_argument("--width", type=int, default=C1_WIDTH, help="config-1 trace width (profiling cases)")
-    ap.add_argument("--case", default="", help="profiling: lde|commit:bb|gl:LOG_H:WIDTH:LOG_B alone")
+    ap.add_argument("--case", default="",
+                    help="profiling: lde|commit:bb|gl:LOG_H:WIDTH:LOG_B alone, or c3lde (the headline's LDE stage)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
