@@ -7,9 +7,15 @@
 // terminal full rounds.  MDS-light applies the circulant [2 3 1 1] to each
 // 4-chunk and adds the column sums (external.hpp:67-77, 170-201).
 //
-// The state is held in registers (fully unrolled), round constants come from
-// the kernel-parameter struct (constant bank), and BabyBear runs in
-// Montgomery form so that x^D is a chain of single Montgomery products.
+// The state is held in registers, round constants come from the
+// kernel-parameter struct (constant bank), and BabyBear runs in Montgomery
+// form so that x^D is a chain of single Montgomery products.  Each round's
+// body is unrolled over the state words, but the rounds themselves stay a
+// loop: the fully unrolled permutation (about 5,600 instructions for BabyBear,
+// 12,500 for Goldilocks) overflowed the instruction cache, and warps waited
+// for instructions more than for the multiplier (ncu: "no instruction" the
+// top stall, issue active about 50%).  Rolled, the isolated permutation runs
+// 16% (BabyBear) and 21% (Goldilocks) faster.
 #pragma once
 #include "internal.hpp"
 
@@ -102,13 +108,13 @@ __device__ __forceinline__ uint32_t bbadd(uint32_t a, uint32_t b) { return bb::a
 template <int D, int RF, int RP>
 __device__ __forceinline__ void p2_bb16(uint32_t* s, const P2BB16& p) {
     mds_light<uint32_t, 16, bbadd>(s);
-#pragma unroll
+#pragma unroll 1
     for (int r = 0; r < RF / 2; ++r) {
 #pragma unroll
         for (int i = 0; i < 16; ++i) s[i] = bb_sbox(bb_add_rc(s[i], p.initial[r][i]), D);
         mds_light<uint32_t, 16, bbadd>(s);
     }
-#pragma unroll
+#pragma unroll 1
     for (int r = 0; r < RP; ++r) {
         s[0] = bb_sbox(bb_add_rc(s[0], p.internal[r]), D);
         const uint32_t sum = bb_sum16(s);
@@ -116,7 +122,7 @@ __device__ __forceinline__ void p2_bb16(uint32_t* s, const P2BB16& p) {
 #pragma unroll
         for (int i = 1; i < 16; ++i) s[i] = bb::add(bb_mul_pow2(s[i], i), sum);
     }
-#pragma unroll
+#pragma unroll 1
     for (int r = 0; r < RF / 2; ++r) {
 #pragma unroll
         for (int i = 0; i < 16; ++i) s[i] = bb_sbox(bb_add_rc(s[i], p.terminal[r][i]), D);
@@ -265,13 +271,13 @@ __device__ __forceinline__ uint64_t gl_add_lazy(uint64_t a, uint64_t c) {
 template <int D, int RF, int RP>
 __device__ __forceinline__ void p2_gl8(uint64_t* s, const P2GL8& p) {
     mds_light_gl8(s);
-#pragma unroll
+#pragma unroll 1
     for (int r = 0; r < RF / 2; ++r) {
 #pragma unroll
         for (int i = 0; i < 8; ++i) s[i] = gl_sbox(gl_add_lazy(s[i], p.initial[r][i]), D);
         mds_light_gl8(s);
     }
-#pragma unroll
+#pragma unroll 1
     for (int r = 0; r < RP; ++r) {
         // internal layer (generic.hpp:148-175): s_i <- s_i * 2^i + sum(s)
         s[0] = gl_sbox(gl_add_lazy(s[0], p.internal[r]), D);
@@ -282,7 +288,7 @@ __device__ __forceinline__ void p2_gl8(uint64_t* s, const P2GL8& p) {
 #pragma unroll
         for (int i = 1; i < 8; ++i) s[i] = g2red(g2add(g2shl(s[i], i), sum));
     }
-#pragma unroll
+#pragma unroll 1
     for (int r = 0; r < RF / 2; ++r) {
 #pragma unroll
         for (int i = 0; i < 8; ++i) s[i] = gl_sbox(gl_add_lazy(s[i], p.terminal[r][i]), D);
