@@ -73,6 +73,12 @@ struct LdeCfg<FGL> {
 #define P3G_LDE_MINB2 2
 #endif
 
+// Resident CTAs per SM that pass 2's launch bounds ask for: at least
+// P3G_LDE_MINB2 and enough for 16 warps, so a 128-thread tile (2^9 rows and
+// fewer) gets the 128-register budget of the 256-thread one instead of
+// 173 registers and 12% of the warps (measured at 2^18 x 128).
+constexpr int lde_minb2(int threads) { return 512 / threads > P3G_LDE_MINB2 ? 512 / threads : P3G_LDE_MINB2; }
+
 constexpr int LDE_SINGLE_MAX = 10;  // single-kernel LDE up to h = 2^10
 constexpr int LDE_PASS_MAX = 21;    // three-pass LDE up to h = 2^21
 // above it, one more split h = 2^21 * B with B <= 32 (dft.cuh, big_run; B is
@@ -417,7 +423,8 @@ k_lde_pass1(const LdeJobs<typename F::T> J, int n1, RootTab<F> roots, const type
 
 // ------------------------------------------------------------ pass 2 (LOGN = n1)
 template <class F, int LOGN>
-__global__ void __launch_bounds__(Tile<F, LOGN, LdeCfg<F>::C2>::THREADS, P3G_LDE_MINB2)
+__global__ void __launch_bounds__(Tile<F, LOGN, LdeCfg<F>::C2>::THREADS,
+                                  lde_minb2(Tile<F, LOGN, LdeCfg<F>::C2>::THREADS))
 k_lde_pass2(const LdeJobs<typename F::T> J, int n2, int log_b, const typename F::T* __restrict__ sp,
             const typename F::T* __restrict__ sq, RootTab<F> roots, const typename F::TW* __restrict__ gtwi,
             const typename F::TW* __restrict__ gtwf, const typename F::TW* __restrict__ gpre) {

@@ -328,7 +328,7 @@ __global__ void __launch_bounds__(128) k_grind(typename H::Params p, const Grind
 #pragma unroll 1
         for (int pass = 0; pass < passes; ++pass) {
             if (pass == 1) s[0] = hi;
-            H::template perm<D, RF, RP>(s, p);
+            H::template perm<D, RF, RP, false>(s, p);
         }
         if ((uint64_t(H::squeeze(s[H::RATE - 1])) & a.mask) == 0) atomicMin(found, c);
     }

@@ -104,30 +104,41 @@ __device__ __forceinline__ void mds_light(T* s) {
 
 __device__ __forceinline__ uint32_t bbadd(uint32_t a, uint32_t b) { return bb::add(a, b); }
 
-// State in Montgomery form.
-template <int D, int RF, int RP>
+// Calls f(r) for r = 0 .. N-1, as a loop (ROLL) or unrolled.
+template <bool ROLL, int N, class Fn>
+__device__ __forceinline__ void rounds(const Fn& f) {
+    if constexpr (ROLL) {
+#pragma unroll 1
+        for (int r = 0; r < N; ++r) f(r);
+    } else {
+#pragma unroll
+        for (int r = 0; r < N; ++r) f(r);
+    }
+}
+
+// State in Montgomery form.  ROLL: the round loops stay loops (the default;
+// the proof-of-work search, whose candidate loop wraps the permutation, ran
+// faster unrolled when measured).
+template <int D, int RF, int RP, bool ROLL = true>
 __device__ __forceinline__ void p2_bb16(uint32_t* s, const P2BB16& p) {
     mds_light<uint32_t, 16, bbadd>(s);
-#pragma unroll 1
-    for (int r = 0; r < RF / 2; ++r) {
+    rounds<ROLL, RF / 2>([&](int r) {
 #pragma unroll
         for (int i = 0; i < 16; ++i) s[i] = bb_sbox(bb_add_rc(s[i], p.initial[r][i]), D);
         mds_light<uint32_t, 16, bbadd>(s);
-    }
-#pragma unroll 1
-    for (int r = 0; r < RP; ++r) {
+    });
+    rounds<ROLL, RP>([&](int r) {
         s[0] = bb_sbox(bb_add_rc(s[0], p.internal[r]), D);
         const uint32_t sum = bb_sum16(s);
         s[0] = bb::add(s[0], sum);  // diag[0] = 1
 #pragma unroll
         for (int i = 1; i < 16; ++i) s[i] = bb::add(bb_mul_pow2(s[i], i), sum);
-    }
-#pragma unroll 1
-    for (int r = 0; r < RF / 2; ++r) {
+    });
+    rounds<ROLL, RF / 2>([&](int r) {
 #pragma unroll
         for (int i = 0; i < 16; ++i) s[i] = bb_sbox(bb_add_rc(s[i], p.terminal[r][i]), D);
         mds_light<uint32_t, 16, bbadd>(s);
-    }
+    });
 }
 
 // ------------------------------------------------------------------ BabyBear 16, one lane per word
@@ -268,17 +279,15 @@ __device__ __forceinline__ uint64_t gl_add_lazy(uint64_t a, uint64_t c) {
     return t;
 }
 
-template <int D, int RF, int RP>
+template <int D, int RF, int RP, bool ROLL = true>
 __device__ __forceinline__ void p2_gl8(uint64_t* s, const P2GL8& p) {
     mds_light_gl8(s);
-#pragma unroll 1
-    for (int r = 0; r < RF / 2; ++r) {
+    rounds<ROLL, RF / 2>([&](int r) {
 #pragma unroll
         for (int i = 0; i < 8; ++i) s[i] = gl_sbox(gl_add_lazy(s[i], p.initial[r][i]), D);
         mds_light_gl8(s);
-    }
-#pragma unroll 1
-    for (int r = 0; r < RP; ++r) {
+    });
+    rounds<ROLL, RP>([&](int r) {
         // internal layer (generic.hpp:148-175): s_i <- s_i * 2^i + sum(s)
         s[0] = gl_sbox(gl_add_lazy(s[0], p.internal[r]), D);
         G2 sum = g2(s[0]);  // carry count below 8, left unreduced
@@ -287,13 +296,12 @@ __device__ __forceinline__ void p2_gl8(uint64_t* s, const P2GL8& p) {
         s[0] = g2red(g2add(g2(s[0]), sum));
 #pragma unroll
         for (int i = 1; i < 8; ++i) s[i] = g2red(g2add(g2shl(s[i], i), sum));
-    }
-#pragma unroll 1
-    for (int r = 0; r < RF / 2; ++r) {
+    });
+    rounds<ROLL, RF / 2>([&](int r) {
 #pragma unroll
         for (int i = 0; i < 8; ++i) s[i] = gl_sbox(gl_add_lazy(s[i], p.terminal[r][i]), D);
         mds_light_gl8(s);
-    }
+    });
 }
 
 // ------------------------------------------------------------------ field-generic sponge glue
@@ -305,8 +313,8 @@ struct HBB {
     static __device__ __forceinline__ T squeeze(T m) { return bb::canon(bb::smul(int32_t(m), 1)); }
     // BabyBear(uint32_t) reduces its argument (baby_bear.hpp:51)
     static __device__ __forceinline__ T from_u32(uint32_t x) { return x % bb::P; }
-    template <int D, int RF, int RP>
-    static __device__ __forceinline__ void perm(T* s, const Params& p) { p2_bb16<D, RF, RP>(s, p); }
+    template <int D, int RF, int RP, bool ROLL = true>
+    static __device__ __forceinline__ void perm(T* s, const Params& p) { p2_bb16<D, RF, RP, ROLL>(s, p); }
 };
 struct HGL {
     using T = uint64_t;
@@ -316,8 +324,8 @@ struct HGL {
     // the permutation leaves words below 2^64, not necessarily below p
     static __device__ __forceinline__ T squeeze(T v) { return v >= gl::P ? v - gl::P : v; }
     static __device__ __forceinline__ T from_u32(uint32_t x) { return x; }  // goldilocks.hpp:34
-    template <int D, int RF, int RP>
-    static __device__ __forceinline__ void perm(T* s, const Params& p) { p2_gl8<D, RF, RP>(s, p); }
+    template <int D, int RF, int RP, bool ROLL = true>
+    static __device__ __forceinline__ void perm(T* s, const Params& p) { p2_gl8<D, RF, RP, ROLL>(s, p); }
 };
 
 }  // namespace p3g
