@@ -31,7 +31,9 @@ def nvcc() -> str:
 
 
 def _flags():
-    return ARCH + [
+    # P3G_NVCC_FLAGS: extra nvcc flags (e.g. -D settings of the kernels' build-time knobs)
+    extra = os.environ.get("P3G_NVCC_FLAGS", "").split()
+    return ARCH + extra + [
         "-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",
         "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
         "-I", os.path.join(REPO, "include"), "-I", CSRC,

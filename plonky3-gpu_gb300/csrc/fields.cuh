@@ -131,15 +131,16 @@ P3G_HD uint64_t sub(uint64_t a, uint64_t b) {
 #ifdef __CUDA_ARCH__
     // d = a - b; a borrow wraps by 2^64 = EPS (mod p): subtract EPS, i.e.
     // the borrow mask m = 0xffffffff from the low word
-    uint32_t d0, d1, m;
+    uint32_t d0, d1;
     asm("{\n\t"
-        "sub.cc.u32 %0, %3, %5;\n\t"
-        "subc.cc.u32 %1, %4, %6;\n\t"
-        "subc.u32 %2, 0, 0;\n\t"
-        "sub.cc.u32 %0, %0, %2;\n\t"
+        ".reg .u32 m;\n\t"
+        "sub.cc.u32 %0, %2, %4;\n\t"
+        "subc.cc.u32 %1, %3, %5;\n\t"
+        "subc.u32 m, 0, 0;\n\t"
+        "sub.cc.u32 %0, %0, m;\n\t"
         "subc.u32 %1, %1, 0;\n\t"
         "}"
-        : "=&r"(d0), "=&r"(d1), "=&r"(m)
+        : "=&r"(d0), "=&r"(d1)
         : "r"(uint32_t(a)), "r"(uint32_t(a >> 32)), "r"(uint32_t(b)), "r"(uint32_t(b >> 32)));
     return (uint64_t(d1) << 32) | d0;
 #else

@@ -77,7 +77,11 @@ struct LdeCfg<FGL> {
 // P3G_LDE_MINB2 and enough for 16 warps, so a 128-thread tile (2^9 rows and
 // fewer) gets the 128-register budget of the 256-thread one instead of
 // 173 registers and 12% of the warps (measured at 2^18 x 128).
-constexpr int lde_minb2(int threads) { return 512 / threads > P3G_LDE_MINB2 ? 512 / threads : P3G_LDE_MINB2; }
+// (At most 16: tiny tiles of a few threads would ask for more CTAs than an
+// SM holds.)
+constexpr int lde_minb2(int threads) {
+    return 512 / threads > P3G_LDE_MINB2 ? (512 / threads < 16 ? 512 / threads : 16) : P3G_LDE_MINB2;
+}
 
 constexpr int LDE_SINGLE_MAX = 10;  // single-kernel LDE up to h = 2^10
 constexpr int LDE_PASS_MAX = 21;    // three-pass LDE up to h = 2^21

@@ -138,6 +138,12 @@ __device__ __forceinline__ void reg_dif(typename F::T* x) {
 #endif
 template <class T>
 __host__ __device__ constexpr int ss_max_lr() { return sizeof(T) == 8 ? P3G_SS_MLR8 : P3G_SS_MLR4; }
+// Groups of a super-stage a thread's loop unrolls (1: the loop stays rolled;
+// settable at build time to compare).
+#ifndef P3G_SS_GROUP_UNROLL
+#define P3G_SS_GROUP_UNROLL 1
+#endif
+constexpr int SS_GROUP_UNROLL = P3G_SS_GROUP_UNROLL;
 __host__ __device__ constexpr int ss_count(int logn, int mlr) { return logn == 0 ? 0 : (logn + mlr - 1) / mlr; }
 __host__ __device__ constexpr int ss_radix(int logn, int j, int mlr) {
     // ceil-balanced split: the first (logn % cnt) parts get one more bit
@@ -193,7 +199,7 @@ __device__ __forceinline__ void super_stage(typename F::T* tile, const typename 
     constexpr int TWS = LOGN - LS;  // omega_S = omega_N^(2^TWS)
     constexpr bool FIRST = J == 0, LAST = J == CNT - 1;
     static_assert(GROUPS % SH::TPC == 0, "groups per thread");
-#pragma unroll 1
+#pragma unroll SS_GROUP_UNROLL
     for (int g = t; g < GROUPS; g += SH::TPC) {
         const int blk = g / M, i_lo = g % M;
         const int base = blk * (1 << LS) + i_lo;

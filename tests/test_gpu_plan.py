@@ -152,3 +152,33 @@ def test_host_input_plan_rejects_pageable_memory(gpu_ctx):
     with pytest.raises(P.P3GError) as e:
         P.Plan(gpu_ctx, P.BABYBEAR, [(t.ctypes.data, 6, 8, 1, 31)], n_streams=1, host=True)
     assert e.value.status == 1
+
+
+def test_plan_batches_equal_shapes_into_one_launch_per_pass(gpu_ctx):
+    """Eight traces of one shape (three-pass height) and four of another
+    (single-kernel height) in a plan with fixed streams: the LDEs run as one
+    launch per pass for each shape group, so adding traces of an existing
+    shape adds no kernels; the tree equals the oracle's."""
+    rng = np.random.default_rng(17)
+    shapes = [(12, int(rng.integers(5, 70))) for _ in range(8)] + [(9, int(rng.integers(1, 30))) for _ in range(4)]
+    traces = [rng.integers(0, O.BB_P, size=(1 << lh, w), dtype=np.uint32) for lh, w in shapes]
+    bufs = [gpu_ctx.to_device(t) for t in traces]
+    kernels = []
+    for n in (len(traces), 2):
+        sel = [0, 8] if n == 2 else list(range(n))
+        plan = P.Plan(gpu_ctx, P.BABYBEAR, [(bufs[i].ptr, shapes[i][0], shapes[i][1], 1, 31) for i in sel],
+                      n_streams=1)
+        plan.launch()
+        gpu_ctx.sync()
+        kernels.append(plan.kernels_per_launch)
+        if n == len(traces):
+            want, _ = _oracle_commit(traces, 0)
+            got = plan.tree.layers()
+            for g, w in zip(got, want):
+                assert np.array_equal(g, w)
+        plan.destroy()
+    # the same LDE launches for 12 traces as for one trace of each shape; only
+    # the row-hash and tree kernels may differ
+    assert kernels[0] <= kernels[1] + 2, kernels
+    for b in bufs:
+        b.free()
