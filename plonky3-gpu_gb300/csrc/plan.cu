@@ -217,6 +217,7 @@ void capture(p3g_ctx* ctx, p3g_plan* plan, int k, bool grouped) {
             if (hi) {
                 for (size_t i : g.idx) {
                     const auto& t = plan->traces[i];
+                    if (t.width == 0) continue;  // nothing to copy (d_trace may be null)
                     P3G_CUDA(cudaMemcpyAsync(plan->d_traces[i], t.d_trace, esz * (size_t(1) << t.log_h) * t.width,
                                              cudaMemcpyHostToDevice, cs));
                 }

@@ -115,6 +115,7 @@ def test_host_input_plan_copies_and_commits(gpu_ctx, n_streams):
     torch = pytest.importorskip("torch")
     rng = np.random.default_rng(60 + n_streams)
     traces = _batch(rng, 7, 3, 13, 30)
+    traces.append(np.zeros((1 << 5, 0), np.uint32))  # a zero-width trace: nothing to copy
     pinned = []
     for t in traces:
         pt = torch.empty(t.size, dtype=torch.int32, pin_memory=True)
@@ -126,7 +127,7 @@ def test_host_input_plan_copies_and_commits(gpu_ctx, n_streams):
     pf.numpy().view(np.uint32)[:] = fv.reshape(-1)
     beta = rng.integers(0, O.BB_P, size=4, dtype=np.uint32)
     d_fout = gpu_ctx.alloc((1 << (lh_fold - 1)) * 16)
-    plan = P.Plan(gpu_ctx, P.BABYBEAR, [(p.data_ptr(), t.shape[0].bit_length() - 1, t.shape[1], 1, 31)
+    plan = P.Plan(gpu_ctx, P.BABYBEAR, [(p.data_ptr() if t.size else 0, t.shape[0].bit_length() - 1, t.shape[1], 1, 31)
                                         for p, t in zip(pinned, traces)],
                   fold=(pf.data_ptr(), d_fout.ptr, lh_fold, 1, beta), n_streams=n_streams, host=True)
     for rep in range(2):
