@@ -67,7 +67,20 @@ static __constant__ uint32_t c_bb_shoup_pow2[16] = {P3G_SH16};
 // s * 2^i mod p for s in [0, p), 1 <= i <= 15 (Shoup: q = floor(s w' / 2^32),
 // s*2^i - q*p lies in [0, 2p)).  Multiplying the Montgomery representative by
 // the plain constant 2^i is the same as multiplying the field element.
+// For i <= 2 (s is canonical, so 2s < 2p < 2^32) repeated modular doubling
+// does it on the ALU pipe alone: the permutation is bound by the IMAD pipe,
+// and this measured 2.3% faster than the Shoup product there (doubling up to
+// i = 1 or 3 gained 0.9% and 1.2%; up to i = 6 lost 1.5%).
 __device__ __forceinline__ uint32_t bb_mul_pow2(uint32_t s, int i) {
+    if (i <= 2) {
+#pragma unroll
+        for (int j = 0; j < 2; ++j)
+            if (j < i) {
+                const uint32_t d = s << 1, t = d - bb::P;
+                s = d < t ? d : t;
+            }
+        return s;
+    }
     const uint32_t q = __umulhi(s, c_bb_shoup_pow2[i]);
     const uint32_t r = (s << i) - q * bb::P;
     const uint32_t t = r - bb::P;
