@@ -52,6 +52,8 @@ C3_FOLD_LOG = 19
 C1_LOG_H, C1_WIDTH, C1_LOG_B = 20, 256, 1
 # the SM count and SMSPs of a GB300 (the issue bound below)
 SMSPS = 152 * 4
+# batches the end-to-end leg keeps in flight
+E2E_DEPTH = 3
 
 
 def peaks():
@@ -675,33 +677,34 @@ def run_ours(args):
 
     # ---- end to end: host-input plans (p3g_plan_commit_host), the traces and
     # the quotient in pinned host memory, copied in by every launch; the root
-    # and the fold output are read back after every step.  Two plans over the
-    # same host inputs (their own device copies, LDEs, trees and fold outputs)
-    # alternate on two streams, so one batch's host-to-device copies overlap
-    # the other batch's hashing; the host keeps two batches in flight (it
-    # reads back step i after enqueuing step i + 1).  The serial figure (one
-    # batch at a time) is reported beside it.
+    # and the fold output are read back after every step.  E2E_DEPTH plans
+    # over the same host inputs (their own device copies, LDEs, trees and fold
+    # outputs) take turns on as many streams, so later batches' host-to-device
+    # copies overlap the current batch's hashing; the host keeps E2E_DEPTH
+    # batches in flight (it reads back step i after enqueuing step
+    # i + E2E_DEPTH - 1).  The serial figure (one batch at a time) is reported
+    # beside it.
     pinned = [pinned_copy(torch, t) for t in traces]
     pin_fold = pinned_copy(torch, fold_in)
     htr = [(pt_.data_ptr(), lh, w, C3_LOG_B, SHIFT) for pt_, (lh, w) in zip(pinned, shapes)]
-    fouts = [d_fout, ctx.alloc((1 << (fold_log - 1)) * 16)]
+    fouts = [d_fout] + [ctx.alloc((1 << (fold_log - 1)) * 16) for _ in range(E2E_DEPTH - 1)]
     plans_h = [P.Plan(ctx, P.BABYBEAR, htr, 0, fold=(pin_fold.data_ptr(), fo.ptr, fold_log, 1, beta), n_streams=0,
                       host=True) for fo in fouts]
-    streams_h = [stream, torch.cuda.Stream(device=dev)]
+    streams_h = [stream] + [torch.cuda.Stream(device=dev) for _ in range(E2E_DEPTH - 1)]
     root_ptrs = []
     for ph in plans_h:
         nl = len(ph.tree.info()[0])
         root_ptrs.append(ph.tree.layer_ptr(nl - 1))
-    roots = [torch.zeros(8, dtype=torch.int32, pin_memory=True) for _ in range(2)]
-    folds = [torch.zeros((1 << (fold_log - 1)) * 4, dtype=torch.int32, pin_memory=True) for _ in range(2)]
+    roots = [torch.zeros(8, dtype=torch.int32, pin_memory=True) for _ in range(E2E_DEPTH)]
+    folds = [torch.zeros((1 << (fold_log - 1)) * 4, dtype=torch.int32, pin_memory=True) for _ in range(E2E_DEPTH)]
     lib = P.load()
 
     def launch(i):
-        j = i % 2
+        j = i % E2E_DEPTH
         plans_h[j].launch(streams_h[j].cuda_stream)
 
     def read(i):  # waits for step i, then copies its root and fold output to the host
-        j = i % 2
+        j = i % E2E_DEPTH
         sp = streams_h[j].cuda_stream
         P.check(lib.p3g_memcpy_d2h(ctx.handle, roots[j].data_ptr(), root_ptrs[j], 32, sp))
         P.check(lib.p3g_memcpy_d2h(ctx.handle, folds[j].data_ptr(), fouts[j].ptr, folds[j].numel() * 4, sp))
@@ -712,14 +715,15 @@ def run_ours(args):
     torch.cuda.synchronize(dev)
     done = []
     t_start = time.perf_counter()
-    launch(0)
+    for i in range(min(E2E_DEPTH - 1, n_e2e)):
+        launch(i)
     for i in range(n_e2e):
-        if i + 1 < n_e2e:
-            launch(i + 1)
+        if i + E2E_DEPTH - 1 < n_e2e:
+            launch(i + E2E_DEPTH - 1)
         read(i)
         done.append(time.perf_counter())
     torch.cuda.synchronize(dev)
-    root_h = roots[(n_e2e - 1) % 2].numpy().view(np.uint32).copy()
+    root_h = roots[(n_e2e - 1) % E2E_DEPTH].numpy().view(np.uint32).copy()
     t0_timed = done[args.warmup - 1] if args.warmup > 0 else t_start
     e2e_total_ms = (done[-1] - t0_timed) * 1e3
     e2e_int = [(done[i] - done[i - 1]) * 1e3 for i in range(max(args.warmup, 1), n_e2e)]
@@ -739,7 +743,8 @@ def run_ours(args):
     e2e_streams = plans_h[0].n_streams
     for ph in plans_h:
         ph.destroy()
-    fouts[1].free()
+    for fo in fouts[1:]:
+        fo.free()
     del pinned, pin_fold
     kernels_per_step = plan.kernels_per_launch
     n_streams = plan.n_streams
@@ -794,8 +799,8 @@ def run_ours(args):
                 "p50_ms": float(np.percentile(e2e_int, 50)), "p99_ms": float(np.percentile(e2e_int, 99)),
                 "intervals_ms": [round(x, 3) for x in e2e_int], "streams": e2e_streams,
                 "call": "p3g_plan_launch of p3g_plan_commit_host plans (64 pinned host traces and the quotient "
-                        "copied in by the graph every step), root and fold output read back every step; two "
-                        "batches in flight on two streams (p50/p99 over the intervals between step completions)",
+                        f"copied in by the graph every step), root and fold output read back every step; {E2E_DEPTH} "
+                        f"batches in flight on {E2E_DEPTH} streams (p50/p99 over the intervals between step completions)",
                 "serial": {"value": elems / (statistics.mean(serial_ms) / 1e3), "unit": UNIT,
                            "p50_ms": float(np.percentile(serial_ms, 50)),
                            "p99_ms": float(np.percentile(serial_ms, 99)),
