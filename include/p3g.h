@@ -212,7 +212,9 @@ typedef struct {
 /* The trace-commitment hot path: for every trace, the coset LDE with rows in
  * bit-reversed order, then one mixed-height MMCS commit over all LDEs (the
  * LDEs are owned by the returned tree; see p3g_tree_leaf_ptr).  With one
- * trace this is the per-trace commit; with many it is the batched commit. */
+ * trace this is the per-trace commit; with many it is the batched commit, and
+ * traces of equal (log_h, log_blowup, shift) run their LDEs as one launch per
+ * pass.  Shifts must be canonical and non-zero; log_h up to 26. */
 P3G_API int p3g_commit_traces(p3g_ctx *ctx, int field, const p3g_trace *traces, size_t n_traces,
                       uint32_t cap_height, p3g_tree **tree_out, void *h_cap_out, void *stream);
 

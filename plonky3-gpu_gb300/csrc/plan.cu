@@ -126,11 +126,9 @@ void lde_group_run(p3g_ctx* ctx, int field, const LdeGroup& g, const p3g_trace* 
         gw.push_back(traces[i].width);
     }
     if (bb)
-        lde_group_bb(ctx, g.log_h, g.log_b, gin.data(), const_cast<void* const*>(g.scr.data()), gout.data(), gw.data(),
-                     g.idx.size(), const_cast<void* const*>(g.tab), st);
+        lde_group_bb(ctx, g.log_h, g.log_b, gin.data(), g.scr.data(), gout.data(), gw.data(), g.idx.size(), g.tab, st);
     else
-        lde_group_gl(ctx, g.log_h, g.log_b, gin.data(), const_cast<void* const*>(g.scr.data()), gout.data(), gw.data(),
-                     g.idx.size(), const_cast<void* const*>(g.tab), st);
+        lde_group_gl(ctx, g.log_h, g.log_b, gin.data(), g.scr.data(), gout.data(), gw.data(), g.idx.size(), g.tab, st);
 }
 
 void lde_group_release(p3g_ctx* ctx, LdeGroup& g, cudaStream_t st) {
