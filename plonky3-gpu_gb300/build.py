@@ -2,7 +2,7 @@
 
 Each translation unit is compiled in parallel into _build/, then linked
 in-tree as plonky3-gpu_gb300/lib/libp3g_gb300.so.  Rebuilds only what changed
-(source or header newer than its object).
+(source or header newer than its object, or other compiler flags).
 """
 from __future__ import annotations
 
@@ -48,10 +48,10 @@ def _headers_mtime() -> float:
     return m
 
 
-def _compile(src: str, hdr_mtime: float, verbose: bool) -> str:
+def _compile(src: str, hdr_mtime: float, verbose: bool, flags_changed: bool) -> str:
     obj = os.path.join(BUILD, src.replace(".cu", ".o"))
     srcp = os.path.join(CSRC, src)
-    if os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(srcp), hdr_mtime):
+    if not flags_changed and os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(srcp), hdr_mtime):
         return obj
     cmd = [nvcc()] + _flags() + ["-c", srcp, "-o", obj]
     if verbose:
@@ -68,9 +68,17 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
     os.makedirs(BUILD, exist_ok=True)
     os.makedirs(LIBDIR, exist_ok=True)
     hm = _headers_mtime()
+    # objects built with other flags (another P3G_NVCC_FLAGS) are stale too
+    stamp = os.path.join(BUILD, "flags.txt")
+    flags = " ".join(_flags())
+    old = open(stamp).read() if os.path.exists(stamp) else None
+    changed = old != flags
     with cf.ThreadPoolExecutor(max_workers=jobs or len(SOURCES)) as ex:
-        objs = list(ex.map(lambda s: _compile(s, hm, verbose), SOURCES))
-    if not os.path.exists(LIB) or any(os.path.getmtime(o) > os.path.getmtime(LIB) for o in objs):
+        objs = list(ex.map(lambda s: _compile(s, hm, verbose, changed), SOURCES))
+    if changed:
+        with open(stamp, "w") as f:
+            f.write(flags)
+    if changed or not os.path.exists(LIB) or any(os.path.getmtime(o) > os.path.getmtime(LIB) for o in objs):
         cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:

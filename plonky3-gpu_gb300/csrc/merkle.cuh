@@ -62,6 +62,24 @@ __device__ __forceinline__ void hash_group(const Group<typename H::T>& g, uint64
             }
             c += filled;
         } else {
+            // A chunk inside one matrix's row takes RATE loads from one
+            // pointer (most chunks); one that spans matrices goes element by
+            // element below.  With every element on that general path the
+            // 64-trace batched commit's step took 6% longer (83.5 against
+            // 78.5 ms on one GB300).  The row pointer is recomputed per chunk
+            // from shared memory: keeping it (and the width) in registers
+            // across the permutation measured 5% slower.
+            while (m < g.n && c >= g.w[m]) {
+                ++m;
+                c = 0;
+            }
+            if (m < g.n && c + H::RATE <= g.w[m]) {
+                const T* q = g.ptr[m] + r * g.w[m] + c;
+#pragma unroll
+                for (int i = 0; i < H::RATE; ++i) s[i] = H::absorb(__ldg(q + i));
+                c += H::RATE;
+                filled = H::RATE;
+            }
 #pragma unroll
             for (int i = 0; i < H::RATE; ++i) {
                 if (filled == i) {
