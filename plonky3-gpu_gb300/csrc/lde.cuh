@@ -195,6 +195,8 @@ struct GLoad {
     }
 };
 // Shared tile row bitrev(i), times pre[i] (coefficients -> twisted coefficients).
+// base < M (the first super-stage), so bitrev(base + M*k) is
+// bitrev(base) + bitrev(M*k) with no common bit.
 template <class F, class SH, int LOGN>
 struct PermLoad {
     using T = typename F::T;
@@ -203,22 +205,22 @@ struct PermLoad {
     int c;
     template <int R, int M>
     __device__ __forceinline__ void group(int base, T* x) const {
+        const auto r0 = SH::row0(int(bitrev_dev(unsigned(base), LOGN)), c);
 #pragma unroll
-        for (int k = 0; k < R; ++k) {
-            const int i = base + M * k;
-            x[k] = F::mul_tw(A[SH::addr(bitrev_dev(unsigned(i), LOGN), c)], pre[i]);
-        }
+        for (int k = 0; k < R; ++k)
+            x[k] = F::mul_tw(A[SH::at(r0, int(bitrev_ct(unsigned(M * k), LOGN)))], pre[base + M * k]);
     }
 };
-// Shared tile, natural positions.
+// Shared tile, natural positions (base is a multiple of 2^LR).
 template <class T, class SH>
 struct TileStore {
     T* A;
     int c;
     template <int LR>
     __device__ __forceinline__ void group(int base, const T* x) const {
+        const auto r0 = SH::row0(base, c);
 #pragma unroll
-        for (int k = 0; k < (1 << LR); ++k) A[SH::addr(base + k, c)] = x[k];
+        for (int k = 0; k < (1 << LR); ++k) A[SH::at(r0, k)] = x[k];
     }
 };
 // x * c for a prepared twiddle (F::TW) or a const-form value (F::T); for

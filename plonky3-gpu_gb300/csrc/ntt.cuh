@@ -174,13 +174,30 @@ struct DftShape {
     static constexpr int SH1 = cmax(RL, LG);
     static constexpr int SH2 = cmax(LOGN - LG, LG);
     static constexpr int TILE = N * C;  // elements
-    static __device__ __forceinline__ int addr(int row, int c) {
+    static __host__ __device__ __forceinline__ int swz(int row) { return (row ^ (row >> SH1) ^ (row >> SH2)) & (RPL - 1); }
+    static __host__ __device__ __forceinline__ int addr(int row, int c) {
         if constexpr (RPL == 1) {
             return row * C + c;
         } else {
-            const int sub = (row ^ (row >> SH1) ^ (row >> SH2)) & (RPL - 1);
-            return (row >> LG) * LINE + sub * C + c;
+            return (row >> LG) * LINE + swz(row) * C + c;
         }
+    }
+    // The rows one thread touches in a group are base + mk with base and mk
+    // sharing no set bit, mk a compile-time offset.  The swizzle is linear
+    // over XOR and the line index over such a sum, so row0(base, c) is
+    // computed once per group and at(r0, mk) == addr(base + mk, c) costs an
+    // XOR and an add per element (mk's terms fold into constants).
+    struct Row0 {
+        int line;  // (base >> LG) * LINE, or base * C + c without a swizzle
+        int sub;   // swz(base) * C + c
+    };
+    static __host__ __device__ __forceinline__ Row0 row0(int base, int c) {
+        if constexpr (RPL == 1) return {base * C + c, 0};
+        else return {(base >> LG) * LINE, swz(base) * C + c};
+    }
+    static __host__ __device__ __forceinline__ int at(const Row0& r, int mk) {
+        if constexpr (RPL == 1) return r.line + mk * C;
+        else return r.line + (mk >> LG) * LINE + (r.sub ^ (swz(mk) * C));
     }
 };
 
@@ -202,13 +219,14 @@ __device__ __forceinline__ void super_stage(typename F::T* tile, const typename 
 #pragma unroll SS_GROUP_UNROLL
     for (int g = t; g < GROUPS; g += SH::TPC) {
         const int blk = g / M, i_lo = g % M;
-        const int base = blk * (1 << LS) + i_lo;
+        const int base = blk * (1 << LS) + i_lo;  // i_lo < M: disjoint from M*k
         T x[R];
         if constexpr (FIRST) {
             load.template group<R, M>(base, x);  // rows base + M*k
         } else {
+            const auto r0 = SH::row0(base, c);
 #pragma unroll
-            for (int k = 0; k < R; ++k) x[k] = tile[SH::addr(base + M * k, c)];
+            for (int k = 0; k < R; ++k) x[k] = tile[SH::at(r0, M * k)];
         }
         reg_dif<F, LR, INV>(x);
         if constexpr (LAST) {
@@ -219,8 +237,9 @@ __device__ __forceinline__ void super_stage(typename F::T* tile, const typename 
                 const int e = (i_lo * int(bitrev_ct(unsigned(s), LR))) << TWS;
                 x[s] = F::mul_tw(x[s], tw[e]);
             }
+            const auto r0 = SH::row0(base, c);
 #pragma unroll
-            for (int k = 0; k < R; ++k) tile[SH::addr(base + M * k, c)] = x[k];
+            for (int k = 0; k < R; ++k) tile[SH::at(r0, M * k)] = x[k];
         }
     }
 }
