@@ -105,13 +105,13 @@ k_dft_single(const typename F::T* __restrict__ in, typename F::T* __restrict__ o
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* A = reinterpret_cast<T*>(smem_raw);
     TW* tw = reinterpret_cast<TW*>(A + SH::TILE);
-    TW* pre = tw + N;
+    TW* pre = tw + SH::TWA;
     TW* post = pre + N;
     const int tid = threadIdx.x, c = tid % C, t = tid / C;
     const int col = tile_coord<C>(w).ct * C + c;
     const bool ok = col < w;
+    for (int e = tid; e < SH::TWN; e += NT) tw[e] = gtw ? gtw[e] : stage_tw<F, LOGN>(roots, e, INV != 0);
     for (int e = tid; e < N; e += NT) {
-        tw[e] = gtw ? gtw[e] : F::tw_from_const(INV ? roots.omega_inv(LOGN, e) : roots.omega(LOGN, e));
         pre[e] = gpre[e];
         if (gpost) post[e] = gpost[e];
     }
@@ -135,7 +135,7 @@ k_dft_pass_a(const typename F::T* __restrict__ in, typename F::T* __restrict__ m
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* A = reinterpret_cast<T*>(smem_raw);
     TW* tw = reinterpret_cast<TW*>(A + SH::TILE);
-    TW* pre = tw + N;
+    TW* pre = tw + SH::TWA;
     TW* post = pre + N;
     const int tid = threadIdx.x, c = tid % C, t = tid / C;
     const TileCoord tc_ = tile_coord<C>(w);
@@ -145,8 +145,8 @@ k_dft_pass_a(const typename F::T* __restrict__ in, typename F::T* __restrict__ m
     const int64_t N2 = int64_t(1) << n2;
     const int n = LOGN + n2;
     const T sk2 = sq[k2];
+    for (int e = tid; e < SH::TWN; e += NT) tw[e] = gtw ? gtw[e] : stage_tw<F, LOGN>(roots, e, INV != 0);
     for (int e = tid; e < N; e += NT) {
-        tw[e] = gtw ? gtw[e] : F::tw_from_const(INV ? roots.omega_inv(LOGN, e) : roots.omega(LOGN, e));
         pre[e] = gpre[e];
         const unsigned m1 = bitrev_dev(unsigned(e), LOGN);
         const uint64_t ex = uint64_t(k2) * m1;
@@ -173,16 +173,15 @@ k_dft_pass_b(const typename F::T* src, typename F::T* out, int w, int n1, int bi
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* A = reinterpret_cast<T*>(smem_raw);
     TW* tw = reinterpret_cast<TW*>(A + SH::TILE);
-    TW* post = tw + N;
+    TW* post = tw + SH::TWA;
     const int tid = threadIdx.x, c = tid % C, t = tid / C;
     const TileCoord tc_ = tile_coord<C>(w);
     const int col = tc_.ct * C + c;
     const bool ok = col < w;
     const int64_t base = tc_.blk * N;
-    for (int e = tid; e < N; e += NT) {
-        tw[e] = gtw ? gtw[e] : F::tw_from_const(INV ? roots.omega_inv(LOGN, e) : roots.omega(LOGN, e));
-        if (gpost) post[e] = gpost[e];
-    }
+    for (int e = tid; e < SH::TWN; e += NT) tw[e] = gtw ? gtw[e] : stage_tw<F, LOGN>(roots, e, INV != 0);
+    if (gpost)
+        for (int e = tid; e < N; e += NT) post[e] = gpost[e];
     __syncthreads();
     GLoad<T> ld{src + base * w + col, w, ok};
     ScaledOutStore<F> st{out + col, w, base, n1 + LOGN, bitrev_out != 0, ok, gpost ? post : nullptr};
@@ -195,7 +194,7 @@ static void launch_dft_single(const typename F::T* in, typename F::T* out, int w
                               const typename F::TW* post, const typename F::TW* dft_tw, RootTab<F> roots,
                               cudaStream_t st) {
     using SH = DftTile<F, LOGN>;
-    const size_t smem = SH::TILE * sizeof(typename F::T) + 3 * SH::N * sizeof(typename F::TW);
+    const size_t smem = SH::TILE * sizeof(typename F::T) + (SH::TWA + 2 * SH::N) * sizeof(typename F::TW);
     auto k = k_dft_single<F, LOGN, INV>;
     set_smem(k, smem);
     const dim3 grid = tile_grid(1, w, LdeCfg<F>::C13);
@@ -208,7 +207,7 @@ static void launch_dft_pass_a(const typename F::T* in, typename F::T* mid, int w
                               const typename F::T* sq, const typename F::T* a1, const typename F::TW* dft_tw,
                               RootTab<F> roots, cudaStream_t st) {
     using SH = DftTile<F, LOGN>;
-    const size_t smem = SH::TILE * sizeof(typename F::T) + 3 * SH::N * sizeof(typename F::TW);
+    const size_t smem = SH::TILE * sizeof(typename F::T) + (SH::TWA + 2 * SH::N) * sizeof(typename F::TW);
     auto k = k_dft_pass_a<F, LOGN, INV>;
     set_smem(k, smem);
     const dim3 grid = tile_grid(int64_t(1) << n2, w, LdeCfg<F>::C13);
@@ -221,7 +220,7 @@ static void launch_dft_pass_b(const typename F::T* mid, typename F::T* out, int 
                               const typename F::TW* post, const typename F::TW* dft_tw, RootTab<F> roots,
                               cudaStream_t st) {
     using SH = DftTile<F, LOGN>;
-    const size_t smem = SH::TILE * sizeof(typename F::T) + 2 * SH::N * sizeof(typename F::TW);
+    const size_t smem = SH::TILE * sizeof(typename F::T) + (SH::TWA + SH::N) * sizeof(typename F::TW);
     auto k = k_dft_pass_b<F, LOGN, INV>;
     set_smem(k, smem);
     const dim3 grid = tile_grid(int64_t(1) << n1, w, LdeCfg<F>::C13);

@@ -90,30 +90,54 @@ constexpr int LDE_PASS_MAX = 21;    // three-pass LDE up to h = 2^21
 constexpr int LDE_BIG_MAX = LDE_PASS_MAX + 5;
 
 // Prepared in-tile DFT twiddles (one table per context and field): for every
-// LOGN in 1..DFT_TW_MAXLOG the N = 2^LOGN powers omega_N^e, e < N, as F::TW;
-// the forward tables first, then the inverse ones.  Kernels copy their
-// LOGN's table into shared memory instead of deriving every entry from the
-// two-level root table (two loads, two products and, for BabyBear, a
-// 64-bit Shoup quotient per entry and CTA).
+// LOGN in 1..DFT_TW_MAXLOG the stage-ordered table of the size-2^LOGN
+// transform (ntt.cuh: ss_tw_size entries) as F::TW; the forward tables
+// first, then the inverse ones.  Kernels copy their LOGN's table into shared
+// memory instead of deriving every entry from the two-level root table (two
+// loads, two products and, for BabyBear, a 64-bit Shoup quotient per entry
+// and CTA).
 constexpr int DFT_TW_MAXLOG = 11;
-constexpr size_t DFT_TW_BLOCK = (size_t(2) << DFT_TW_MAXLOG) - 2;  // sum of 2^L, L = 1..11
+template <class T>
+constexpr size_t dft_tw_block() {  // entries of one direction, LOGN = 1..11
+    size_t n = 0;
+    for (int L = 1; L <= DFT_TW_MAXLOG; ++L) n += size_t(ss_tw_size(L, ss_max_lr<T>()));
+    return n;
+}
+template <class T>
 constexpr size_t dft_tw_offset(int logn, bool inv) {
-    return (inv ? DFT_TW_BLOCK : 0) + (size_t(1) << logn) - 2;
+    size_t o = inv ? dft_tw_block<T>() : 0;
+    for (int L = 1; L < logn; ++L) o += size_t(ss_tw_size(L, ss_max_lr<T>()));
+    return o;
 }
 template <class F>
 std::vector<typename F::TW> build_dft_tw() {
-    std::vector<typename F::TW> v(2 * DFT_TW_BLOCK);
+    using T = typename F::T;
+    constexpr int MLR = ss_max_lr<T>();
+    std::vector<typename F::TW> v(2 * dft_tw_block<T>());
     for (int L = 1; L <= DFT_TW_MAXLOG; ++L) {
         const uint64_t wf = F::root(unsigned(L)), wi = F::h_inv(wf);
+        std::vector<uint64_t> pf(size_t(1) << L), pi(size_t(1) << L);
         uint64_t a = 1, b = 1;
-        for (size_t e = 0; e < (size_t(1) << L); ++e) {
-            v[dft_tw_offset(L, false) + e] = F::h_tw(a);
-            v[dft_tw_offset(L, true) + e] = F::h_tw(b);
+        for (size_t e = 0; e < pf.size(); ++e) {
+            pf[e] = a;
+            pi[e] = b;
             a = F::h_mul(a, wf);
             b = F::h_mul(b, wi);
         }
+        for (int i = 0; i < ss_tw_size(L, MLR); ++i) {
+            const uint32_t e = ss_tw_exp(L, MLR, i);
+            v[dft_tw_offset<T>(L, false) + size_t(i)] = F::h_tw(pf[e]);
+            v[dft_tw_offset<T>(L, true) + size_t(i)] = F::h_tw(pi[e]);
+        }
     }
     return v;
+}
+// Entry i of the stage-ordered table of the size-2^LOGN transform, from the
+// root table (kernels without a prepared table).
+template <class F, int LOGN>
+__device__ __forceinline__ typename F::TW stage_tw(RootTab<F> roots, int i, bool inv) {
+    const uint32_t e = ss_tw_exp(LOGN, ss_max_lr<typename F::T>(), i);
+    return F::tw_from_const(inv ? roots.omega_inv(LOGN, e) : roots.omega(LOGN, e));
 }
 
 // out[i] = scale * base^i, all in const form.
@@ -355,8 +379,8 @@ k_lde_single(const LdeJobs<typename F::T> J, int log_b, int bitrev_out, const ty
     T* A = reinterpret_cast<T*>(smem_raw);
     T* B = A + SH::TILE;
     TW* twi = reinterpret_cast<TW*>(B + SH::TILE);
-    TW* twf = twi + N;
-    TW* pre = twf + N;
+    TW* twf = twi + SH::TWA;
+    TW* pre = twf + SH::TWA;
     unsigned local;
     const LdeJob<T>& jb = lde_job(J, 0, local);
     const int w = int(jb.w);
@@ -365,9 +389,9 @@ k_lde_single(const LdeJobs<typename F::T> J, int log_b, int bitrev_out, const ty
     const bool ok = col < w;
     const int logH = LOGN + log_b;
 
-    for (int e = tid; e < N; e += NT) {
-        twi[e] = gtwi ? gtwi[e] : F::tw_from_const(roots.omega_inv(LOGN, e));
-        twf[e] = gtwf ? gtwf[e] : F::tw_from_const(roots.omega(LOGN, e));
+    for (int e = tid; e < SH::TWN; e += NT) {
+        twi[e] = gtwi ? gtwi[e] : stage_tw<F, LOGN>(roots, e, true);
+        twf[e] = gtwf ? gtwf[e] : stage_tw<F, LOGN>(roots, e, false);
     }
     __syncthreads();
     {
@@ -399,7 +423,7 @@ k_lde_pass1(const LdeJobs<typename F::T> J, int n1, RootTab<F> roots, const type
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* A = reinterpret_cast<T*>(smem_raw);
     TW* tw = reinterpret_cast<TW*>(A + SH::TILE);
-    T* post = reinterpret_cast<T*>(tw + N);  // const form
+    T* post = reinterpret_cast<T*>(tw + SH::TWA);  // const form
     unsigned local;
     const LdeJob<T>& jb = lde_job(J, 0, local);
     const int w = int(jb.w);
@@ -411,10 +435,8 @@ k_lde_pass1(const LdeJobs<typename F::T> J, int n1, RootTab<F> roots, const type
     const int64_t N1 = int64_t(1) << n1;
     const int n = n1 + LOGN;
 
-    for (int e = tid; e < N; e += NT) {
-        tw[e] = gtwi ? gtwi[e] : F::tw_from_const(roots.omega_inv(LOGN, e));
-        post[e] = roots.omega_inv(n, uint64_t(i1) * bitrev_dev(e, LOGN));
-    }
+    for (int e = tid; e < SH::TWN; e += NT) tw[e] = gtwi ? gtwi[e] : stage_tw<F, LOGN>(roots, e, true);
+    for (int e = tid; e < N; e += NT) post[e] = roots.omega_inv(n, uint64_t(i1) * bitrev_dev(e, LOGN));
     __syncthreads();
     // scratch is tiled by pass 2's column tiles: element (row r, column col)
     // at ((col / C2) * h + r) * C2 + col % C2, so that each pass-2 CTA reads
@@ -443,8 +465,8 @@ k_lde_pass2(const LdeJobs<typename F::T> J, int n2, int log_b, const typename F:
     T* A = reinterpret_cast<T*>(smem_raw);
     T* B = A + SH::TILE;
     TW* twi = reinterpret_cast<TW*>(B + SH::TILE);
-    TW* twf = twi + N;
-    TW* pre = twf + N;
+    TW* twf = twi + SH::TWA;
+    TW* pre = twf + SH::TWA;
     T* post = reinterpret_cast<T*>(pre + N);  // const form
     unsigned local;
     const LdeJob<T>& jb = lde_job(J, 1, local);
@@ -459,9 +481,9 @@ k_lde_pass2(const LdeJobs<typename F::T> J, int n2, int log_b, const typename F:
     const int64_t h = int64_t(1) << n;
     const int logH = n + log_b;
 
-    for (int e = tid; e < N; e += NT) {
-        twi[e] = gtwi ? gtwi[e] : F::tw_from_const(roots.omega_inv(LOGN, e));
-        twf[e] = gtwf ? gtwf[e] : F::tw_from_const(roots.omega(LOGN, e));
+    for (int e = tid; e < SH::TWN; e += NT) {
+        twi[e] = gtwi ? gtwi[e] : stage_tw<F, LOGN>(roots, e, true);
+        twf[e] = gtwf ? gtwf[e] : stage_tw<F, LOGN>(roots, e, false);
     }
     __syncthreads();
     {
@@ -510,7 +532,7 @@ k_lde_pass3(const LdeJobs<typename F::T> J, int n1, int log_b, int bitrev_out, R
     const int logH = n + log_b;
     const int64_t base = blk * N;  // = t*h + s1*N2
 
-    for (int e = tid; e < N; e += NT) tw[e] = gtwf ? gtwf[e] : F::tw_from_const(roots.omega(LOGN, e));
+    for (int e = tid; e < SH::TWN; e += NT) tw[e] = gtwf ? gtwf[e] : stage_tw<F, LOGN>(roots, e, false);
     __syncthreads();
     GLoad<T> ld{jb.mid + base * w + col, w, ok};
     OutStore<T> st{jb.out + col, w, base, logH, bitrev_out != 0, ok};
@@ -527,7 +549,7 @@ static void set_smem(Kern k, size_t bytes) {
 // the kernels then derive it from the root table).
 template <class F>
 static const typename F::TW* tw_table(const typename F::TW* dft_tw, int logn, bool inv) {
-    return dft_tw && logn <= DFT_TW_MAXLOG ? dft_tw + dft_tw_offset(logn, inv) : nullptr;
+    return dft_tw && logn <= DFT_TW_MAXLOG ? dft_tw + dft_tw_offset<typename F::T>(logn, inv) : nullptr;
 }
 
 template <class F, int LOGN>
@@ -535,7 +557,7 @@ static void launch_single(const LdeJobs<typename F::T>& J, unsigned ctas, int lo
                           const typename F::TW* pre, RootTab<F> roots, const typename F::TW* dft_tw,
                           cudaStream_t st) {
     using SH = Tile<F, LOGN, LdeCfg<F>::C13>;
-    size_t smem = 2 * SH::TILE * sizeof(typename F::T) + 3 * SH::N * sizeof(typename F::TW);
+    size_t smem = 2 * SH::TILE * sizeof(typename F::T) + (2 * SH::TWA + SH::N) * sizeof(typename F::TW);
     auto k = k_lde_single<F, LOGN>;
     set_smem(k, smem);
     k<<<ctas, SH::THREADS, smem, st>>>(J, log_b, br, sq, roots, tw_table<F>(dft_tw, LOGN, true),
@@ -547,7 +569,7 @@ template <class F, int LOGN>
 static void launch_pass1(const LdeJobs<typename F::T>& J, unsigned ctas, int n1, RootTab<F> roots,
                          const typename F::TW* dft_tw, cudaStream_t st) {
     using SH = Tile<F, LOGN, LdeCfg<F>::C13>;
-    size_t smem = SH::TILE * sizeof(typename F::T) + SH::N * (sizeof(typename F::TW) + sizeof(typename F::T));
+    size_t smem = SH::TILE * sizeof(typename F::T) + SH::TWA * sizeof(typename F::TW) + SH::N * sizeof(typename F::T);
     auto k = k_lde_pass1<F, LOGN>;
     set_smem(k, smem);
     k<<<ctas, SH::THREADS, smem, st>>>(J, n1, roots, tw_table<F>(dft_tw, LOGN, true));
@@ -559,7 +581,8 @@ static void launch_pass2(const LdeJobs<typename F::T>& J, unsigned ctas, int n2,
                          const typename F::T* sq, const typename F::TW* pre, RootTab<F> roots,
                          const typename F::TW* dft_tw, cudaStream_t st) {
     using SH = Tile<F, LOGN, LdeCfg<F>::C2>;
-    size_t smem = 2 * SH::TILE * sizeof(typename F::T) + SH::N * (3 * sizeof(typename F::TW) + sizeof(typename F::T));
+    size_t smem = 2 * SH::TILE * sizeof(typename F::T) + (2 * SH::TWA + SH::N) * sizeof(typename F::TW) +
+                  SH::N * sizeof(typename F::T);
     auto k = k_lde_pass2<F, LOGN>;
     set_smem(k, smem);
     k<<<ctas, SH::THREADS, smem, st>>>(J, n2, log_b, sp, sq, roots, tw_table<F>(dft_tw, LOGN, true),
@@ -571,7 +594,7 @@ template <class F, int LOGN>
 static void launch_pass3(const LdeJobs<typename F::T>& J, unsigned ctas, int n1, int log_b, int br, RootTab<F> roots,
                          const typename F::TW* dft_tw, cudaStream_t st) {
     using SH = Tile<F, LOGN, LdeCfg<F>::C13>;
-    size_t smem = SH::TILE * sizeof(typename F::T) + SH::N * sizeof(typename F::TW);
+    size_t smem = SH::TILE * sizeof(typename F::T) + SH::TWA * sizeof(typename F::TW);
     auto k = k_lde_pass3<F, LOGN>;
     set_smem(k, smem);
     k<<<ctas, SH::THREADS, smem, st>>>(J, n1, log_b, br, roots, tw_table<F>(dft_tw, LOGN, false));

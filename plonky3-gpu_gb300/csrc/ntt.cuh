@@ -155,6 +155,30 @@ __host__ __device__ constexpr int ss_consumed(int logn, int j, int mlr) {
     for (int i = 0; i < j; ++i) s += ss_radix(logn, i, mlr);
     return s;
 }
+// Inter-super-stage twiddles in stage order.  Super-stage J (every one but
+// the last) multiplies slot s of group i_lo by omega_N^((i_lo * bitrev(s)) <<
+// TWS_J); the table holds that value at ss_tw_off(J) + i_lo * R_J + s, so a
+// group's R_J twiddles sit at one base address plus compile-time offsets
+// (one address per group instead of a product per twiddle).  Stage J's block
+// has 2^LS_J entries (s = 0 included, unused); the whole table
+// ss_tw_size(LOGN) entries (LOGN at LOGN <= 2 * radix, more above).
+__host__ __device__ constexpr int ss_tw_off(int logn, int j, int mlr) {
+    int o = 0;
+    for (int i = 0; i < j; ++i) o += 1 << (logn - ss_consumed(logn, i, mlr));
+    return o;
+}
+__host__ __device__ constexpr int ss_tw_size(int logn, int mlr) {
+    return ss_count(logn, mlr) <= 1 ? 0 : ss_tw_off(logn, ss_count(logn, mlr) - 1, mlr);
+}
+// e such that entry idx of the stage-ordered table is omega_N^e (e < N)
+__host__ __device__ inline uint32_t ss_tw_exp(int logn, int mlr, int idx) {
+    int j = 0;
+    while (j + 2 < ss_count(logn, mlr) && idx >= ss_tw_off(logn, j + 1, mlr)) ++j;
+    const int lr = ss_radix(logn, j, mlr);
+    const unsigned local = unsigned(idx - ss_tw_off(logn, j, mlr));
+    const unsigned i_lo = local >> lr, s = local & ((1u << lr) - 1u);
+    return (i_lo * bitrev_ct(s, lr)) << ss_consumed(logn, j, mlr);
+}
 __host__ __device__ constexpr int cmax(int a, int b) { return a > b ? a : b; }
 __host__ __device__ constexpr int ilog2(int x) { return x <= 1 ? 0 : 1 + ilog2(x >> 1); }
 
@@ -174,6 +198,9 @@ struct DftShape {
     static constexpr int SH1 = cmax(RL, LG);
     static constexpr int SH2 = cmax(LOGN - LG, LG);
     static constexpr int TILE = N * C;  // elements
+    // stage-ordered twiddle table: entries, and the size a kernel allots
+    static constexpr int TWN = ss_tw_size(LOGN, MLR);
+    static constexpr int TWA = TWN > N ? TWN : N;
     static __host__ __device__ __forceinline__ int swz(int row) { return (row ^ (row >> SH1) ^ (row >> SH2)) & (RPL - 1); }
     static __host__ __device__ __forceinline__ int addr(int row, int c) {
         if constexpr (RPL == 1) {
@@ -201,7 +228,7 @@ struct DftShape {
     }
 };
 
-// One super-stage J.  tw[e] = omega_N^e (prepared twiddle), e < N.
+// One super-stage J.  tw: the stage-ordered twiddle table (prepared twiddles).
 template <class F, class SH, int LOGN, int J, int C, int INV, class Load, class Store>
 __device__ __forceinline__ void super_stage(typename F::T* tile, const typename F::TW* tw, int t, int c,
                                             Load& load, Store& store) {
@@ -213,7 +240,6 @@ __device__ __forceinline__ void super_stage(typename F::T* tile, const typename 
     constexpr int R = 1 << LR;
     constexpr int M = (1 << LS) >> LR;
     constexpr int GROUPS = (1 << LOGN) >> LR;
-    constexpr int TWS = LOGN - LS;  // omega_S = omega_N^(2^TWS)
     constexpr bool FIRST = J == 0, LAST = J == CNT - 1;
     static_assert(GROUPS % SH::TPC == 0, "groups per thread");
 #pragma unroll SS_GROUP_UNROLL
@@ -232,11 +258,9 @@ __device__ __forceinline__ void super_stage(typename F::T* tile, const typename 
         if constexpr (LAST) {
             store.template group<LR>(base, x);  // positions base + k (M == 1)
         } else {
+            const typename F::TW* twg = tw + ss_tw_off(LOGN, J, MLR) + i_lo * R;
 #pragma unroll
-            for (int s = 1; s < R; ++s) {
-                const int e = (i_lo * int(bitrev_ct(unsigned(s), LR))) << TWS;
-                x[s] = F::mul_tw(x[s], tw[e]);
-            }
+            for (int s = 1; s < R; ++s) x[s] = F::mul_tw(x[s], twg[s]);
             const auto r0 = SH::row0(base, c);
 #pragma unroll
             for (int k = 0; k < R; ++k) tile[SH::at(r0, M * k)] = x[k];
