@@ -492,13 +492,22 @@ k_lde_pass2(const LdeJobs<typename F::T> J, int n2, int log_b, const typename F:
         cta_dif<F, SH, LOGN, C, 1>(A, twi, t, c, ld, st);
     }
     const T sqk2 = sq[k2];
+    uint64_t u_prev = 0;
     for (int tc = 0; tc < (1 << log_b); ++tc) {
         const uint64_t u = bitrev_dev(unsigned(tc), log_b);
+        // post[k] = sq[k2] * omega_H^(k2 * (u + bitrev(k) * 2^b)): built from
+        // the root table for the first coset, then moved on to the next coset
+        // by one product with omega_H^(k2 * (u - u_prev)) (each thread owns
+        // the entries it updates; the barrier after the last coset's
+        // transform ended every read)
+        const T step = tc ? roots.omega(logH, uint64_t(k2) * u - uint64_t(k2) * u_prev) : T(0);
         for (int k = tid; k < N; k += NT) {
             pre[k] = gpre ? gpre[tc * N + k]
                           : F::tw_from_const(F::cmul(sp[k], roots.omega(logH, u * uint64_t(N2) * k)));
-            post[k] = F::cmul(sqk2, roots.omega(logH, uint64_t(k2) * (u + (uint64_t(bitrev_dev(k, LOGN)) << log_b))));
+            post[k] = tc ? F::cmul(post[k], step)
+                         : F::cmul(sqk2, roots.omega(logH, uint64_t(k2) * (uint64_t(bitrev_dev(k, LOGN)) << log_b)));
         }
+        u_prev = u;
         __syncthreads();
         PermLoad<F, SH, LOGN> ld{A, pre, c};
         GStore<F, true, T> st{jb.mid + (tc * h + k2) * w + col, N2 * w, post, ok};
