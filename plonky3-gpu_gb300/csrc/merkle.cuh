@@ -106,7 +106,12 @@ __device__ __forceinline__ void hash_group(const Group<typename H::T>& g, uint64
 // injected group's row hashes) are hashed by one persistent kernel: work
 // units of HASH_ROWS rows are handed out through an atomic counter, units of
 // the most expensive groups first, so small groups never leave SMs idle.
-constexpr int HASH_ROWS = 256;  // rows (= threads) per work unit
+// rows (= threads) per work unit (settable at build time, -DP3G_HASH_ROWS=,
+// to compare unit sizes)
+#ifndef P3G_HASH_ROWS
+#define P3G_HASH_ROWS 256
+#endif
+constexpr int HASH_ROWS = P3G_HASH_ROWS;
 
 template <class T>
 struct HashEntry {
