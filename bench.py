@@ -52,7 +52,7 @@ C3_FOLD_LOG = 19
 C1_LOG_H, C1_WIDTH, C1_LOG_B = 20, 256, 1
 # the SM count and SMSPs of a GB300 (the issue bound below)
 SMSPS = 152 * 4
-# batches the end-to-end leg keeps in flight
+# batches the end-to-end leg keeps in flight (default of --e2e-depth)
 E2E_DEPTH = 3
 
 
@@ -677,34 +677,35 @@ def run_ours(args):
 
     # ---- end to end: host-input plans (p3g_plan_commit_host), the traces and
     # the quotient in pinned host memory, copied in by every launch; the root
-    # and the fold output are read back after every step.  E2E_DEPTH plans
+    # and the fold output are read back after every step.  `depth` plans
     # over the same host inputs (their own device copies, LDEs, trees and fold
     # outputs) take turns on as many streams, so later batches' host-to-device
-    # copies overlap the current batch's hashing; the host keeps E2E_DEPTH
+    # copies overlap the current batch's hashing; the host keeps `depth`
     # batches in flight (it reads back step i after enqueuing step
-    # i + E2E_DEPTH - 1).  The serial figure (one batch at a time) is reported
+    # i + depth - 1).  The serial figure (one batch at a time) is reported
     # beside it.
+    depth = args.e2e_depth
     pinned = [pinned_copy(torch, t) for t in traces]
     pin_fold = pinned_copy(torch, fold_in)
     htr = [(pt_.data_ptr(), lh, w, C3_LOG_B, SHIFT) for pt_, (lh, w) in zip(pinned, shapes)]
-    fouts = [d_fout] + [ctx.alloc((1 << (fold_log - 1)) * 16) for _ in range(E2E_DEPTH - 1)]
+    fouts = [d_fout] + [ctx.alloc((1 << (fold_log - 1)) * 16) for _ in range(depth - 1)]
     plans_h = [P.Plan(ctx, P.BABYBEAR, htr, 0, fold=(pin_fold.data_ptr(), fo.ptr, fold_log, 1, beta), n_streams=0,
                       host=True) for fo in fouts]
-    streams_h = [stream] + [torch.cuda.Stream(device=dev) for _ in range(E2E_DEPTH - 1)]
+    streams_h = [stream] + [torch.cuda.Stream(device=dev) for _ in range(depth - 1)]
     root_ptrs = []
     for ph in plans_h:
         nl = len(ph.tree.info()[0])
         root_ptrs.append(ph.tree.layer_ptr(nl - 1))
-    roots = [torch.zeros(8, dtype=torch.int32, pin_memory=True) for _ in range(E2E_DEPTH)]
-    folds = [torch.zeros((1 << (fold_log - 1)) * 4, dtype=torch.int32, pin_memory=True) for _ in range(E2E_DEPTH)]
+    roots = [torch.zeros(8, dtype=torch.int32, pin_memory=True) for _ in range(depth)]
+    folds = [torch.zeros((1 << (fold_log - 1)) * 4, dtype=torch.int32, pin_memory=True) for _ in range(depth)]
     lib = P.load()
 
     def launch(i):
-        j = i % E2E_DEPTH
+        j = i % depth
         plans_h[j].launch(streams_h[j].cuda_stream)
 
     def read(i):  # waits for step i, then copies its root and fold output to the host
-        j = i % E2E_DEPTH
+        j = i % depth
         sp = streams_h[j].cuda_stream
         P.check(lib.p3g_memcpy_d2h(ctx.handle, roots[j].data_ptr(), root_ptrs[j], 32, sp))
         P.check(lib.p3g_memcpy_d2h(ctx.handle, folds[j].data_ptr(), fouts[j].ptr, folds[j].numel() * 4, sp))
@@ -715,15 +716,15 @@ def run_ours(args):
     torch.cuda.synchronize(dev)
     done = []
     t_start = time.perf_counter()
-    for i in range(min(E2E_DEPTH - 1, n_e2e)):
+    for i in range(min(depth - 1, n_e2e)):
         launch(i)
     for i in range(n_e2e):
-        if i + E2E_DEPTH - 1 < n_e2e:
-            launch(i + E2E_DEPTH - 1)
+        if i + depth - 1 < n_e2e:
+            launch(i + depth - 1)
         read(i)
         done.append(time.perf_counter())
     torch.cuda.synchronize(dev)
-    root_h = roots[(n_e2e - 1) % E2E_DEPTH].numpy().view(np.uint32).copy()
+    root_h = roots[(n_e2e - 1) % depth].numpy().view(np.uint32).copy()
     t0_timed = done[args.warmup - 1] if args.warmup > 0 else t_start
     e2e_total_ms = (done[-1] - t0_timed) * 1e3
     e2e_int = [(done[i] - done[i - 1]) * 1e3 for i in range(max(args.warmup, 1), n_e2e)]
@@ -799,8 +800,8 @@ def run_ours(args):
                 "p50_ms": float(np.percentile(e2e_int, 50)), "p99_ms": float(np.percentile(e2e_int, 99)),
                 "intervals_ms": [round(x, 3) for x in e2e_int], "streams": e2e_streams,
                 "call": "p3g_plan_launch of p3g_plan_commit_host plans (64 pinned host traces and the quotient "
-                        f"copied in by the graph every step), root and fold output read back every step; {E2E_DEPTH} "
-                        f"batches in flight on {E2E_DEPTH} streams (p50/p99 over the intervals between step completions)",
+                        f"copied in by the graph every step), root and fold output read back every step; {args.e2e_depth} "
+                        f"batches in flight on {args.e2e_depth} streams (p50/p99 over the intervals between step completions)",
                 "serial": {"value": elems / (statistics.mean(serial_ms) / 1e3), "unit": UNIT,
                            "p50_ms": float(np.percentile(serial_ms, 50)),
                            "p99_ms": float(np.percentile(serial_ms, 99)),
@@ -857,6 +858,8 @@ def main():
     ap.add_argument("--no-prover", action="store_true",
                     help="skip the PCS-open, FRI and proof-of-work measurements (profiling the commit alone)")
     ap.add_argument("--serving-requests", type=int, default=10000, help="requests over the whole rate sweep")
+    ap.add_argument("--e2e-depth", type=int, default=E2E_DEPTH,
+                    help="batches the end-to-end leg keeps in flight (one host-input plan and stream each)")
     ap.add_argument("--c3-shrink", type=int, default=0,
                     help="divide every config-3 height by 2^k (profiling cases)")
     ap.add_argument("--ref-shrink", type=int, default=4,
